@@ -1,0 +1,102 @@
+"""ctypes binding of libemix_gb300.so (the C ABI declared in include/emix_gb300.h).
+
+The library is the product: there is no Python or CPU fallback.  Importing
+this module loads the in-tree shared library and raises if it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libemix_gb300.so"
+
+EMIX_OK = 0
+STATUS_NAMES = {0: "EMIX_OK", 1: "EMIX_ERR_ARG", 2: "EMIX_ERR_CUDA", 3: "EMIX_ERR_ALLOC",
+                4: "EMIX_ERR_UNSUPPORTED", 5: "EMIX_ERR_TIMEOUT"}
+
+dp = C.POINTER(C.c_double)
+vp = C.c_void_p
+i3 = C.c_int * 3
+
+
+class EmixError(RuntimeError):
+    def __init__(self, rc: int, where: str, msg: str):
+        super().__init__(f"{where}: {STATUS_NAMES.get(rc, rc)}: {msg}")
+        self.rc = rc
+
+
+class EmixParams(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("scheme", C.c_int * 3),
+        ("h", C.c_double * 3),
+        ("sgs_model", C.c_int),
+        ("cs", C.c_double), ("amu0", C.c_double), ("c4", C.c_double),
+        ("mach", C.c_double), ("dt", C.c_double),
+        ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes); the order follows include/emix_gb300.h
+PROTOTYPES = {
+    "emix_last_error": (C.c_char_p, []),
+    "emix_version": (C.c_char_p, []),
+    "cudaDeriv": (None, [vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                         C.c_int, C.c_int, C.c_int]),
+    "cuDivergence": (None, [vp] * 9 + [C.c_double] * 3 + [C.c_int] * 3),
+    "emix_set_legacy_scheme": (C.c_int, [C.c_int]),
+    "emix_deriv_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double,
+                                 C.c_int, C.c_int, C.c_int, vp]),
+    "emix_cudaDeriv": (C.c_int, [i3, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                                 C.c_int, C.c_int, C.c_int]),
+    "emix_cudaDeriv_dev": (C.c_int, [i3, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                                     C.c_int, C.c_int, C.c_int, vp]),
+    "emix_cuDivergence": (C.c_int, [i3] + [vp] * 9 + [C.c_double] * 3 + [C.c_int] * 3),
+    "emix_cuDivergence_dev": (C.c_int, [i3] + [vp] * 9 + [C.c_double] * 3 + [C.c_int] * 3 + [vp]),
+    "emix_flux_dev": (C.c_int, [C.c_int] + [vp] * 12 + [C.c_int] * 3 + [vp]),
+    "emix_sgs_setup_dev": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]),
+    "emix_sgs_viscosity_dev": (C.c_int, [C.c_int, C.c_double, C.c_double] + [vp] * 7 +
+                               [C.c_int] * 3 + [vp]),
+    "emix_weno5_advect_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4 + [vp]),
+    "emix_weno5_advect": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4),
+    "emix_ghost_pad_dev": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
+    "emix_ghost_unpad_dev": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
+    "emix_ctx_create": (C.c_int, [C.POINTER(EmixParams), C.POINTER(vp)]),
+    "emix_ctx_destroy": (C.c_int, [vp]),
+    "emix_ctx_set_stream": (C.c_int, [vp, vp]),
+    "emix_ctx_set_static": (C.c_int, [vp, vp, vp, vp]),
+    "emix_ctx_upload": (C.c_int, [vp, vp, vp]),
+    "emix_ctx_download": (C.c_int, [vp, vp, vp]),
+    "emix_ctx_state": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    "emix_step": (C.c_int, [vp, C.c_int, C.c_int]),
+    "emix_step_host": (C.c_int, [vp, vp, vp, C.c_int]),
+    "emix_ctx_launches_per_step": (C.c_int, [vp]),
+    "emix_ctx_device_bytes": (C.c_longlong, [vp]),
+}
+
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Load the library once; raises ``RuntimeError`` if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(p), mode=C.RTLD_GLOBAL)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, where: str):
+    if rc != EMIX_OK:
+        msg = load().emix_last_error()
+        raise EmixError(rc, where, msg.decode() if msg else "")

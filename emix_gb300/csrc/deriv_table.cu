@@ -1,0 +1,236 @@
+// deriv_table.cu -- host-side factor tables of the compact first derivative.
+//
+// Each scheme of the reference is a tridiagonal system  a_i x_{i-1} + b_i x_i
+// + c_i x_{i+1} = r_i  with an explicit right-hand-side stencil.  The
+// reference re-runs the Thomas recurrence for every pencil, one divide per
+// row (src/Schemes/derivCompact.cu:199-212, solver/derivada.f90:111-122).
+// Here the recurrence runs once per (scheme, n, h) on the host and the
+// kernels only do multiply-adds: the pivot 1/bet_i and the 1/h scale are
+// folded into the right-hand-side coefficients.
+//
+// The coefficient tables restate the reference:
+//   A    solver/derivada.f90:22-89 (rows), :104-109 (RHS)
+//   B    src/MSVSingle/derivada_incomp.f90:148-190,209-214 (rows), :306-313 (RHS)
+//   BPER src/MSVSingle/derivada_incomp.f90:192-206 (rows), :231-247 (RHS, cyclic)
+//   C    src/Schemes/derivCompact.cu:90-99 (RHS), :162-190 (rows)
+#include "common.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+namespace emix {
+
+namespace {
+
+struct RowDef {
+    double a, b, c;      // tridiagonal row
+    int kind;            // 0 interior, 1 closure low (f_0..f_3), 2 closure high (f_{n-1}..f_{n-4})
+    double ars, brs;     // interior stencil
+    double cc[4];        // closure stencil
+};
+
+void set_interior(RowDef &r, double a, double c, double ars, double brs) {
+    r.a = a; r.b = 1.0; r.c = c; r.kind = 0; r.ars = ars; r.brs = brs;
+    for (double &v : r.cc) v = 0.0;
+}
+
+void set_closure(RowDef &r, int kind, double a, double c, double c0, double c1, double c2, double c3) {
+    r.a = a; r.b = 1.0; r.c = c; r.kind = kind; r.ars = 0.0; r.brs = 0.0;
+    r.cc[0] = c0; r.cc[1] = c1; r.cc[2] = c2; r.cc[3] = c3;
+}
+
+int define_rows(int scheme, int n, std::vector<RowDef> &R) {
+    R.assign(n, RowDef{});
+    switch (scheme) {
+    case EMIX_SCHEME_A: {
+        const double ars = 3. / 4., ars1 = -17. / 6., brs1 = 3. / 2., crs1 = 1.5, d1 = -1. / 6.;
+        for (int i = 1; i < n - 1; ++i) set_interior(R[i], 1. / 4., 1. / 4., ars, 0.0);
+        set_closure(R[0], 1, 0.0, 3.0, ars1, brs1, crs1, d1);
+        set_closure(R[n - 1], 2, 3.0, 0.0, -ars1, -brs1, -crs1, -d1);
+        // rows 1 and n-2 are interior rows of the reference; written as
+        // closures so that the kernels never read f_{-1} or f_{n}
+        set_closure(R[1], 1, 1. / 4., 1. / 4., -ars, 0.0, ars, 0.0);
+        set_closure(R[n - 2], 2, 1. / 4., 1. / 4., ars, 0.0, -ars, 0.0);
+        return 0;
+    }
+    case EMIX_SCHEME_B: {
+        const double ars = 7. / 9., brs = 1. / 36., ars1 = -2.5, brs1 = 2., crs1 = 0.5, ars2 = 0.75;
+        for (int i = 2; i < n - 2; ++i) set_interior(R[i], 1.0 / 3.0, 1.0 / 3.0, ars, brs);
+        set_closure(R[0], 1, 0.0, 2.0, ars1, brs1, crs1, 0.0);
+        set_closure(R[1], 1, 0.25, 0.25, -ars2, 0.0, ars2, 0.0);
+        set_closure(R[n - 2], 2, 0.25, 0.25, ars2, 0.0, -ars2, 0.0);
+        set_closure(R[n - 1], 2, 2.0, 0.0, -ars1, -brs1, -crs1, 0.0);
+        return 0;
+    }
+    case EMIX_SCHEME_BPER: {
+        const double ars = 7. / 9., brs = 1. / 36.;
+        for (int i = 0; i < n; ++i) set_interior(R[i], 1.0 / 3.0, 1.0 / 3.0, ars, brs);
+        return 0;
+    }
+    case EMIX_SCHEME_C: {
+        const double ars = 14.0 / (9.0 * 2.0), brs = 1.0 / (9.0 * 4.0);
+        const double ars1 = -17.0 / 6.0, brs1 = 3.0 / 2.0, crs1 = 3.0 / 2.0, drs1 = -1.0 / 6.0;
+        const double ars2 = -3.0 / 4.0, crs2 = 3.0 / 4.0;
+        for (int i = 2; i < n - 2; ++i) set_interior(R[i], 1.0 / 3.0, 1.0 / 3.0, ars, brs);
+        set_closure(R[0], 1, 0.0, 3.0, ars1, brs1, crs1, drs1);
+        set_closure(R[1], 1, 1.0 / 4.0, 1.0 / 4.0, ars2, 0.0, crs2, 0.0);
+        set_closure(R[n - 2], 2, 1.0 / 4.0, 1.0 / 4.0, -ars2, 0.0, -crs2, 0.0);
+        set_closure(R[n - 1], 2, 3.0, 0.0, -ars1, -brs1, -crs1, -drs1);
+        return 0;
+    }
+    default:
+        return 1;
+    }
+}
+
+} // namespace
+
+int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow *rows,
+                           double *clo, double *chi, double *u0, double *zz) {
+    if (n < 6 || n > kTableMaxN || !(h > 0.0)) return EMIX_ERR_ARG;
+    std::vector<RowDef> R;
+    if (define_rows(scheme, n, R)) return EMIX_ERR_ARG;
+    const bool per = scheme == EMIX_SCHEME_BPER;
+    const double s = 1.0 / h;
+
+    std::vector<double> bb(n), bet(n), gam(n, 0.0);
+    for (int i = 0; i < n; ++i) bb[i] = R[i].b;
+    double alpha = 0.0, beta = 0.0, gamma = 0.0;
+    if (per) {  // Sherman-Morrison split of the cyclic matrix (derivada_incomp.f90:243-250)
+        alpha = R[0].a;
+        beta = R[n - 1].c;
+        gamma = -R[0].b;
+        bb[0] = R[0].b - gamma;
+        bb[n - 1] = R[n - 1].b - alpha * beta / gamma;
+    }
+    bet[0] = bb[0];
+    for (int i = 1; i < n; ++i) {
+        gam[i] = R[i - 1].c / bet[i - 1];
+        bet[i] = bb[i] - R[i].a * gam[i];
+        if (bet[i] == 0.0 || !std::isfinite(bet[i])) return EMIX_ERR_ARG;
+    }
+
+    t.n = n;
+    t.scheme = scheme;
+    t.periodic = per ? 1 : 0;
+    t.nlo = t.nhi = 0;
+    for (int k = 0; k < kMaxClosure * 4; ++k) clo[k] = chi[k] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double ib = 1.0 / bet[i];
+        DerivRow &r = rows[i];
+        r.A = s * R[i].ars * ib;
+        r.B = s * R[i].brs * ib;
+        r.m = i == 0 ? 0.0 : R[i].a * ib;
+        r.g = i == n - 1 ? 0.0 : gam[i + 1];
+        if (R[i].kind == 1) {
+            if (i != t.nlo || t.nlo >= kMaxClosure) return EMIX_ERR_ARG;
+            for (int q = 0; q < 4; ++q) clo[4 * t.nlo + q] = s * R[i].cc[q] * ib;
+            ++t.nlo;
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        if (R[i].kind != 2) continue;
+        const int k = n - 1 - i;
+        if (k != t.nhi || t.nhi >= kMaxClosure) return EMIX_ERR_ARG;
+        const double ib = 1.0 / bet[i];
+        for (int q = 0; q < 4; ++q) chi[4 * t.nhi + q] = s * R[i].cc[q] * ib;
+        ++t.nhi;
+    }
+
+    t.ku = 0; t.zlo = 0; t.zhi = n; t.sm1 = 0.0; t.sm2 = 0.0;
+    if (per) {
+        // zz = A'^{-1} (gamma, 0, ..., 0, alpha): same forward/backward sweep
+        std::vector<double> w(n);
+        w[0] = gamma / bet[0];
+        for (int i = 1; i < n; ++i) {
+            double ri = (i == n - 1) ? alpha : 0.0;
+            w[i] = (ri - R[i].a * w[i - 1]) / bet[i];
+        }
+        zz[n - 1] = w[n - 1];
+        for (int i = n - 2; i >= 0; --i) zz[i] = w[i] - gam[i + 1] * zz[i + 1];
+        // y_0 = sum_k U0_k w_k with U0_k = prod_{j<k} (-gam_{j+1})
+        double p = 1.0;
+        int ku = 0;
+        while (ku < n && std::fabs(p) > 1e-22) {
+            u0[ku++] = p;
+            if (ku < n) p *= -gam[ku];
+        }
+        t.ku = ku;
+        t.sm1 = beta / gamma;
+        t.sm2 = 1.0 / (1.0 + zz[0] + t.sm1 * zz[n - 1]);
+        double zmax = 0.0;
+        for (int i = 0; i < n; ++i) zmax = std::fmax(zmax, std::fabs(zz[i]));
+        const double thr = 1e-22 * zmax;
+        int zlo = 0;
+        while (zlo < n && std::fabs(zz[zlo]) > thr) ++zlo;
+        int zhi = n;
+        while (zhi > 0 && std::fabs(zz[zhi - 1]) > thr) --zhi;
+        if (zlo >= zhi) { zlo = n; zhi = n; }
+        t.zlo = zlo;
+        t.zhi = zhi;
+    }
+    return EMIX_OK;
+}
+
+namespace {
+
+struct TableKey {
+    int dev, scheme, n;
+    double h;
+    bool operator<(const TableKey &o) const {
+        return std::tie(dev, scheme, n, h) < std::tie(o.dev, o.scheme, o.n, o.h);
+    }
+};
+
+std::mutex g_table_mu;
+std::map<TableKey, DerivTable> g_tables;   // device buffers live until process exit
+
+} // namespace
+
+int get_deriv_table(int scheme, int n, double h, DerivTable *out) {
+    int dev = 0;
+    EMIX_CUDA_TRY(cudaGetDevice(&dev));
+    TableKey key{dev, scheme, n, h};
+    std::lock_guard<std::mutex> lock(g_table_mu);
+    auto it = g_tables.find(key);
+    if (it != g_tables.end()) {
+        *out = it->second;
+        return EMIX_OK;
+    }
+    if (n < 6 || n > kTableMaxN) return EMIX_ERR_ARG;
+    std::vector<DerivRow> rows(n);
+    std::vector<double> clo(kMaxClosure * 4), chi(kMaxClosure * 4), u0(n, 0.0), zz(n, 0.0);
+    DerivTable t{};
+    int rc = build_deriv_table_host(scheme, n, h, t, rows.data(), clo.data(), chi.data(),
+                                    u0.data(), zz.data());
+    if (rc) return rc;
+    // one allocation: rows | clo | chi | u0 | zz
+    const size_t nd = (size_t)4 * n + 8 * kMaxClosure + 2 * (size_t)n;
+    double *buf = nullptr;
+    if (cudaMalloc(&buf, nd * sizeof(double)) != cudaSuccess) {
+        set_last_message("cudaMalloc of a derivative table failed");
+        return EMIX_ERR_ALLOC;
+    }
+    std::vector<double> host(nd);
+    std::memcpy(host.data(), rows.data(), (size_t)n * sizeof(DerivRow));
+    double *p = host.data() + 4 * (size_t)n;
+    std::memcpy(p, clo.data(), 4 * kMaxClosure * sizeof(double));
+    std::memcpy(p + 4 * kMaxClosure, chi.data(), 4 * kMaxClosure * sizeof(double));
+    std::memcpy(p + 8 * kMaxClosure, u0.data(), (size_t)n * sizeof(double));
+    std::memcpy(p + 8 * kMaxClosure + n, zz.data(), (size_t)n * sizeof(double));
+    EMIX_CUDA_TRY(cudaMemcpy(buf, host.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
+    t.rows = reinterpret_cast<const DerivRow *>(buf);
+    t.clo = buf + 4 * (size_t)n;
+    t.chi = t.clo + 4 * kMaxClosure;
+    t.u0 = t.chi + 4 * kMaxClosure;
+    t.zz = t.u0 + n;
+    g_tables[key] = t;
+    *out = t;
+    return EMIX_OK;
+}
+
+} // namespace emix

@@ -1,0 +1,374 @@
+// step.cu -- device-resident RK3 step (solver/rungek_ico.f90:61-313).
+//
+// A context owns every field of one grid in one device allocation.  A step
+// is a fixed sequence of launches on the context stream (optionally replayed
+// from a captured CUDA graph):
+//
+//   prim (u, p from um0) ; pad phi into the ghosted grid
+//   for substep s = 1, 2, 3:
+//     level-set stage s  (WENO5, SSP-RK3 weights of substep s, velocity u^{s-1})
+//     velocity gradients  x, y, z                (cudaDeriv without dT: unused)
+//     SGS viscosity       vis = c4 + amut        (viscosidad_t + viscosidad)
+//     fluxes              15 fields, 5 equations x 3 directions, inviscid+viscous
+//     flux divergence     R_m = d/dxi E_m + d/deta F_m + d/dzeta G_m
+//     RK update + conversions (clip, mask, rebuild um1)
+//
+// The level set is advanced as part of the same SSP-RK3 step (one TVD stage
+// per flow substep, each with the velocity the flow stage uses); with a
+// frozen velocity this is exactly one cuAdvectLsJB step.
+#include "deriv.cuh"
+#include "pointwise.cuh"
+#include "weno.cuh"
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace emix {
+int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
+                 double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st);
+
+__global__ void k_metric_products(const double *__restrict__ jbn, double *__restrict__ jx,
+                                  double *__restrict__ jy, double *__restrict__ jz, long n) {
+    EMIX_FOR_CELLS(q, n) {
+        const double j10 = jbn[9 * n + q];
+        jx[q] = j10 * jbn[q];
+        jy[q] = j10 * jbn[4 * n + q];
+        jz[q] = j10 * jbn[8 * n + q];
+    }
+}
+} // namespace emix
+
+using namespace emix;
+
+struct emix_ctx {
+    emix_params p{};
+    int dev = 0;
+    long n = 0, ng = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own = nullptr;
+    double *arena = nullptr;
+    size_t arena_bytes = 0;
+    double *um0, *um, *u, *pres, *dvel, *vis, *amut, *vort, *flux, *R, *W, *jbn, *jx, *jy, *jz,
+        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB;
+    DerivTable T[3];
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool static_set = false;
+    int launches = 0;
+};
+
+namespace {
+
+int issue_step(emix_ctx *c) {
+    const emix_params &p = c->p;
+    const long n = c->n;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    cudaStream_t st = c->stream;
+    const int gb = cells_grid(n);
+    int launches = 0;
+    int rc;
+    const double inv_m2 = 1.0 / (p.mach * p.mach);
+
+    k_prim<<<gb, 256, 0, st>>>(c->um0, c->u, c->pres, inv_m2, n);
+    ++launches;
+    if (p.level_set) {
+        const long ngc = c->ng;
+        k_ghost_pad<<<cells_grid(ngc), 256, 0, st>>>(c->phig0, c->phi, p.ls_ghost, 1.0, nx, ny, nz);
+        ++launches;
+    }
+    EMIX_CUDA_TRY(cudaGetLastError());
+
+    for (int s = 1; s <= 3; ++s) {
+        const double *umcur = s == 1 ? c->um0 : c->um;
+        if (p.level_set) {
+            WenoArgs a{};
+            const int g = p.ls_ghost;
+            a.phi = s == 1 ? c->phig0 : (s == 2 ? c->phigA : c->phigB);
+            a.phi0 = c->phig0;
+            a.out = s == 1 ? c->phigA : (s == 2 ? c->phigB : c->phi);
+            a.out_interior = s == 3 ? 1 : 0;
+            a.vel = c->u;
+            a.jbn = c->jbn;
+            a.reflect = 1;
+            a.nxg = nx + 2 * g; a.nyg = ny + 2 * g; a.nzg = nz + 2 * g; a.g = g;
+            a.sx = 1.0 / p.h[0]; a.sy = 1.0 / p.h[1]; a.sz = 1.0 / p.h[2];
+            a.dt = p.dt; a.stage = s; a.ref_bugs = p.ref_bugs;
+            if ((rc = launch_weno_stage(a, st))) return rc;
+            ++launches;
+        }
+        // velocity gradients (cudaDeriv; dT/dx_i feeds nothing on this path:
+        // the m=5 viscous fluxes are zero, flujos_compact.f90:187-214)
+        for (int ax = 0; ax < 3; ++ax) {
+            const double *in[3] = {c->u, c->u + n, c->u + 2 * n};
+            double *out[3] = {c->dvel + 3 * ax * n, c->dvel + (3 * ax + 1) * n, c->dvel + (3 * ax + 2) * n};
+            if ((rc = launch_deriv(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, st))) return rc;
+            ++launches;
+        }
+        // SGS viscosity
+        if (p.sgs_model == EMIX_SGS_STRUCTURE) {
+            k_sgs_sf<<<gb, 256, 0, st>>>(c->u, c->ratios, c->dxyz, p.amu0, c->amut, nx, ny, nz);
+            k_vort<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->vort, n);
+            const double cutoff = cos(20.0 * atan(1.0) / 45.0);
+            k_selective<<<gb, 256, 0, st>>>(c->vort, c->amut, c->vis, cutoff, p.c4, nx, ny, nz);
+            launches += 3;
+        } else {
+            k_sgs_smag<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->dxyz,
+                                           p.sgs_model == EMIX_SGS_NONE ? 0.0 : p.cs, p.c4, nullptr,
+                                           c->vis, n);
+            ++launches;
+        }
+        // fluxes
+        FluxArgs fa{};
+        for (int q = 0; q < 15; ++q) fa.F[q] = c->flux + q * n;
+        fa.um = umcur; fa.u = c->u; fa.pres = c->pres; fa.dvel = c->dvel; fa.vis = c->vis;
+        fa.jbn = c->jbn; fa.jx = c->jx; fa.jy = c->jy; fa.jz = c->jz; fa.n = n;
+        k_flux_all<<<gb, 256, 0, st>>>(fa);
+        ++launches;
+        EMIX_CUDA_TRY(cudaGetLastError());
+        // divergence: R_m = sum over directions of the compact derivative
+        for (int ax = 0; ax < 3; ++ax) {
+            const double *in[5];
+            double *out[5], *wb[5];
+            for (int m = 0; m < 5; ++m) {
+                in[m] = c->flux + (3 * m + ax) * n;
+                out[m] = c->R + m * n;
+                wb[m] = c->W + m * n;
+            }
+            if (ax == 0)
+                rc = launch_deriv(c->T[ax], ax, EPI_STORE, 5, in, out, out, nx, ny, nz, st);
+            else
+                rc = launch_deriv(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, st);
+            if (rc) return rc;
+            ++launches;
+        }
+        // RK update and conversions
+        RkArgs ra{};
+        ra.R = c->R; ra.um0 = c->um0; ra.um = c->um;
+        ra.out = s == 3 ? c->um0 : c->um;
+        ra.u = c->u; ra.pres = c->pres; ra.jbn = c->jbn; ra.mask = c->mask;
+        ra.dt = p.dt; ra.mach = p.mach; ra.inv_m2 = inv_m2; ra.stage = s; ra.n = n;
+        k_rk_post<<<gb, 256, 0, st>>>(ra);
+        ++launches;
+        EMIX_CUDA_TRY(cudaGetLastError());
+    }
+    c->launches = launches;
+    return EMIX_OK;
+}
+
+bool params_ok(const emix_params *p) {
+    if (!p) return false;
+    if (p->nx < 6 || p->ny < 6 || p->nz < 6 || p->nx > kTableMaxN || p->ny > kTableMaxN ||
+        p->nz > kTableMaxN || p->ny > 65535 || p->nz > 65535)
+        return false;
+    for (int a = 0; a < 3; ++a) {
+        if (p->scheme[a] < EMIX_SCHEME_A || p->scheme[a] > EMIX_SCHEME_C) return false;
+        if (!(p->h[a] > 0.0)) return false;
+    }
+    if (p->sgs_model < EMIX_SGS_NONE || p->sgs_model > EMIX_SGS_STRUCTURE) return false;
+    if (!(p->mach > 0.0) || !(p->dt > 0.0)) return false;
+    if (p->level_set && (p->ls_ghost < 3 || p->ls_ghost > p->nx || p->ls_ghost > p->ny ||
+                         p->ls_ghost > p->nz))
+        return false;
+    return true;
+}
+
+void drop_graph(emix_ctx *c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+}
+
+} // namespace
+
+extern "C" {
+
+int emix_ctx_create(const emix_params *p, emix_ctx **out) {
+    if (!out || !params_ok(p)) return EMIX_ERR_ARG;
+    *out = nullptr;
+    emix_ctx *c = new (std::nothrow) emix_ctx();
+    if (!c) return EMIX_ERR_ALLOC;
+    c->p = *p;
+    EMIX_CUDA_TRY(cudaGetDevice(&c->dev));
+    const long n = (long)ncell(p->nx, p->ny, p->nz);
+    const int g = p->level_set ? p->ls_ghost : 0;
+    const long ng = p->level_set ? (long)(p->nx + 2 * g) * (p->ny + 2 * g) * (p->nz + 2 * g) : 0;
+    c->n = n;
+    c->ng = ng;
+    const int dims[3] = {p->nx, p->ny, p->nz};
+    for (int a = 0; a < 3; ++a) {
+        int rc = get_deriv_table(p->scheme[a], dims[a], p->h[a], &c->T[a]);
+        if (rc) { delete c; return rc; }
+    }
+    const bool sf = p->sgs_model == EMIX_SGS_STRUCTURE;
+    const long nfield = 5 + 5 + 3 + 1 + 9 + 1 + 15 + 5 + 5 + 11 + 3 + 1 + 1 + (p->level_set ? 1 : 0) +
+                        (sf ? 1 + 3 + 6 : 0);
+    const size_t bytes = ((size_t)nfield * n + 3 * (size_t)ng) * sizeof(double);
+    if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_message("cudaMalloc of the context arena failed");
+        delete c;
+        return EMIX_ERR_ALLOC;
+    }
+    c->arena_bytes = bytes;
+    double *q = c->arena;
+    auto take = [&](long cnt) { double *r = q; q += cnt; return r; };
+    c->um0 = take(5 * n); c->um = take(5 * n); c->u = take(3 * n); c->pres = take(n);
+    c->dvel = take(9 * n); c->vis = take(n); c->flux = take(15 * n); c->R = take(5 * n);
+    c->W = take(5 * n); c->jbn = take(11 * n); c->jx = take(n); c->jy = take(n); c->jz = take(n);
+    c->mask = take(n); c->dxyz = take(n);
+    c->phi = p->level_set ? take(n) : nullptr;
+    c->amut = sf ? take(n) : nullptr;
+    c->vort = sf ? take(3 * n) : nullptr;
+    c->ratios = sf ? take(6 * n) : nullptr;
+    c->phig0 = p->level_set ? take(ng) : nullptr;
+    c->phigA = p->level_set ? take(ng) : nullptr;
+    c->phigB = p->level_set ? take(ng) : nullptr;
+    if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(c->arena);
+        delete c;
+        set_last_message("cudaStreamCreate failed");
+        return EMIX_ERR_CUDA;
+    }
+    c->stream = c->own;
+    if (cudaMemsetAsync(c->arena, 0, bytes, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(c->own);
+        cudaFree(c->arena);
+        delete c;
+        set_last_message("clearing the context arena failed");
+        return EMIX_ERR_CUDA;
+    }
+    *out = c;
+    return EMIX_OK;
+}
+
+int emix_ctx_destroy(emix_ctx *c) {
+    if (!c) return EMIX_ERR_ARG;
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    if (c->own) cudaStreamDestroy(c->own);
+    cudaFree(c->arena);
+    delete c;
+    return EMIX_OK;
+}
+
+int emix_ctx_set_stream(emix_ctx *c, void *stream) {
+    if (!c) return EMIX_ERR_ARG;
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    drop_graph(c);
+    return EMIX_OK;
+}
+
+int emix_ctx_set_static(emix_ctx *c, const double *jbn, const double *mask, const double *xyz) {
+    if (!c || !jbn || !mask || !xyz) return EMIX_ERR_ARG;
+    const long n = c->n;
+    const emix_params &p = c->p;
+    cudaStream_t st = c->stream;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->jbn, jbn, 11 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->mask, mask, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    // coordinates go through the flux buffer (free at this point)
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->flux, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    double *ratios = c->ratios ? c->ratios : c->flux + 3 * n;
+    k_sgs_setup<<<cells_grid(n), 256, 0, st>>>(c->flux, c->dxyz, ratios, p.nx, p.ny, p.nz);
+    k_metric_products<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->jx, c->jy, c->jz, n);
+    EMIX_CUDA_TRY(cudaGetLastError());
+    EMIX_CUDA_TRY(cudaStreamSynchronize(st));
+    c->static_set = true;
+    return EMIX_OK;
+}
+
+int emix_ctx_upload(emix_ctx *c, const double *um, const double *phi) {
+    if (!c || !um) return EMIX_ERR_ARG;
+    const long n = c->n;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->p.level_set) {
+        if (!phi) return EMIX_ERR_ARG;
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return EMIX_OK;
+}
+
+int emix_ctx_download(emix_ctx *c, double *um, double *phi) {
+    if (!c || !um) return EMIX_ERR_ARG;
+    const long n = c->n;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(um, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (c->p.level_set && phi)
+        EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return EMIX_OK;
+}
+
+int emix_ctx_state(emix_ctx *c, double **um, double **phi) {
+    if (!c) return EMIX_ERR_ARG;
+    if (um) *um = c->um0;
+    if (phi) *phi = c->phi;
+    return EMIX_OK;
+}
+
+int emix_step(emix_ctx *c, int nsteps, int use_graph) {
+    if (!c || nsteps < 0) return EMIX_ERR_ARG;
+    if (!c->static_set) {
+        set_last_message("emix_step: static fields not set (emix_ctx_set_static)");
+        return EMIX_ERR_ARG;
+    }
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; ++s) {
+            int rc = issue_step(c);
+            if (rc) return rc;
+        }
+        return EMIX_OK;
+    }
+    if (!c->gexec) {
+        EMIX_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = issue_step(c);
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+        if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+        if (e != cudaSuccess) { set_last_error(e, "cudaStreamEndCapture", __FILE__, __LINE__); return EMIX_ERR_CUDA; }
+        c->graph = gr;
+        e = cudaGraphInstantiate(&c->gexec, gr, 0);
+        if (e != cudaSuccess) {
+            drop_graph(c);
+            set_last_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+            return EMIX_ERR_CUDA;
+        }
+    }
+    for (int s = 0; s < nsteps; ++s) EMIX_CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+    return EMIX_OK;
+}
+
+int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
+    if (!c || !um || nsteps < 0) return EMIX_ERR_ARG;
+    if (c->p.level_set && !phi) return EMIX_ERR_ARG;
+    const long n = c->n;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->p.level_set)
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = emix_step(c, nsteps, 1);
+    if (rc) return rc;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(um, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (c->p.level_set)
+        EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return EMIX_OK;
+}
+
+int emix_ctx_launches_per_step(emix_ctx *c) {
+    if (!c) return -1;
+    if (c->launches == 0) {
+        // count without launching: 2 + 3*(ls + 3 + sgs + 1 + 3 + 1)
+        const int ls = c->p.level_set ? 1 : 0;
+        const int sgs = c->p.sgs_model == EMIX_SGS_STRUCTURE ? 3 : 1;
+        return 1 + ls + 3 * (ls + 3 + sgs + 1 + 3 + 1);
+    }
+    return c->launches;
+}
+
+long long emix_ctx_device_bytes(emix_ctx *c) { return c ? (long long)c->arena_bytes : -1; }
+
+} // extern "C"

@@ -1,0 +1,308 @@
+"""Python mirror of the reference's operator interface over the C ABI.
+
+Function names and argument meaning follow the reference's Fortran -> C
+boundary (``cudaDeriv``, ``cuDivergence``; solver/deriv_vel_cuda.f90:19-39,
+solver/divergencia_cuda.f90:21-42) and its level-set driver
+(``cuAdvectLsJB``, src/LevelSet/lsTransportEc.cu:201-418).  Host arrays are
+numpy float64, C-ordered as ``(ncomp, nz, ny, nx)`` -- the same bytes as the
+Fortran ``(nx, ny, nz, ncomp)`` arrays.  Device forms take torch CUDA tensors
+and launch on torch's current stream.  Errors raise :class:`EmixError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import EmixError, EmixParams, check, i3  # noqa: F401
+from .fields import SCHEME_A, SCHEME_B, SCHEME_BPER, SCHEME_C  # noqa: F401
+
+SGS_NONE, SGS_SMAGORINSKY, SGS_STRUCTURE = 0, 1, 2
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous float64")
+        return a.ctypes.data
+    if a is None:
+        return None
+    # torch tensor
+    if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
+        raise ValueError("tensors must be contiguous float64")
+    return a.data_ptr()
+
+
+def _stream():
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dims(a):
+    nz, ny, nx = a.shape[-3:]
+    return nx, ny, nz
+
+
+def _schemes(s):
+    if isinstance(s, int):
+        s = (s, s, s)
+    return i3(*s)
+
+
+# --------------------------------------------------------------------------
+# host-pointer forms
+# --------------------------------------------------------------------------
+def cudaDeriv(vel: np.ndarray, temp: np.ndarray, h, schemes=SCHEME_C):
+    """Velocity and temperature gradients in computational coordinates.
+
+    vel (3, nz, ny, nx), temp (nz, ny, nx), h = (hx, hy, hz).  Returns
+    dvel (9, ...) ordered d/dx(u,v,w), d/dy(u,v,w), d/dz(u,v,w) and
+    dtemp (3, ...), as solver/cuDeriv.cu:629-644."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(temp)
+    dvel = np.empty((9, nz, ny, nx))
+    dtemp = np.empty((3, nz, ny, nx))
+    rc = lib.emix_cudaDeriv(_schemes(schemes), _ptr(dvel), _ptr(dtemp), _ptr(vel), _ptr(temp),
+                            h[0], h[1], h[2], nx, ny, nz)
+    check(rc, "emix_cudaDeriv")
+    return dvel, dtemp
+
+
+def cudaDeriv_legacy(dvel, dtemp, vel, temp, amut, dxyzsgd, jbn, dx, dy, dz, nx, ny, nz):
+    """The reference symbol itself (void, prints on error)."""
+    lib = _lib.load()
+    lib.cudaDeriv(_ptr(dvel), _ptr(dtemp), _ptr(vel), _ptr(temp), _ptr(amut), _ptr(dxyzsgd),
+                  _ptr(jbn), dx, dy, dz, nx, ny, nz)
+
+
+def cuDivergence(e, f, g, ev, fv, gv, jbn, h, schemes=SCHEME_C):
+    """rs, rsv of solver/cuDivergence.cu:107-189 (host arrays)."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(e)
+    rs = np.empty((nz, ny, nx))
+    rsv = np.empty((nz, ny, nx))
+    rc = lib.emix_cuDivergence(_schemes(schemes), _ptr(rs), _ptr(rsv), _ptr(e), _ptr(f), _ptr(g),
+                               _ptr(ev), _ptr(fv), _ptr(gv), _ptr(jbn), h[0], h[1], h[2],
+                               nx, ny, nz)
+    check(rc, "emix_cuDivergence")
+    return rs, rsv
+
+
+def cuDivergence_legacy(rs, rsv, e, f, g, ev, fv, gv, jbn, dx, dy, dz, nx, ny, nz):
+    lib = _lib.load()
+    lib.cuDivergence(_ptr(rs), _ptr(rsv), _ptr(e), _ptr(f), _ptr(g), _ptr(ev), _ptr(fv),
+                     _ptr(gv), _ptr(jbn), dx, dy, dz, nx, ny, nz)
+
+
+def set_legacy_scheme(scheme: int):
+    check(_lib.load().emix_set_legacy_scheme(scheme), "emix_set_legacy_scheme")
+
+
+def weno5_advect(phi: np.ndarray, vel: np.ndarray, jbn: np.ndarray, h, dt: float,
+                 ref_bugs: int = 0) -> np.ndarray:
+    """One WENO5 TVD-RK3 step on ghost-padded host arrays (cuAdvectLsJB).
+    Returns the new phi; the input is not modified."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(phi)
+    out = np.array(phi, dtype=np.float64, copy=True, order="C")
+    rc = lib.emix_weno5_advect(_ptr(out), _ptr(vel), _ptr(jbn), h[0], h[1], h[2], dt,
+                               nx, ny, nz, ref_bugs)
+    check(rc, "emix_weno5_advect")
+    return out
+
+
+# --------------------------------------------------------------------------
+# device forms (torch tensors)
+# --------------------------------------------------------------------------
+def deriv_dev(x, axis: int, h: float, scheme=SCHEME_C):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(x)
+    nf = 1 if x.dim() == 3 else x.shape[0]
+    out = torch.empty_like(x)
+    check(lib.emix_deriv_dev(scheme, axis, nf, _ptr(out), _ptr(x), h, nx, ny, nz, _stream()),
+          "emix_deriv_dev")
+    return out
+
+
+def cudaDeriv_dev(vel, temp, h, schemes=SCHEME_C):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(vel)
+    dvel = torch.empty((9, nz, ny, nx), dtype=torch.float64, device=vel.device)
+    dtemp = None if temp is None else torch.empty((3, nz, ny, nx), dtype=torch.float64,
+                                                  device=vel.device)
+    check(lib.emix_cudaDeriv_dev(_schemes(schemes), _ptr(dvel), _ptr(dtemp), _ptr(vel),
+                                 _ptr(temp), h[0], h[1], h[2], nx, ny, nz, _stream()),
+          "emix_cudaDeriv_dev")
+    return dvel, dtemp
+
+
+def cuDivergence_dev(e, f, g, ev, fv, gv, jbn, h, schemes=SCHEME_C):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(e)
+    rs = torch.empty_like(e)
+    rsv = torch.empty_like(e)
+    check(lib.emix_cuDivergence_dev(_schemes(schemes), _ptr(rs), _ptr(rsv), _ptr(e), _ptr(f),
+                                    _ptr(g), _ptr(ev), _ptr(fv), _ptr(gv), _ptr(jbn),
+                                    h[0], h[1], h[2], nx, ny, nz, _stream()),
+          "emix_cuDivergence_dev")
+    return rs, rsv
+
+
+def flux_dev(neq, um, u, pres, dvel, jbn, vis):
+    """flujos(neq): returns (e, f, g, ev, fv, gv) as device tensors."""
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(pres)
+    out = [torch.empty_like(pres) for _ in range(6)]
+    check(lib.emix_flux_dev(neq, *[_ptr(o) for o in out], _ptr(um), _ptr(u), _ptr(pres),
+                            _ptr(dvel), _ptr(jbn), _ptr(vis), nx, ny, nz, _stream()),
+          "emix_flux_dev")
+    return tuple(out)
+
+
+def sgs_setup_dev(xyz):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(xyz)
+    dxyz = torch.empty(xyz.shape[1:], dtype=torch.float64, device=xyz.device)
+    ratios = torch.empty((6,) + tuple(xyz.shape[1:]), dtype=torch.float64, device=xyz.device)
+    check(lib.emix_sgs_setup_dev(_ptr(xyz), _ptr(dxyz), _ptr(ratios), nx, ny, nz, _stream()),
+          "emix_sgs_setup_dev")
+    return dxyz, ratios
+
+
+def sgs_viscosity_dev(model, coef, c4, u, dvel, jbn, dxyzsgd, ratios=None):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(dxyzsgd)
+    amut = torch.empty_like(dxyzsgd)
+    vis = torch.empty_like(dxyzsgd)
+    check(lib.emix_sgs_viscosity_dev(model, coef, c4, _ptr(u), _ptr(dvel), _ptr(jbn),
+                                     _ptr(dxyzsgd), _ptr(ratios), _ptr(amut), _ptr(vis),
+                                     nx, ny, nz, _stream()),
+          "emix_sgs_viscosity_dev")
+    return amut, vis
+
+
+def weno5_advect_dev(phi, vel, jbn, h, dt, ref_bugs=0):
+    """In-place WENO5 TVD-RK3 step on padded device tensors."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(phi)
+    check(lib.emix_weno5_advect_dev(_ptr(phi), _ptr(vel), _ptr(jbn), h[0], h[1], h[2], dt,
+                                    nx, ny, nz, ref_bugs, _stream()),
+          "emix_weno5_advect_dev")
+    return phi
+
+
+def ghost_pad_dev(val, g, direction=1.0):
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(val)
+    out = torch.empty((nz + 2 * g, ny + 2 * g, nx + 2 * g), dtype=torch.float64, device=val.device)
+    check(lib.emix_ghost_pad_dev(_ptr(out), _ptr(val), g, direction, nx, ny, nz, _stream()),
+          "emix_ghost_pad_dev")
+    return out
+
+
+def ghost_unpad_dev(ghost, g):
+    import torch
+    lib = _lib.load()
+    nzg, nyg, nxg = ghost.shape
+    nx, ny, nz = nxg - 2 * g, nyg - 2 * g, nzg - 2 * g
+    out = torch.empty((nz, ny, nx), dtype=torch.float64, device=ghost.device)
+    check(lib.emix_ghost_unpad_dev(_ptr(out), _ptr(ghost), g, nx, ny, nz, _stream()),
+          "emix_ghost_unpad_dev")
+    return out
+
+
+# --------------------------------------------------------------------------
+# device-resident RK3 step
+# --------------------------------------------------------------------------
+class Context:
+    """One grid resident in device memory; wraps ``emix_ctx``."""
+
+    def __init__(self, workload=None, *, params: EmixParams | None = None, level_set=True,
+                 ref_bugs=0, ls_ghost=5):
+        lib = _lib.load()
+        if params is None:
+            w = workload
+            g = w.grid
+            params = EmixParams()
+            params.nx, params.ny, params.nz = g.nx, g.ny, g.nz
+            for a in range(3):
+                params.scheme[a] = w.schemes[a]
+                params.h[a] = g.h(a)
+            params.sgs_model = w.sgs_model
+            params.cs = w.cs
+            params.amu0 = w.amu0
+            params.c4 = 1.0 / w.reynolds
+            params.mach = w.mach
+            params.dt = w.dt
+            params.level_set = 1 if level_set else 0
+            params.ls_ghost = ls_ghost
+            params.ref_bugs = ref_bugs
+        self.params = params
+        self._h = C.c_void_p()
+        check(lib.emix_ctx_create(C.byref(params), C.byref(self._h)), "emix_ctx_create")
+        self.lib = lib
+        if workload is not None:
+            self.set_static(workload.jbn, workload.mask, workload.grid.coords())
+            self.upload(workload.um, workload.phi if level_set else None)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self.lib.emix_ctx_set_stream(self._h, C.c_void_p(stream_ptr)), "emix_ctx_set_stream")
+
+    def set_static(self, jbn, mask, xyz):
+        jbn = np.ascontiguousarray(jbn, dtype=np.float64)
+        mask = np.ascontiguousarray(mask, dtype=np.float64)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        check(self.lib.emix_ctx_set_static(self._h, _ptr(jbn), _ptr(mask), _ptr(xyz)),
+              "emix_ctx_set_static")
+
+    def upload(self, um, phi=None):
+        um = np.ascontiguousarray(um, dtype=np.float64)
+        phi = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
+        check(self.lib.emix_ctx_upload(self._h, _ptr(um), _ptr(phi)), "emix_ctx_upload")
+
+    def download(self):
+        p = self.params
+        um = np.empty((5, p.nz, p.ny, p.nx))
+        phi = np.empty((p.nz, p.ny, p.nx)) if p.level_set else None
+        check(self.lib.emix_ctx_download(self._h, _ptr(um), _ptr(phi)), "emix_ctx_download")
+        return um, phi
+
+    def state_ptrs(self):
+        a, b = C.c_void_p(), C.c_void_p()
+        check(self.lib.emix_ctx_state(self._h, C.byref(a), C.byref(b)), "emix_ctx_state")
+        return a.value, b.value
+
+    def step(self, nsteps=1, use_graph=False):
+        check(self.lib.emix_step(self._h, nsteps, 1 if use_graph else 0), "emix_step")
+
+    def step_host(self, um, phi, nsteps=1):
+        check(self.lib.emix_step_host(self._h, _ptr(um), _ptr(phi), nsteps), "emix_step_host")
+
+    def launches_per_step(self):
+        return self.lib.emix_ctx_launches_per_step(self._h)
+
+    def device_bytes(self):
+        return self.lib.emix_ctx_device_bytes(self._h)
+
+    def close(self):
+        if self._h:
+            self.lib.emix_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,230 @@
+/*
+ * emix_gb300.h -- C ABI of the GB300-native eMix3d hot path.
+ *
+ * The library (libemix_gb300.so) replaces the CUDA side of the reference's
+ * Fortran -> C boundary.  Plain pointers and sizes only; no C++ or torch
+ * types.  Fields are Fortran column-major (i fastest, index
+ * i + nx*(j + ny*k)); multi-component arrays stack components with stride
+ * nx*ny*nz.  All arithmetic is IEEE FP64.
+ *
+ * Two families of entry points:
+ *   - the reference's own symbols (cudaDeriv, cuDivergence) with byte-identical
+ *     signatures: host pointers, synchronous, void return; on error they print
+ *     a message and return (they never exit or trap);
+ *   - emix_* functions that return an int status (EMIX_OK == 0) and come in
+ *     host-pointer and device-pointer ("_dev") forms.
+ *
+ * Every entry point runs on the calling thread's current CUDA device.
+ */
+#ifndef EMIX_GB300_H
+#define EMIX_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    EMIX_OK = 0,
+    EMIX_ERR_ARG = 1,          /* bad size, null pointer, unknown option      */
+    EMIX_ERR_CUDA = 2,         /* a CUDA runtime call failed                  */
+    EMIX_ERR_ALLOC = 3,        /* device or pinned allocation failed          */
+    EMIX_ERR_UNSUPPORTED = 4,  /* option not built                            */
+    EMIX_ERR_TIMEOUT = 5       /* a bounded device wait gave up               */
+};
+
+/* ---- compact first-derivative schemes ----------------------------------- */
+enum {
+    EMIX_SCHEME_A = 0,     /* Pade-4 interior, alpha_1 = 3 closure: solver/derivada.f90:2-125           */
+    EMIX_SCHEME_B = 1,     /* Lele-6 interior, 3rd/4th-order closure: src/MSVSingle/derivada_incomp.f90:130-218,297-329 */
+    EMIX_SCHEME_BPER = 2,  /* cyclic Lele-6 (Sherman-Morrison): src/MSVSingle/derivada_incomp.f90:221-294 */
+    EMIX_SCHEME_C = 3      /* Lele-6 interior, alpha_1 = 3 closure: src/Schemes/derivCompact.cu:81-215 */
+};
+
+/* ---- SGS models --------------------------------------------------------- */
+enum {
+    EMIX_SGS_NONE = 0,
+    EMIX_SGS_SMAGORINSKY = 1,   /* nu_t = (Cs*Delta)^2 sqrt(2 S_ij S_ij); not in the reference        */
+    EMIX_SGS_STRUCTURE = 2      /* selective structure function: solver/sgdm_incomp.f90:117-395      */
+};
+
+/* Message describing the last error on the calling thread ("" if none). */
+const char *emix_last_error(void);
+
+/* Library version string. */
+const char *emix_version(void);
+
+/* ========================================================================
+ * Reference symbols (drop-in)
+ * ======================================================================== */
+
+/* Replaces cudaDeriv, solver/cuDeriv.cu:529-539 (Fortran interface
+ * solver/deriv_vel_cuda.f90:19-39).  Outputs dVel[9] in the order d/dx(u,v,w),
+ * d/dy(u,v,w), d/dz(u,v,w) and dTemp[3] = dT/dx, dT/dy, dT/dz, in
+ * computational coordinates.  deltaX/Y/Z are the grid spacings h (the
+ * kernel scales by 1/h).  amut, dxyzsgd and jbn are accepted and unused, as in
+ * the reference.  Scheme: the one set by emix_set_legacy_scheme (default
+ * EMIX_SCHEME_C, the reference's production GPU scheme). */
+void cudaDeriv(double *dVel, double *dTemp, double *vel, double *temp,
+               double *amut, double *dxyzsgd, double *jbn,
+               double deltaX, double deltaY, double deltaZ,
+               int Nx, int Ny, int Nz);
+
+/* Replaces cuDivergence, solver/cuDivergence.cu:107-119 (Fortran interface
+ * solver/divergencia_cuda.f90:21-42).  rs  = jbn11*(d/dxi(jbn10*jbn1*e) +
+ * d/deta(jbn10*jbn5*f) + d/dzeta(jbn10*jbn9*g)), rsv the same for ev,fv,gv.
+ * jbn holds 11 components; the inputs are not modified. */
+void cuDivergence(double *rs, double *rsv, double *e, double *f, double *g,
+                  double *ev, double *fv, double *gv, double *jbn,
+                  double deltaX, double deltaY, double deltaZ,
+                  int Nx, int Ny, int Nz);
+
+/* Scheme used by the two symbols above (EMIX_SCHEME_*).  Returns status. */
+int emix_set_legacy_scheme(int scheme);
+
+/* ========================================================================
+ * Status-returning operators
+ * ======================================================================== */
+
+/* Compact derivative of nf fields along axis (0=x, 1=y, 2=z), device
+ * pointers.  in and out hold nf fields each (stride nx*ny*nz) and must not
+ * overlap.  Replaces cu::cs::dFdX/dFdY/dFdZ, src/Schemes/derivCompact.cu:222-409,
+ * generalised to every scheme of the reference. */
+int emix_deriv_dev(int scheme, int axis, int nf, double *out, const double *in,
+                   double h, int nx, int ny, int nz, void *stream);
+
+/* cudaDeriv with status, explicit per-axis schemes, host pointers. */
+int emix_cudaDeriv(const int schemes[3], double *dVel, double *dTemp,
+                   const double *vel, const double *temp,
+                   double hx, double hy, double hz, int nx, int ny, int nz);
+
+/* Same, device pointers, asynchronous on stream.  dTemp/temp may be NULL
+ * (the temperature derivatives are then skipped). */
+int emix_cudaDeriv_dev(const int schemes[3], double *dVel, double *dTemp,
+                       const double *vel, const double *temp,
+                       double hx, double hy, double hz, int nx, int ny, int nz,
+                       void *stream);
+
+/* cuDivergence with status, explicit schemes, host pointers. */
+int emix_cuDivergence(const int schemes[3], double *rs, double *rsv,
+                      const double *e, const double *f, const double *g,
+                      const double *ev, const double *fv, const double *gv,
+                      const double *jbn, double hx, double hy, double hz,
+                      int nx, int ny, int nz);
+
+/* Same, device pointers. */
+int emix_cuDivergence_dev(const int schemes[3], double *rs, double *rsv,
+                          const double *e, const double *f, const double *g,
+                          const double *ev, const double *fv, const double *gv,
+                          const double *jbn, double hx, double hy, double hz,
+                          int nx, int ny, int nz, void *stream);
+
+/* flujos(neq), solver/flujos_compact.f90:1-220: inviscid and viscous fluxes
+ * of equation neq (1..5) into e,f,g,ev,fv,gv.  um[5], u[3], pres, dvel[9],
+ * jbn[11], vis.  Device pointers. */
+int emix_flux_dev(int neq, double *e, double *f, double *g,
+                  double *ev, double *fv, double *gv,
+                  const double *um, const double *u, const double *pres,
+                  const double *dvel, const double *jbn, const double *vis,
+                  int nx, int ny, int nz, void *stream);
+
+/* INISGDM, solver/sgdm_incomp.f90:2-114: filter width dxyzsgd and the six
+ * spacing ratios (order xp, xm, yp, ym, zp, zm) from grid coordinates
+ * xyz[3].  Device pointers. */
+int emix_sgs_setup_dev(const double *xyz, double *dxyzsgd, double *ratios,
+                       int nx, int ny, int nz, void *stream);
+
+/* viscosidad_t + viscosidad (solver/sgdm_incomp.f90:117-162,
+ * src/MSVSingle/viscosidad_incomp.f90:12-20): eddy viscosity amut and
+ * vis = c4 + amut.  model = EMIX_SGS_*; coef = Cs (Smagorinsky) or amu0
+ * (structure function).  u[3], dvel[9], jbn[11], dxyzsgd, ratios[6] (only
+ * read by the structure-function model).  amut may be NULL.  Device
+ * pointers. */
+int emix_sgs_viscosity_dev(int model, double coef, double c4,
+                           const double *u, const double *dvel, const double *jbn,
+                           const double *dxyzsgd, const double *ratios,
+                           double *amut, double *vis,
+                           int nx, int ny, int nz, void *stream);
+
+/* One WENO5 TVD-RK3 step of phi_t + vel . grad(phi) = 0 on ghost-padded
+ * arrays, as cuAdvectLsJB (src/LevelSet/lsTransportEc.cu:201-418): phi
+ * (nxg*nyg*nzg, updated in place), vel[3] and jbn[11] (components 0, 4 and 8
+ * read) all on the padded grid; hx,hy,hz are the spacings h.  ref_bugs = 1
+ * keeps the reference's z-top neighbour index (lsTools.cu:636).  Device
+ * pointers; the scratch (three padded fields) is allocated per call. */
+int emix_weno5_advect_dev(double *phi, const double *vel, const double *jbn,
+                          double hx, double hy, double hz, double dt,
+                          int nxg, int nyg, int nzg, int ref_bugs, void *stream);
+
+/* Same, host pointers, synchronous. */
+int emix_weno5_advect(double *phi, const double *vel, const double *jbn,
+                      double hx, double hy, double hz, double dt,
+                      int nxg, int nyg, int nzg, int ref_bugs);
+
+/* Ghost padding (cuSwapToGhost + cuGhostCellsMirror3dZ/Y/X,
+ * src/LevelSet/lsTools.cu:482-585,772-796) and unpadding (cuSwapFromGhost,
+ * :798-822).  ghost is (nx+2g)(ny+2g)(nz+2g).  Device pointers. */
+int emix_ghost_pad_dev(double *ghost, const double *val, int g, double direction,
+                       int nx, int ny, int nz, void *stream);
+int emix_ghost_unpad_dev(double *val, const double *ghost, int g,
+                         int nx, int ny, int nz, void *stream);
+
+/* ========================================================================
+ * Device-resident RK3 step (solver/rungek_ico.f90:61-313)
+ * ======================================================================== */
+
+typedef struct emix_params {
+    int nx, ny, nz;
+    int scheme[3];      /* per axis, EMIX_SCHEME_*                                */
+    double h[3];        /* computational spacing per axis                          */
+    int sgs_model;      /* EMIX_SGS_*                                              */
+    double cs;          /* Smagorinsky constant                                    */
+    double amu0;        /* structure-function constant (0.1781 in the reference)   */
+    double c4;          /* 1/Re                                                    */
+    double mach;        /* um(1) = p*Mach^2                                        */
+    double dt;
+    int level_set;      /* 1: advance the level set with the flow (WENO5, SSP-RK3) */
+    int ls_ghost;       /* ghost layers of the level-set grid (5 in the reference) */
+    int ref_bugs;       /* 1: keep the reference's z-top WENO neighbour index      */
+} emix_params;
+
+typedef struct emix_ctx emix_ctx;
+
+/* Create a context holding every field of one grid in device memory. */
+int emix_ctx_create(const emix_params *p, emix_ctx **out);
+int emix_ctx_destroy(emix_ctx *ctx);
+
+/* Stream the context launches on (NULL = the legacy default stream). */
+int emix_ctx_set_stream(emix_ctx *ctx, void *stream);
+
+/* Static inputs from host memory: jbn[11], mask, grid coordinates xyz[3]
+ * (used to build the SGS filter width, as INISGDM). */
+int emix_ctx_set_static(emix_ctx *ctx, const double *jbn, const double *mask,
+                        const double *xyz);
+
+/* State transfer, host memory: um[5] (p*Mach^2, rho*u, rho*v, rho*w, T) and
+ * phi (may be NULL when the level set is off). */
+int emix_ctx_upload(emix_ctx *ctx, const double *um, const double *phi);
+int emix_ctx_download(emix_ctx *ctx, double *um, double *phi);
+
+/* Device pointers of the state (um: 5 fields, phi: 1 field). */
+int emix_ctx_state(emix_ctx *ctx, double **um, double **phi);
+
+/* Advance nsteps RK3 steps on the device, asynchronously on the context
+ * stream.  use_graph = 1 replays a captured CUDA graph of one step. */
+int emix_step(emix_ctx *ctx, int nsteps, int use_graph);
+
+/* End-to-end form: copy um/phi from host, advance nsteps, copy back;
+ * synchronous. */
+int emix_step_host(emix_ctx *ctx, double *um, double *phi, int nsteps);
+
+/* Number of kernel launches one step issues (for accounting). */
+int emix_ctx_launches_per_step(emix_ctx *ctx);
+
+/* Bytes of device memory the context holds. */
+long long emix_ctx_device_bytes(emix_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EMIX_GB300_H */

@@ -1,0 +1,132 @@
+/*
+ * oracle.h -- CPU restatement of the eMix3d per-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
+ * implementation in emix_gb300/csrc; only tests/, __graft_entry__.smoke()
+ * and the CPU-baseline leg of bench.py load it.  The product path never
+ * calls it.
+ *
+ * Every function restates one piece of the reference (jramirezcr/eMix3d) and
+ * names the file:line it follows.  Arithmetic is written in the same order
+ * as the reference so that results agree to rounding; the build uses
+ * -ffp-contract=off so x86 and Arm hosts give identical results.
+ *
+ * Layout: Fortran column-major, i fastest, linear index i + nx*(j + ny*k)
+ * (src/Engine/cuArray.cu:123).  Multi-component arrays stack components
+ * with stride nx*ny*nz (solver/cuDeriv.cu:588-590).
+ *
+ * Parity pinning: the reference has no tests, golden vectors or fixtures,
+ * and its Fortran CPU path cannot be compiled here (no Fortran compiler).
+ * The restatement is pinned by analytic known-answer tests (modified
+ * wavenumber, polynomial exactness, WENO5 linear-weight limit) and by
+ * committed golden vectors generated from this restatement; see the test
+ * suite for what each pin covers.
+ */
+#ifndef EMIX_ORACLE_H
+#define EMIX_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Compact-scheme variants (one per coefficient table in the reference). */
+enum {
+    ORC_SCHEME_A = 0,      /* solver/derivada.f90:2-125 (Pade-4, alpha=1/4, alpha_1=3)   */
+    ORC_SCHEME_B = 1,      /* src/MSVSingle/derivada_incomp.f90:130-218,297-329 (Lele-6) */
+    ORC_SCHEME_BPER = 2,   /* src/MSVSingle/derivada_incomp.f90:221-294 (cyclic Lele-6)  */
+    ORC_SCHEME_C = 3       /* src/Schemes/derivCompact.cu:81-215 (production GPU)       */
+};
+
+/* One pencil, in place.  h is the grid spacing in computational space. */
+int orc_deriv_pencil(int scheme, int n, double *u, double h);
+
+/* Derivative of a 3-D field along axis (0=x,1=y,2=z); gather/derivnper/scatter
+ * as solver/deriv_vel.f90:17-161. */
+int orc_deriv3d(int scheme, int axis, int nx, int ny, int nz, double h,
+                const double *in, double *out);
+
+/* cudaDeriv contract (solver/cuDeriv.cu:529-654): 9 velocity and 3
+ * temperature derivatives in computational coordinates. */
+int orc_cudaDeriv(const int *schemes, double *dvel, double *dtemp,
+                  const double *vel, const double *temp,
+                  double hx, double hy, double hz, int nx, int ny, int nz);
+
+/* cuDivergence contract (solver/cuDivergence.cu:107-189 and
+ * solver/divergencia.f90:225-354).  Inputs are not modified. */
+int orc_cuDivergence(const int *schemes, double *rs, double *rsv,
+                     const double *e, const double *f, const double *g,
+                     const double *ev, const double *fv, const double *gv,
+                     const double *jbn, double hx, double hy, double hz,
+                     int nx, int ny, int nz);
+
+/* flujos(neq) (solver/flujos_compact.f90:21-217).  neq in 1..5. */
+int orc_flujos(int neq, int nx, int ny, int nz,
+               double *e, double *f, double *g,
+               double *ev, double *fv, double *gv,
+               const double *um, const double *u, const double *pres,
+               const double *dvel, const double *jbn, const double *vis);
+
+/* INISGDM (solver/sgdm_incomp.f90:2-114): filter width and the six
+ * one-sided spacing ratios from grid coordinates xyz (3 components). */
+int orc_inisgdm(int nx, int ny, int nz, const double *xyz,
+                double *dxyzsgd, double *ratios /* 6: xp,xm,yp,ym,zp,zm */);
+
+/* viscosidad_t with the selective structure-function model
+ * (solver/sgdm_incomp.f90:117-162,166-315,319-343,346-395). */
+int orc_sgs_sf(int nx, int ny, int nz, const double *u, const double *dvel,
+               const double *jbn, const double *dxyzsgd, const double *ratios,
+               double amu0, double *amut);
+
+/* Smagorinsky eddy viscosity from the physical gradient jbn(1|5|9)*dvel:
+ * nu_t = (Cs*Delta)^2 * sqrt(2 S_ij S_ij).  Not in the reference. */
+int orc_sgs_smag(int nx, int ny, int nz, const double *dvel, const double *jbn,
+                 const double *dxyzsgd, double cs, double *amut);
+
+/* viscosidad (src/MSVSingle/viscosidad_incomp.f90:12-20): vis = c4 + amut. */
+int orc_viscosidad(int n, const double *amut, double c4, double *vis);
+
+/* Level set: ghost padding and mirroring (src/LevelSet/lsTools.cu:482-585,
+ * 772-822), and one WENO5 TVD-RK3 advection step on ghosted arrays
+ * (src/LevelSet/lsTransportEc.cu:201-418). */
+int orc_to_ghost(double *ghost, const double *val, int g, int nx, int ny, int nz);
+int orc_mirror_ghost(double *ghost, int g, int nx, int ny, int nz, double direction);
+int orc_from_ghost(double *val, const double *ghost, int g, int nx, int ny, int nz);
+int orc_weno_rhs(double *rs, const double *phi, const double *vel, const double *jbn,
+                 double hx, double hy, double hz, int nxg, int nyg, int nzg,
+                 int ref_bugs);
+int orc_weno_advect(double *phi, const double *vel, const double *jbn,
+                    double hx, double hy, double hz, double dt,
+                    int nxg, int nyg, int nzg, int ref_bugs);
+double orc_phi_x_weno(double b1, double b2, double b3, double b4, double b5);
+
+/* Parameters of one RK3 step (solver/rungek_ico.f90:61-313). */
+typedef struct {
+    int nx, ny, nz;
+    int scheme[3];        /* per axis: ORC_SCHEME_* */
+    double h[3];          /* computational spacing per axis */
+    int sgs_model;        /* 0 none, 1 Smagorinsky, 2 selective structure function */
+    double cs;            /* Smagorinsky constant */
+    double amu0;          /* structure-function constant (0.1781 in the reference) */
+    double c4;            /* 1/Re */
+    double mach;
+    double dt;
+    int level_set;        /* 1: advance the level set with the flow: one WENO5 TVD stage per substep */
+    int ls_ghost;         /* ghost layers for the level set (5 in the reference) */
+    int ref_bugs;         /* 1: reproduce the reference's z-top WENO index */
+} orc_step_params;
+
+/* One RK3 step.  State in/out: um (5 fields) and phi (1 field, may be NULL
+ * when level_set == 0).  Static inputs: jbn (11), mask, dxyzsgd, ratios (6,
+ * only for the structure-function model). */
+int orc_step(const orc_step_params *p, double *um, double *phi,
+             const double *jbn, const double *mask,
+             const double *dxyzsgd, const double *ratios);
+
+/* Number of OpenMP threads the oracle uses (0 = library default). */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
