@@ -206,7 +206,11 @@ def stirred_tank(n=256, seed=2, nmodes=64, kmax=8, omega=1.0, radius=1.0, height
     rng_k = uniform(seed, 10, (nmodes, 3))
     rng_a = uniform(seed, 11, (nmodes, 6))
     u = np.stack([-omega * Y, omega * X, np.zeros_like(X)])
-    pert = np.zeros_like(u)
+    # mode m: amp_c * sin(kx*pi*x/R + ky*pi*y/R + kz*pi*z/H + 2*pi*u2_0), summed as
+    # Im(sum_m [amp_c e^{i p} E_z E_y](z,y) [E_x](x)): one complex GEMM per component
+    ks = np.zeros((nmodes, 3))
+    amps = np.zeros((nmodes, 3))
+    phase = np.zeros(nmodes)
     for m in range(nmodes):
         k = np.round(rng_k[m] * kmax)
         while np.sqrt(np.sum(k * k)) > kmax:
@@ -214,11 +218,18 @@ def stirred_tank(n=256, seed=2, nmodes=64, kmax=8, omega=1.0, radius=1.0, height
         # Box-Muller from two uniforms per component -> Gaussian amplitude
         u1 = 0.5 * (rng_a[m, :3] + 1.0) + 1e-12
         u2 = 0.5 * (rng_a[m, 3:] + 1.0)
-        amp = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
-        ph = k[0] * math.pi * X / radius + k[1] * math.pi * Y / radius + k[2] * math.pi * Z / height
-        s = np.sin(ph + 2.0 * math.pi * u2[0])
-        for c in range(3):
-            pert[c] += amp[c] * s
+        ks[m] = k
+        amps[m] = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+        phase[m] = 2.0 * math.pi * u2[0]
+    x1, y1, z1 = (g.coords1d(a) for a in range(3))
+    Ex = np.exp(1j * np.outer(ks[:, 0] * math.pi / radius, x1))          # (m, nx)
+    Ey = np.exp(1j * np.outer(ks[:, 1] * math.pi / radius, y1))          # (m, ny)
+    Ez = np.exp(1j * np.outer(ks[:, 2] * math.pi / height, z1))          # (m, nz)
+    base = (Ez[:, :, None] * Ey[:, None, :]) * np.exp(1j * phase)[:, None, None]  # (m, nz, ny)
+    base = base.reshape(nmodes, -1).T                                     # (nz*ny, m)
+    pert = np.empty_like(u)
+    for c in range(3):
+        pert[c] = ((base * amps[:, c]) @ Ex).imag.reshape(g.shape)
     rms = math.sqrt(float(np.mean(np.sum(pert * pert, axis=0))))
     if rms > 0:
         pert *= 0.1 * omega * radius / rms
