@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 eMix3d hot path: Mcell-RK3-steps/s.
+
+One step = one full RK3 step (three substeps: compact velocity gradients,
+SGS viscosity, fluxes, compact flux divergence, RK update, WENO5 level-set
+stage) of the 256^3 wall-bounded stirred-tank workload (Lele-6 compact
+scheme with 3rd/4th-order closures, Smagorinsky Cs = 0.1, CFL 0.3), FP64.
+Fields are seeded synthetic data of that configuration.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun every rank advances its own independent replica of the grid
+(the path has no exchange step), so ``value`` is the sum over ranks and the
+scaling is weak.  ``--impl reference`` times the CPU restatement of the
+reference's algorithm (the oracle) on all host threads, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_GRID = 256
+SAMPLE_N = 96            # CPU sample grid (same generator, fewer cells)
+G = 5                    # level-set ghost layers
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# Algorithmic bytes per launch of each kernel class, per cell of the grid
+# (n = cells, ng = ghost-padded cells of the level-set grid): every field a
+# kernel must read or write, once.
+def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1) -> float:
+    d = 8.0
+    if name == "weno_stage":       # phi_s (ng) + phi_0 (ng, stages 2,3) + u(3n) + jbn(3n) -> out
+        return d * ((1.0 + 2.0 / 3.0) * ng + 6 * n + (2.0 * ng + n) / 3.0)
+    if name in ("grad_x", "grad_y", "grad_z"):
+        return d * 6 * n           # 3 in, 3 out
+    if name == "div_x":
+        return d * 10 * n          # 5 in, 5 out
+    if name in ("div_y", "div_z"):
+        return d * 15 * n          # 5 in, 5 accumulated (read + write)
+    if name == "flux":
+        return d * 40 * n          # um 5, u 3, p, dvel 9, vis, jbn 3, J*metric 3 -> 15
+    if name == "sgs":
+        return d * (14 if sgs == 1 else 20) * n
+    if name == "rk_post":
+        return d * (17 * 2 + 12) / 3.0 * n + d * 9 * n
+    if name == "prim":
+        return d * 8 * n
+    if name == "ghost_pad":
+        return d * (n + ng)
+    return 0.0
+
+
+# FP64 lane operations per cell of each kernel class (per launch), counted
+# from the kernel source (adds, multiplies and FMAs; a divide or square root
+# counted as the 8 operations of its refinement sequence).
+FP64_OPS_PER_CELL = {
+    "weno_stage": 3 * 62 + 8, "grad_x": 3 * 6, "grad_y": 3 * 6, "grad_z": 3 * 6,
+    "div_x": 5 * 6, "div_y": 5 * 7, "div_z": 5 * 7, "flux": 55, "sgs": 32,
+    "rk_post": 45, "prim": 12, "ghost_pad": 0,
+}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        out.update(sm_mhz=float(np.median(sm)) if sm else None,
+                   sm_max_mhz=max(mx) if mx else None, reasons=reasons, samples=len(rows))
+        return out
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(steps: int, warmup: int):
+    """Oracle (CPU restatement of the reference algorithm) on the SAMPLE_N^3
+    tank, all host threads.  Returns (Mcell-steps/s, seconds, threads)."""
+    from emix_gb300 import fields as F
+    from oracle import oracle_py as O
+    w = F.stirred_tank(n=SAMPLE_N)
+    p = O.step_params(w)
+    d, r = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
+    um, phi = w.um, w.phi
+    for _ in range(warmup):
+        um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
+    sec = time.perf_counter() - t0
+    return w.grid.ncell * steps / sec / 1e6, sec, O.get_threads()
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    v, sec, thr = cpu_sample(args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": "Mcell-RK3-steps/s", "value": round(v, 4),
+        "unit": "Mcell-RK3-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * sec / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": config_dict(None),
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mcell-RK3-steps/s", "cores": thr,
+                         "kind": "port",
+                         "sample": f"RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator, "
+                                   f"{SAMPLE_N ** 3} cells per step), CPU restatement of the "
+                                   f"reference algorithm, {thr} threads"},
+        "e2e": {"value": round(v, 4), "unit": "Mcell-RK3-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_dict(w):
+    return {
+        "workload": f"stirred tank {N_GRID}^3 walls, RK3 step with WENO5 level set",
+        "grid": [N_GRID, N_GRID, N_GRID],
+        "scheme": "Lele-6 compact, 3rd/4th-order closures (derivada_incomp.f90)",
+        "sgs": "Smagorinsky Cs=0.1", "level_set": "WENO5 TVD stage per substep",
+        "cfl": 0.3, "dt": None if w is None else w.dt, "precision": "fp64",
+        "l2": "inputs larger than L2 (9 GB resident, 128 MiB per field)",
+        "parallelism": "replicas (one independent grid per GPU)",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="emix", choices=["emix", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    from emix_gb300 import fields as F
+    from emix_gb300 import ops
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    w = F.stirred_tank(n=N_GRID)
+    n = w.grid.ncell
+    ng = (N_GRID + 2 * G) ** 3
+    ctx = ops.Context(w, level_set=True, ls_ghost=G)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.step(args.warmup, use_graph=True)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    sampler = ClockSampler(local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    ctx.step(args.steps, use_graph=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    value = world * n * args.steps / (ms * 1e-3) / 1e6
+    launches_per_step = ctx.launches_per_step()
+
+    # ---- end-to-end through the host-pointer entry point ----
+    um_h = torch.from_numpy(np.ascontiguousarray(w.um)).pin_memory()
+    phi_h = torch.from_numpy(np.ascontiguousarray(w.phi)).pin_memory()
+    um_np, phi_np = um_h.numpy(), phi_h.numpy()
+    ctx.step_host(um_np, phi_np, 1)
+    torch.cuda.synchronize()
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        ctx.step_host(um_np, phi_np, 1)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = max_over_ranks(f0.elapsed_time(f1))
+    e2e_value = world * n * args.steps / (ms_e2e * 1e-3) / 1e6
+    assert np.isfinite(um_np).all() and np.isfinite(phi_np).all()
+
+    # ---- per-kernel times (CUDA events around every launch) ----
+    prof = ctx.profile(nsteps=max(3, min(args.steps, 10)))
+    psteps = max(3, min(args.steps, 10))
+    total = sum(v[0] for v in prof.values()) or 1.0
+    kernels = {k: {"ms_per_launch": round(v[0] / v[1], 4) if v[1] else 0.0,
+                   "launches_per_step": v[1] // psteps,
+                   "share": round(v[0] / total, 4)} for k, v in prof.items() if v[1]}
+    top = max(prof, key=lambda k: prof[k][0])
+    top_ms = prof[top][0] / prof[top][1]
+    hbm_peak, peak_kind = _peaks()
+    fp64_peak = ops.fp64_peak()
+    ab = algorithmic_bytes(top, n, ng)
+    cells_top = ng if top in ("weno_stage", "ghost_pad") else n
+    fp64_ach = FP64_OPS_PER_CELL.get(top, 0) * cells_top / (top_ms * 1e-3)
+    achieved = ab / (top_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get(top)
+    roofline = {
+        "kernel": top, "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak,
+        "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+        "binding": "fp64",
+        "fp64": {"achieved": round(fp64_ach / 1e9, 2), "peak": round(fp64_peak / 1e9, 2),
+                 "unit": "G FP64 lane-ops/s", "frac": round(fp64_ach / fp64_peak, 4),
+                 "peak_source": "measured live (emix_fp64_peak: FMA chains)"},
+    }
+    ctx.close()
+
+    line = {
+        "metric": "Mcell-RK3-steps/s", "value": round(value, 3), "unit": "Mcell-RK3-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(w),
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mcell-RK3-steps/s",
+                "h2d_bytes_per_step": int(6 * n * 8), "d2h_bytes_per_step": int(6 * n * 8),
+                "api": "emix_step_host (pinned host buffers, H2D um+phi, one step, D2H um+phi)"},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline,
+        "kernels": kernels,
+        "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, sec, thr = cpu_sample(2, 1)
+        line["cpu_baseline"] = {
+            "value": round(v, 4), "unit": "Mcell-RK3-steps/s", "cores": thr, "kind": "port",
+            "sample": f"2 RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator), CPU "
+                      f"restatement of the reference algorithm, {sec:.1f} s, {thr} threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

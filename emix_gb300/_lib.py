@@ -73,6 +73,10 @@ PROTOTYPES = {
     "emix_step_host": (C.c_int, [vp, vp, vp, C.c_int]),
     "emix_ctx_launches_per_step": (C.c_int, [vp]),
     "emix_ctx_device_bytes": (C.c_longlong, [vp]),
+    "emix_ctx_profile": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "emix_profile_class_count": (C.c_int, []),
+    "emix_profile_class_name": (C.c_char_p, [C.c_int]),
+    "emix_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
 }
 
 _lib = None

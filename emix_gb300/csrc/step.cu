@@ -56,9 +56,35 @@ struct emix_ctx {
     cudaGraphExec_t gexec = nullptr;
     bool static_set = false;
     int launches = 0;
+    // optional per-launch timing (emix_ctx_profile): events around every launch
+    bool prof = false;
+    int prof_n = 0;
+    cudaEvent_t prof_ev[2 * 64] = {};
+    int prof_cls[64] = {};
 };
 
+static const char *kClassNames[] = {
+    "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
+    "div_x", "div_y", "div_z", "rk_post"};
+enum { CLS_PRIM, CLS_PAD, CLS_WENO, CLS_GRADX, CLS_GRADY, CLS_GRADZ, CLS_SGS, CLS_FLUX,
+       CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_COUNT };
+
 namespace {
+
+struct ProfScope {
+    emix_ctx *c;
+    int slot;
+    ProfScope(emix_ctx *c_, int cls) : c(c_), slot(-1) {
+        if (c->prof && c->prof_n < 64) {
+            slot = c->prof_n++;
+            c->prof_cls[slot] = cls;
+            cudaEventRecord(c->prof_ev[2 * slot], c->stream);
+        }
+    }
+    ~ProfScope() {
+        if (slot >= 0) cudaEventRecord(c->prof_ev[2 * slot + 1], c->stream);
+    }
+};
 
 int issue_step(emix_ctx *c) {
     const emix_params &p = c->p;
@@ -70,10 +96,14 @@ int issue_step(emix_ctx *c) {
     int rc;
     const double inv_m2 = 1.0 / (p.mach * p.mach);
 
-    k_prim<<<gb, 256, 0, st>>>(c->um0, c->u, c->pres, inv_m2, n);
+    {
+        ProfScope ps(c, CLS_PRIM);
+        k_prim<<<gb, 256, 0, st>>>(c->um0, c->u, c->pres, inv_m2, n);
+    }
     ++launches;
     if (p.level_set) {
         const long ngc = c->ng;
+        ProfScope ps(c, CLS_PAD);
         k_ghost_pad<<<cells_grid(ngc), 256, 0, st>>>(c->phig0, c->phi, p.ls_ghost, 1.0, nx, ny, nz);
         ++launches;
     }
@@ -94,6 +124,7 @@ int issue_step(emix_ctx *c) {
             a.nxg = nx + 2 * g; a.nyg = ny + 2 * g; a.nzg = nz + 2 * g; a.g = g;
             a.sx = 1.0 / p.h[0]; a.sy = 1.0 / p.h[1]; a.sz = 1.0 / p.h[2];
             a.dt = p.dt; a.stage = s; a.ref_bugs = p.ref_bugs;
+            ProfScope ps(c, CLS_WENO);
             if ((rc = launch_weno_stage(a, st))) return rc;
             ++launches;
         }
@@ -102,17 +133,20 @@ int issue_step(emix_ctx *c) {
         for (int ax = 0; ax < 3; ++ax) {
             const double *in[3] = {c->u, c->u + n, c->u + 2 * n};
             double *out[3] = {c->dvel + 3 * ax * n, c->dvel + (3 * ax + 1) * n, c->dvel + (3 * ax + 2) * n};
+            ProfScope ps(c, CLS_GRADX + ax);
             if ((rc = launch_deriv(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, st))) return rc;
             ++launches;
         }
         // SGS viscosity
         if (p.sgs_model == EMIX_SGS_STRUCTURE) {
+            ProfScope ps(c, CLS_SGS);
             k_sgs_sf<<<gb, 256, 0, st>>>(c->u, c->ratios, c->dxyz, p.amu0, c->amut, nx, ny, nz);
             k_vort<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->vort, n);
             const double cutoff = cos(20.0 * atan(1.0) / 45.0);
             k_selective<<<gb, 256, 0, st>>>(c->vort, c->amut, c->vis, cutoff, p.c4, nx, ny, nz);
             launches += 3;
         } else {
+            ProfScope ps(c, CLS_SGS);
             k_sgs_smag<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->dxyz,
                                            p.sgs_model == EMIX_SGS_NONE ? 0.0 : p.cs, p.c4, nullptr,
                                            c->vis, n);
@@ -123,7 +157,10 @@ int issue_step(emix_ctx *c) {
         for (int q = 0; q < 15; ++q) fa.F[q] = c->flux + q * n;
         fa.um = umcur; fa.u = c->u; fa.pres = c->pres; fa.dvel = c->dvel; fa.vis = c->vis;
         fa.jbn = c->jbn; fa.jx = c->jx; fa.jy = c->jy; fa.jz = c->jz; fa.n = n;
-        k_flux_all<<<gb, 256, 0, st>>>(fa);
+        {
+            ProfScope ps(c, CLS_FLUX);
+            k_flux_all<<<gb, 256, 0, st>>>(fa);
+        }
         ++launches;
         EMIX_CUDA_TRY(cudaGetLastError());
         // divergence: R_m = sum over directions of the compact derivative
@@ -135,6 +172,7 @@ int issue_step(emix_ctx *c) {
                 out[m] = c->R + m * n;
                 wb[m] = c->W + m * n;
             }
+            ProfScope ps(c, CLS_DIVX + ax);
             if (ax == 0)
                 rc = launch_deriv(c->T[ax], ax, EPI_STORE, 5, in, out, out, nx, ny, nz, st);
             else
@@ -148,7 +186,10 @@ int issue_step(emix_ctx *c) {
         ra.out = s == 3 ? c->um0 : c->um;
         ra.u = c->u; ra.pres = c->pres; ra.jbn = c->jbn; ra.mask = c->mask;
         ra.dt = p.dt; ra.mach = p.mach; ra.inv_m2 = inv_m2; ra.stage = s; ra.n = n;
-        k_rk_post<<<gb, 256, 0, st>>>(ra);
+        {
+            ProfScope ps(c, CLS_RK);
+            k_rk_post<<<gb, 256, 0, st>>>(ra);
+        }
         ++launches;
         EMIX_CUDA_TRY(cudaGetLastError());
     }
@@ -250,6 +291,8 @@ int emix_ctx_destroy(emix_ctx *c) {
     if (!c) return EMIX_ERR_ARG;
     cudaStreamSynchronize(c->stream);
     drop_graph(c);
+    for (cudaEvent_t &e : c->prof_ev)
+        if (e) cudaEventDestroy(e);
     if (c->own) cudaStreamDestroy(c->own);
     cudaFree(c->arena);
     delete c;
@@ -370,5 +413,34 @@ int emix_ctx_launches_per_step(emix_ctx *c) {
 }
 
 long long emix_ctx_device_bytes(emix_ctx *c) { return c ? (long long)c->arena_bytes : -1; }
+
+const char *emix_profile_class_name(int cls) {
+    return (cls >= 0 && cls < CLS_COUNT) ? kClassNames[cls] : "";
+}
+
+int emix_profile_class_count(void) { return CLS_COUNT; }
+
+int emix_ctx_profile(emix_ctx *c, int nsteps, double *ms, int *launches) {
+    if (!c || nsteps < 1 || !ms || !launches) return EMIX_ERR_ARG;
+    if (!c->static_set) return EMIX_ERR_ARG;
+    for (int k = 0; k < CLS_COUNT; ++k) { ms[k] = 0.0; launches[k] = 0; }
+    for (cudaEvent_t &e : c->prof_ev)
+        if (!e) EMIX_CUDA_TRY(cudaEventCreate(&e));
+    for (int s = 0; s < nsteps; ++s) {
+        c->prof = true;
+        c->prof_n = 0;
+        int rc = issue_step(c);
+        c->prof = false;
+        if (rc) return rc;
+        EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        for (int q = 0; q < c->prof_n; ++q) {
+            float t = 0.f;
+            EMIX_CUDA_TRY(cudaEventElapsedTime(&t, c->prof_ev[2 * q], c->prof_ev[2 * q + 1]));
+            ms[c->prof_cls[q]] += t;
+            launches[c->prof_cls[q]] += 1;
+        }
+    }
+    return EMIX_OK;
+}
 
 } // extern "C"

@@ -219,6 +219,13 @@ def ghost_unpad_dev(ghost, g):
     return out
 
 
+def fp64_peak() -> float:
+    """Measured FP64 FMA lane-operations per second of the current device."""
+    v = C.c_double()
+    check(_lib.load().emix_fp64_peak(C.byref(v)), "emix_fp64_peak")
+    return v.value
+
+
 # --------------------------------------------------------------------------
 # device-resident RK3 step
 # --------------------------------------------------------------------------
@@ -289,6 +296,15 @@ class Context:
 
     def step_host(self, um, phi, nsteps=1):
         check(self.lib.emix_step_host(self._h, _ptr(um), _ptr(phi), nsteps), "emix_step_host")
+
+    def profile(self, nsteps=1):
+        """Per-kernel-class device time: {name: (total_ms, launches)} over nsteps
+        steps, from CUDA events on the context stream."""
+        k = self.lib.emix_profile_class_count()
+        ms = (C.c_double * k)()
+        nl = (C.c_int * k)()
+        check(self.lib.emix_ctx_profile(self._h, nsteps, ms, nl), "emix_ctx_profile")
+        return {self.lib.emix_profile_class_name(i).decode(): (ms[i], nl[i]) for i in range(k)}
 
     def launches_per_step(self):
         return self.lib.emix_ctx_launches_per_step(self._h)

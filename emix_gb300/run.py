@@ -1,0 +1,39 @@
+"""Run RK3 steps of a synthetic workload through the C ABI.
+
+    python -m emix_gb300.run --workload tank --n 256 --steps 2 [--graph]
+
+Used for profiling (ncu) and quick checks; prints one summary line.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="tank", choices=["tank", "tgv"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--no-level-set", action="store_true")
+    a = ap.parse_args(argv)
+    import numpy as np
+    import torch
+    from . import fields as F
+    from . import ops
+    w = F.stirred_tank(n=a.n) if a.workload == "tank" else F.taylor_green(n=a.n)
+    ctx = ops.Context(w, level_set=not a.no_level_set)
+    t0 = time.perf_counter()
+    ctx.step(a.steps, use_graph=a.graph)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    um, phi = ctx.download()
+    ok = bool(np.isfinite(um).all() and (phi is None or np.isfinite(phi).all()))
+    print(f"{w.name}: {a.steps} steps in {sec:.3f} s, finite={ok}, max|um|={float(np.abs(um).max()):.6g}")
+    ctx.close()
+    return 0 if ok else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

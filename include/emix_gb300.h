@@ -224,6 +224,18 @@ int emix_ctx_launches_per_step(emix_ctx *ctx);
 /* Bytes of device memory the context holds. */
 long long emix_ctx_device_bytes(emix_ctx *ctx);
 
+/* Per-kernel timing: run nsteps steps (no graph) with CUDA events around
+ * every launch on the context stream; ms[k] and launches[k] receive the
+ * summed duration and launch count of kernel class k
+ * (k < emix_profile_class_count(), named by emix_profile_class_name). */
+int emix_ctx_profile(emix_ctx *ctx, int nsteps, double *ms, int *launches);
+int emix_profile_class_count(void);
+const char *emix_profile_class_name(int cls);
+
+/* Diagnostic: measured FP64 fused-multiply-add throughput of the current
+ * device in lane operations per second (a short dependent-chain kernel). */
+int emix_fp64_peak(double *lane_ops_per_s);
+
 #ifdef __cplusplus
 }
 #endif
