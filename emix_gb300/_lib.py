@@ -60,6 +60,8 @@ PROTOTYPES = {
                                [C.c_int] * 3 + [vp]),
     "emix_weno5_advect_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4 + [vp]),
     "emix_weno5_advect": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4),
+    "emix_weno5_advect_dev_noalloc": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4
+                                      + [vp]),
     "emix_ghost_pad_dev": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
     "emix_ghost_unpad_dev": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]),
     "emix_ctx_create": (C.c_int, [C.POINTER(EmixParams), C.POINTER(vp)]),

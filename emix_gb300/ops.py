@@ -198,6 +198,20 @@ def weno5_advect_dev(phi, vel, jbn, h, dt, ref_bugs=0):
     return phi
 
 
+def weno5_advect_dev_noalloc(phi, vel, jbn, h, dt, ref_bugs=0):
+    """In-place WENO5 TVD-RK3 step on padded device tensors that allocates no
+    device memory: the stage scratch is a fixed 16 MiB array inside the
+    library, so the padded grid may hold at most 1048576 cells.  For callers
+    that cannot let a library call cudaMalloc.  Calls that overlap on the GPU
+    share (and race on) that array."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(phi)
+    check(lib.emix_weno5_advect_dev_noalloc(_ptr(phi), _ptr(vel), _ptr(jbn), h[0], h[1], h[2], dt,
+                                            nx, ny, nz, ref_bugs, _stream()),
+          "emix_weno5_advect_dev_noalloc")
+    return phi
+
+
 def ghost_pad_dev(val, g, direction=1.0):
     import torch
     lib = _lib.load()

@@ -161,6 +161,18 @@ int emix_weno5_advect(double *phi, const double *vel, const double *jbn,
                       double hx, double hy, double hz, double dt,
                       int nxg, int nyg, int nzg, int ref_bugs);
 
+/* Same step as emix_weno5_advect_dev without allocating device memory; it
+ * has no counterpart in the reference.  For callers that cannot let a library
+ * call cudaMalloc (it can block the device, and fails when another allocator
+ * already holds the memory).  The two padded stage fields come from a 16 MiB
+ * array compiled into the library, so nxg*nyg*nzg must not exceed 1048576
+ * (EMIX_ERR_ARG otherwise).  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race on it. */
+int emix_weno5_advect_dev_noalloc(double *phi, const double *vel, const double *jbn,
+                                  double hx, double hy, double hz, double dt,
+                                  int nxg, int nyg, int nzg, int ref_bugs, void *stream);
+
 /* Ghost padding (cuSwapToGhost + cuGhostCellsMirror3dZ/Y/X,
  * src/LevelSet/lsTools.cu:482-585,772-796) and unpadding (cuSwapFromGhost,
  * :798-822).  ghost is (nx+2g)(ny+2g)(nz+2g).  Device pointers. */
