@@ -76,73 +76,127 @@ EMIX_DEV double rhs_row(const DerivTable &T, const double *__restrict__ fp, long
 //   axis 2 (z): pencils (x, y), element stride nx*ny, other stride nx
 // grid: (ceil(nx/blockDim.x), nother, nf)
 // ---------------------------------------------------------------------------
-template <int EPI>
-__global__ void __launch_bounds__(128)
-k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int o = blockIdx.y;
-    const int f = blockIdx.z;
-    if (x >= nx || o >= nother) return;
-    const long base = x + (long)o * os;
-    const double *__restrict__ in = pick(F.in, f) + base;
-    double *w = pick(F.w, f) + base;
-    double *out = pick(F.out, f) + base;
+// K fields of one pencil in lockstep: K independent dependency chains per
+// thread, interleaved so that the FP64 pipe always has work (ILP).
+template <int EPI, int K>
+EMIX_DEV void pencil_yz(const DerivTable &T, const PencilFields &F, int f0, long base, long s) {
+    const double *in[K];
+    double *w[K], *out[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        in[k] = pick(F.in, f0 + k) + base;
+        w[k] = pick(F.w, f0 + k) + base;
+        out[k] = pick(F.out, f0 + k) + base;
+    }
     const int n = T.n;
     const DerivRow *__restrict__ rows = T.rows;
 
     // forward sweep
-    double wp = 0.0, y0 = 0.0;
+    double wp[K], y0[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) { wp[k] = 0.0; y0[k] = 0.0; }
     int i = 0;
     if (!T.periodic) {
         for (; i < T.nlo; ++i) {
-            const double v = rhs_row(T, in, s, i) - rows[i].m * wp;
-            w[i * s] = v;
-            wp = v;
+            const double m = rows[i].m;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double v = rhs_row(T, in[k], s, i) - m * wp[k];
+                w[k][i * s] = v;
+                wp[k] = v;
+            }
         }
         const int iend = n - T.nhi;
         if (i < iend) {
-            double fm2 = in[(i - 2) * s], fm1 = in[(i - 1) * s], f0 = in[i * s], fp1 = in[(i + 1) * s];
+            double fm2[K], fm1[K], f0c[K], fp1[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                fm2[k] = in[k][(i - 2) * s]; fm1[k] = in[k][(i - 1) * s];
+                f0c[k] = in[k][i * s]; fp1[k] = in[k][(i + 1) * s];
+            }
             for (; i < iend; ++i) {
-                const double fp2 = in[(i + 2) * s];
                 const DerivRow r = rows[i];
-                const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
-                w[i * s] = v;
-                wp = v;
-                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const double fp2 = in[k][(i + 2) * s];
+                    const double v = r.A * (fp1[k] - fm1[k]) + r.B * (fp2 - fm2[k]) - r.m * wp[k];
+                    w[k][i * s] = v;
+                    wp[k] = v;
+                    fm2[k] = fm1[k]; fm1[k] = f0c[k]; f0c[k] = fp1[k]; fp1[k] = fp2;
+                }
             }
         }
         for (; i < n; ++i) {
-            const double v = rhs_row(T, in, s, i) - rows[i].m * wp;
-            w[i * s] = v;
-            wp = v;
+            const double m = rows[i].m;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double v = rhs_row(T, in[k], s, i) - m * wp[k];
+                w[k][i * s] = v;
+                wp[k] = v;
+            }
         }
     } else {
-        double fm2 = in[(n - 2) * s], fm1 = in[(n - 1) * s], f0 = in[0], fp1 = in[s];
+        double fm2[K], fm1[K], f0c[K], fp1[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            fm2[k] = in[k][(n - 2) * s]; fm1[k] = in[k][(n - 1) * s];
+            f0c[k] = in[k][0]; fp1[k] = in[k][s];
+        }
         for (; i < n; ++i) {
             int j = i + 2;
             if (j >= n) j -= n;
-            const double fp2 = in[j * s];
             const DerivRow r = rows[i];
-            const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
-            w[i * s] = v;
-            if (i < T.ku) y0 += T.u0[i] * v;
-            wp = v;
-            fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+            const bool acc = i < T.ku;
+            const double u0 = acc ? T.u0[i] : 0.0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double fp2 = in[k][j * s];
+                const double v = r.A * (fp1[k] - fm1[k]) + r.B * (fp2 - fm2[k]) - r.m * wp[k];
+                w[k][i * s] = v;
+                if (acc) y0[k] += u0 * v;
+                wp[k] = v;
+                fm2[k] = fm1[k]; fm1[k] = f0c[k]; f0c[k] = fp1[k]; fp1[k] = fp2;
+            }
         }
     }
 
     // backward sweep
-    double fact = 0.0;
-    if (T.periodic) fact = (y0 + T.sm1 * wp) * T.sm2;
-    double yn = 0.0;
-    for (i = n - 1; i >= 0; --i) {
-        const double y = w[i * s] - rows[i].g * yn;
-        yn = y;
-        double xv = y;
-        if (T.periodic && (i < T.zlo || i >= T.zhi)) xv = y - fact * T.zz[i];
-        if (EPI == EPI_ACCUM) xv += out[i * s];
-        out[i * s] = xv;
+    double fact[K], yn[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        fact[k] = T.periodic ? (y0[k] + T.sm1 * wp[k]) * T.sm2 : 0.0;
+        yn[k] = 0.0;
     }
+    for (i = n - 1; i >= 0; --i) {
+        const double g = rows[i].g;
+        const bool corr = T.periodic && (i < T.zlo || i >= T.zhi);
+        const double z = corr ? T.zz[i] : 0.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double y = w[k][i * s] - g * yn[k];
+            yn[k] = y;
+            double xv = y;
+            if (corr) xv = y - fact[k] * z;
+            if (EPI == EPI_ACCUM) xv += out[k][i * s];
+            out[k][i * s] = xv;
+        }
+    }
+}
+
+// grid: (ceil(nx/blockDim.x), nother, ceil(nf/K)); block z-index g owns fields
+// K*g .. K*g+K-1 (the last group may hold fewer)
+template <int EPI, int K>
+__global__ void __launch_bounds__(128)
+k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os, int nf) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int o = blockIdx.y;
+    if (x >= nx || o >= nother) return;
+    const long base = x + (long)o * os;
+    const int f0 = blockIdx.z * K;
+    if (K == 2 && f0 + 1 < nf)
+        pencil_yz<EPI, K>(T, F, f0, base, s);
+    else
+        pencil_yz<EPI, 1>(T, F, f0, base, s);
 }
 
 // ---------------------------------------------------------------------------

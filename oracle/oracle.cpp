@@ -9,9 +9,11 @@
  * pencils / planes, so results do not depend on the thread count.
  *
  * Parity pinning: the reference ships no tests, golden vectors or fixtures
- * and its Fortran CPU path cannot be compiled here.  This restatement is
- * pinned by analytic known-answer tests (tests/test_oracle_*.py) and by the
- * golden vectors under tests/golden/ that it generated.
+ * and its Fortran CPU path cannot be compiled here.  Scheme C, cuDivergence,
+ * the WENO5 step and the ghost padding are pinned against outputs of the
+ * reference's own CUDA kernels (tests/golden/reference_cuda.npz); the
+ * Fortran-only parts are pinned by analytic known-answer tests only (parity
+ * unpinned against the reference for those).
  */
 #include "oracle.h"
 

@@ -17,10 +17,12 @@
  *
  * Parity pinning: the reference has no tests, golden vectors or fixtures,
  * and its Fortran CPU path cannot be compiled here (no Fortran compiler).
- * The restatement is pinned by analytic known-answer tests (modified
- * wavenumber, polynomial exactness, WENO5 linear-weight limit) and by
- * committed golden vectors generated from this restatement; see the test
- * suite for what each pin covers.
+ * Scheme C, cuDivergence, the WENO5 TVD-RK3 step and the ghost padding are
+ * pinned against outputs of the reference's own CUDA kernels run on a GPU
+ * (tests/golden/reference_cuda.npz); the Fortran-only parts (schemes A, B and
+ * cyclic B, flujos, the SGS models, the RK loop) are pinned by analytic
+ * known-answer tests only -- parity against the reference's own outputs is
+ * unpinned for those.
  */
 #ifndef EMIX_ORACLE_H
 #define EMIX_ORACLE_H
