@@ -76,135 +76,95 @@ EMIX_DEV double rhs_row(const DerivTable &T, const double *__restrict__ fp, long
 //   axis 2 (z): pencils (x, y), element stride nx*ny, other stride nx
 // grid: (ceil(nx/blockDim.x), nother, nf)
 // ---------------------------------------------------------------------------
-// K fields of one pencil in lockstep: K independent dependency chains per
-// thread, interleaved so that the FP64 pipe always has work (ILP).
-template <int EPI, int K>
-EMIX_DEV void pencil_yz(const DerivTable &T, const PencilFields &F, int f0, long base, long s) {
-    const double *in[K];
-    double *w[K], *out[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        in[k] = pick(F.in, f0 + k) + base;
-        w[k] = pick(F.w, f0 + k) + base;
-        out[k] = pick(F.out, f0 + k) + base;
-    }
-    const int n = T.n;
-    const DerivRow *__restrict__ rows = T.rows;
-
-    // forward sweep
-    double wp[K], y0[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) { wp[k] = 0.0; y0[k] = 0.0; }
-    int i = 0;
-    if (!T.periodic) {
-        for (; i < T.nlo; ++i) {
-            const double m = rows[i].m;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const double v = rhs_row(T, in[k], s, i) - m * wp[k];
-                w[k][i * s] = v;
-                wp[k] = v;
-            }
-        }
-        const int iend = n - T.nhi;
-        if (i < iend) {
-            double fm2[K], fm1[K], f0c[K], fp1[K];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                fm2[k] = in[k][(i - 2) * s]; fm1[k] = in[k][(i - 1) * s];
-                f0c[k] = in[k][i * s]; fp1[k] = in[k][(i + 1) * s];
-            }
-            for (; i < iend; ++i) {
-                const DerivRow r = rows[i];
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const double fp2 = in[k][(i + 2) * s];
-                    const double v = r.A * (fp1[k] - fm1[k]) + r.B * (fp2 - fm2[k]) - r.m * wp[k];
-                    w[k][i * s] = v;
-                    wp[k] = v;
-                    fm2[k] = fm1[k]; fm1[k] = f0c[k]; f0c[k] = fp1[k]; fp1[k] = fp2;
-                }
-            }
-        }
-        for (; i < n; ++i) {
-            const double m = rows[i].m;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const double v = rhs_row(T, in[k], s, i) - m * wp[k];
-                w[k][i * s] = v;
-                wp[k] = v;
-            }
-        }
-    } else {
-        double fm2[K], fm1[K], f0c[K], fp1[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            fm2[k] = in[k][(n - 2) * s]; fm1[k] = in[k][(n - 1) * s];
-            f0c[k] = in[k][0]; fp1[k] = in[k][s];
-        }
-        for (; i < n; ++i) {
-            int j = i + 2;
-            if (j >= n) j -= n;
-            const DerivRow r = rows[i];
-            const bool acc = i < T.ku;
-            const double u0 = acc ? T.u0[i] : 0.0;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const double fp2 = in[k][j * s];
-                const double v = r.A * (fp1[k] - fm1[k]) + r.B * (fp2 - fm2[k]) - r.m * wp[k];
-                w[k][i * s] = v;
-                if (acc) y0[k] += u0 * v;
-                wp[k] = v;
-                fm2[k] = fm1[k]; fm1[k] = f0c[k]; f0c[k] = fp1[k]; fp1[k] = fp2;
-            }
-        }
-    }
-
-    // backward sweep
-    double fact[K], yn[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        fact[k] = T.periodic ? (y0[k] + T.sm1 * wp[k]) * T.sm2 : 0.0;
-        yn[k] = 0.0;
-    }
-    for (i = n - 1; i >= 0; --i) {
-        const double g = rows[i].g;
-        const bool corr = T.periodic && (i < T.zlo || i >= T.zhi);
-        const double z = corr ? T.zz[i] : 0.0;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const double y = w[k][i * s] - g * yn[k];
-            yn[k] = y;
-            double xv = y;
-            if (corr) xv = y - fact[k] * z;
-            if (EPI == EPI_ACCUM) xv += out[k][i * s];
-            out[k][i * s] = xv;
-        }
-    }
-}
-
-// grid: (ceil(nx/blockDim.x), nother, ceil(nf/K)); block z-index g owns fields
-// K*g .. K*g+K-1 (the last group may hold fewer)
-template <int EPI, int K>
+// grid: (ceil(nx/blockDim.x), nother, nf); blockIdx.z = field
+template <int EPI>
 __global__ void __launch_bounds__(128)
-k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os, int nf) {
+k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int o = blockIdx.y;
     if (x >= nx || o >= nother) return;
     const long base = x + (long)o * os;
-    const int f0 = blockIdx.z * K;
-    if (K == 2 && f0 + 1 < nf)
-        pencil_yz<EPI, K>(T, F, f0, base, s);
-    else
-        pencil_yz<EPI, 1>(T, F, f0, base, s);
+    const int f = blockIdx.z;
+    const double *__restrict__ in = pick(F.in, f) + base;
+    double *w = pick(F.w, f) + base;
+    double *out = pick(F.out, f) + base;
+    const int n = T.n;
+    const DerivRow *__restrict__ rows = T.rows;
+
+    // forward sweep; the input two rows ahead is loaded one iteration early
+    double wp = 0.0, y0 = 0.0;
+    int i = 0;
+    if (!T.periodic) {
+        for (; i < T.nlo; ++i) {
+            const double v = rhs_row(T, in, s, i) - rows[i].m * wp;
+            w[i * s] = v;
+            wp = v;
+        }
+        const int iend = n - T.nhi;
+        if (i < iend) {
+            double fm2 = in[(i - 2) * s], fm1 = in[(i - 1) * s], f0 = in[i * s], fp1 = in[(i + 1) * s];
+            double nxt = in[(i + 2) * s];
+            for (; i < iend; ++i) {
+                const double fp2 = nxt;
+                if (i + 3 < n) nxt = in[(i + 3) * s];
+                const DerivRow r = rows[i];
+                const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
+                w[i * s] = v;
+                wp = v;
+                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+            }
+        }
+        for (; i < n; ++i) {
+            const double v = rhs_row(T, in, s, i) - rows[i].m * wp;
+            w[i * s] = v;
+            wp = v;
+        }
+    } else {
+        double fm2 = in[(n - 2) * s], fm1 = in[(n - 1) * s], f0 = in[0], fp1 = in[s];
+        double nxt = in[2 * s];
+        for (; i < n; ++i) {
+            const double fp2 = nxt;
+            int j = i + 3;
+            if (j >= n) j -= n;
+            nxt = in[j * s];
+            const DerivRow r = rows[i];
+            const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
+            w[i * s] = v;
+            if (i < T.ku) y0 += T.u0[i] * v;
+            wp = v;
+            fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+        }
+    }
+
+    // backward sweep; w one row ahead
+    double fact = 0.0;
+    if (T.periodic) fact = (y0 + T.sm1 * wp) * T.sm2;
+    double yn = 0.0;
+    double wn = w[(n - 1) * s];
+    for (i = n - 1; i >= 0; --i) {
+        const double wi = wn;
+        if (i > 0) wn = w[(i - 1) * s];
+        const double y = wi - rows[i].g * yn;
+        yn = y;
+        double xv = y;
+        if (T.periodic && (i < T.zlo || i >= T.zhi)) xv = y - fact * T.zz[i];
+        if (EPI == EPI_ACCUM) xv += out[i * s];
+        out[i * s] = xv;
+    }
 }
 
 // ---------------------------------------------------------------------------
-// x pencils: a warp owns 32 consecutive pencils (flattened (j,k)); chunks of
-// 32 rows go through a per-warp [32][33] shared tile.
+// x pencils: a warp owns 32 consecutive pencils (flattened (j,k)).  Rows are
+// staged 32 at a time (plus a 2-row look-ahead) through a per-warp shared tile
+// with coalesced loads; each lane then walks its own pencil through the tile
+// with the same register sliding window as the y/z kernel, writes w back into
+// the tile, and the tile is stored coalesced.  The backward sweep streams the
+// chunks in reverse the same way.
 // grid: (ceil(npencil / (32*warps_per_block)), 1, nf); block 32*warps
 // ---------------------------------------------------------------------------
-constexpr int kXTile = 32 * 33;
+constexpr int kXRows = 34;          // 32 rows + 2 look-ahead
+constexpr int kXLd = kXRows + 1;    // padded leading dimension (odd: no bank conflicts)
+constexpr int kXTile = 32 * kXLd;
 
 template <int EPI>
 __global__ void __launch_bounds__(128)
@@ -221,28 +181,72 @@ k_deriv_x(DerivTable T, PencilFields F, long npencil) {
     double *w = pick(F.w, f) + p0 * n;
     double *out = pick(F.out, f) + p0 * n;
     const DerivRow *__restrict__ rows = T.rows;
+    double *t = tile + lane * kXLd;      // this lane's pencil in the tile
+    const bool mine = lane < npw;
 
+    // registers of the walk (lane = pencil)
     double wp = 0.0, y0 = 0.0;
+    double fm2 = 0.0, fm1 = 0.0, f0 = 0.0, fp1 = 0.0;
+    double head0 = 0.0, head1 = 0.0, head2 = 0.0, head3 = 0.0;   // f_0..f_3 (closures, wrap)
+    double tail0 = 0.0, tail1 = 0.0, tail2 = 0.0, tail3 = 0.0;   // f_{n-1}..f_{n-4}
+    if (T.periodic && mine) {
+        fm2 = in[(long)lane * n + n - 2];
+        fm1 = in[(long)lane * n + n - 1];
+    }
     for (int c0 = 0; c0 < n; c0 += 32) {
-        const int cl = min(32, n - c0);
-        if (lane < cl) {
-            const int i = c0 + lane;
-            for (int q = 0; q < npw; ++q) tile[q * 33 + lane] = rhs_row(T, in + (long)q * n, 1, i);
+        const int cl = min(32, n - c0);             // rows completed in this chunk
+        const int ld = min(kXRows, n - c0);         // rows loaded (with look-ahead)
+        // coalesced load: row r of pencil q -> tile[q][r]
+        for (int q = 0; q < npw; ++q) {
+            const double *src = in + (long)q * n + c0;
+            if (lane < ld) tile[q * kXLd + lane] = src[lane];
+            if (lane + 32 < ld) tile[q * kXLd + lane + 32] = src[lane + 32];
         }
         __syncwarp();
-        if (lane < npw) {
-            double *t = tile + lane * 33;
-            for (int r = 0; r < cl; ++r) {
+        if (mine) {
+            int r = 0;
+            if (c0 == 0) {
+                head0 = t[0]; head1 = t[1]; head2 = t[2]; head3 = t[3];
+                if (T.periodic) {
+                    f0 = head0; fp1 = head1;   // fm2, fm1 hold f_{n-2}, f_{n-1}
+                } else {
+                    // the table builder guarantees nlo == 2: rows 0 and 1 are
+                    // closures on f_0..f_3, and the window of row 2 is f_0..f_3
+                    fm2 = head0; fm1 = head1; f0 = head2; fp1 = head3;
+                    for (; r < T.nlo; ++r) {
+                        const double *c = T.clo + 4 * r;
+                        const double v = c[0] * head0 + c[1] * head1 + c[2] * head2 + c[3] * head3 -
+                                         rows[r].m * wp;
+                        t[r] = v;
+                        wp = v;
+                    }
+                }
+            }
+            for (; r < cl; ++r) {
                 const int i = c0 + r;
-                const double v = t[r] - rows[i].m * wp;
-                t[r] = v;
+                if (!T.periodic && i >= n - T.nhi) {
+                    // closures on f_{n-1}..f_{n-4} (nhi == 2): at row n-2 the
+                    // window holds exactly those four values
+                    if (i == n - T.nhi) { tail0 = fp1; tail1 = f0; tail2 = fm1; tail3 = fm2; }
+                    const double *c = T.chi + 4 * (n - 1 - i);
+                    const double v = c[0] * tail0 + c[1] * tail1 + c[2] * tail2 + c[3] * tail3 -
+                                     rows[i].m * wp;
+                    t[r] = v;
+                    wp = v;
+                    continue;
+                }
+                const double fp2 = (i + 2 < n) ? t[r + 2] : (i + 2 == n ? head0 : head1);
+                const DerivRow rw = rows[i];
+                const double v = rw.A * (fp1 - fm1) + rw.B * (fp2 - fm2) - rw.m * wp;
                 if (T.periodic && i < T.ku) y0 += T.u0[i] * v;
+                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+                t[r] = v;
                 wp = v;
             }
         }
         __syncwarp();
-        if (lane < cl)
-            for (int q = 0; q < npw; ++q) w[(long)q * n + c0 + lane] = tile[q * 33 + lane];
+        for (int q = 0; q < npw; ++q)
+            if (lane < cl) w[(long)q * n + c0 + lane] = tile[q * kXLd + lane];
         __syncwarp();
     }
 
@@ -251,11 +255,10 @@ k_deriv_x(DerivTable T, PencilFields F, long npencil) {
     double yn = 0.0;
     for (int c0 = ((n - 1) / 32) * 32; c0 >= 0; c0 -= 32) {
         const int cl = min(32, n - c0);
-        if (lane < cl)
-            for (int q = 0; q < npw; ++q) tile[q * 33 + lane] = w[(long)q * n + c0 + lane];
+        for (int q = 0; q < npw; ++q)
+            if (lane < cl) tile[q * kXLd + lane] = w[(long)q * n + c0 + lane];
         __syncwarp();
-        if (lane < npw) {
-            double *t = tile + lane * 33;
+        if (mine) {
             for (int r = cl - 1; r >= 0; --r) {
                 const int i = c0 + r;
                 const double y = t[r] - rows[i].g * yn;
@@ -266,9 +269,9 @@ k_deriv_x(DerivTable T, PencilFields F, long npencil) {
             }
         }
         __syncwarp();
-        if (lane < cl) {
-            for (int q = 0; q < npw; ++q) {
-                double v = tile[q * 33 + lane];
+        for (int q = 0; q < npw; ++q) {
+            if (lane < cl) {
+                double v = tile[q * kXLd + lane];
                 double *o = out + (long)q * n + c0 + lane;
                 if (EPI == EPI_ACCUM) v += *o;
                 *o = v;

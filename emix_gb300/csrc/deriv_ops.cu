@@ -33,13 +33,6 @@ void set_last_message(const char *msg) { t_last_error = msg ? msg : ""; }
 const char *last_error() { return t_last_error.c_str(); }
 
 // ---- launch helper ------------------------------------------------------
-// fields per thread in the y/z pencil kernel (1 or 2); EMIX_YZ_ILP overrides
-static int yz_ilp_default() {
-    const char *e = getenv("EMIX_YZ_ILP");
-    return (e && e[0] == '1') ? 1 : 2;
-}
-static int g_yz_ilp = yz_ilp_default();
-
 int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
                  double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st) {
     if (nf < 1 || nf > kMaxFields) return EMIX_ERR_ARG;
@@ -67,19 +60,11 @@ int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *c
         const long s = axis == 1 ? (long)nx : (long)nx * ny;
         const long os = axis == 1 ? (long)nx * ny : (long)nx;
         if (nother > 65535) return EMIX_ERR_ARG;
-        const int K = g_yz_ilp;
-        dim3 grid((nx + bs - 1) / bs, nother, (nf + K - 1) / K);
-        if (K == 2) {
-            if (epi == EPI_STORE)
-                k_deriv_yz<EPI_STORE, 2><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os, nf);
-            else
-                k_deriv_yz<EPI_ACCUM, 2><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os, nf);
-        } else {
-            if (epi == EPI_STORE)
-                k_deriv_yz<EPI_STORE, 1><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os, nf);
-            else
-                k_deriv_yz<EPI_ACCUM, 1><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os, nf);
-        }
+        dim3 grid((nx + bs - 1) / bs, nother, nf);
+        if (epi == EPI_STORE)
+            k_deriv_yz<EPI_STORE><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os);
+        else
+            k_deriv_yz<EPI_ACCUM><<<grid, bs, 0, st>>>(T, F, nx, nother, s, os);
     }
     EMIX_CUDA_TRY(cudaGetLastError());
     return EMIX_OK;

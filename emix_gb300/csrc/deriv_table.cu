@@ -141,6 +141,9 @@ int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow 
         ++t.nhi;
     }
 
+    // the pencil kernels assume two explicit closure rows at each wall
+    if (!per && (t.nlo != 2 || t.nhi != 2)) return EMIX_ERR_ARG;
+
     t.ku = 0; t.zlo = 0; t.zhi = n; t.sm1 = 0.0; t.sm2 = 0.0;
     if (per) {
         // zz = A'^{-1} (gamma, 0, ..., 0, alpha): same forward/backward sweep

@@ -64,7 +64,7 @@ __global__ void k_flux_one(int neq, double *__restrict__ e, double *__restrict__
     }
 }
 
-__global__ void k_flux_all(FluxArgs a) {
+__global__ void __launch_bounds__(256, 2) k_flux_all(FluxArgs a) {
     const long n = a.n;
     EMIX_FOR_CELLS(q, n) {
         const double r = a.um[q];

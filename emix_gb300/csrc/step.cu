@@ -50,7 +50,7 @@ struct emix_ctx {
     double *arena = nullptr;
     size_t arena_bytes = 0;
     double *um0, *um, *u, *pres, *dvel, *vis, *amut, *vort, *flux, *R, *W, *jbn, *jx, *jy, *jz,
-        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB;
+        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB, *wenoC, *wenoE;
     DerivTable T[3];
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -124,6 +124,15 @@ int issue_step(emix_ctx *c) {
             a.nxg = nx + 2 * g; a.nyg = ny + 2 * g; a.nzg = nz + 2 * g; a.g = g;
             a.sx = 1.0 / p.h[0]; a.sy = 1.0 / p.h[1]; a.sz = 1.0 / p.h[2];
             a.dt = p.dt; a.stage = s; a.ref_bugs = p.ref_bugs;
+            a.wc = c->wenoC; a.we = c->wenoE;
+            // stage 3 writes only the interior, so stage 2 is needed only within
+            // the 3-cell reach of the WENO5 stencil around it, and stage 3 only on
+            // the interior (stage 1 covers the whole padded grid)
+            const int dims[3] = {nx, ny, nz};
+            for (int d = 0; d < 3; ++d) {
+                if (s == 2) { a.r0[d] = g - 3; a.rn[d] = dims[d] + 6; }
+                if (s == 3) { a.r0[d] = g; a.rn[d] = dims[d]; }
+            }
             ProfScope ps(c, CLS_WENO);
             if ((rc = launch_weno_stage(a, st))) return rc;
             ++launches;
@@ -243,7 +252,7 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
         if (rc) { delete c; return rc; }
     }
     const bool sf = p->sgs_model == EMIX_SGS_STRUCTURE;
-    const long nfield = 5 + 5 + 3 + 1 + 9 + 1 + 15 + 5 + 5 + 11 + 3 + 1 + 1 + (p->level_set ? 1 : 0) +
+    const long nfield = 5 + 5 + 3 + 1 + 9 + 1 + 15 + 5 + 5 + 11 + 3 + 1 + 1 + (p->level_set ? 7 : 0) +
                         (sf ? 1 + 3 + 6 : 0);
     const size_t bytes = ((size_t)nfield * n + 3 * (size_t)ng) * sizeof(double);
     if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
@@ -260,6 +269,8 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     c->W = take(5 * n); c->jbn = take(11 * n); c->jx = take(n); c->jy = take(n); c->jz = take(n);
     c->mask = take(n); c->dxyz = take(n);
     c->phi = p->level_set ? take(n) : nullptr;
+    c->wenoC = p->level_set ? take(3 * n) : nullptr;
+    c->wenoE = p->level_set ? take(3 * n) : nullptr;
     c->amut = sf ? take(n) : nullptr;
     c->vort = sf ? take(3 * n) : nullptr;
     c->ratios = sf ? take(6 * n) : nullptr;
@@ -318,6 +329,9 @@ int emix_ctx_set_static(emix_ctx *c, const double *jbn, const double *mask, cons
     double *ratios = c->ratios ? c->ratios : c->flux + 3 * n;
     k_sgs_setup<<<cells_grid(n), 256, 0, st>>>(c->flux, c->dxyz, ratios, p.nx, p.ny, p.nz);
     k_metric_products<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->jx, c->jy, c->jz, n);
+    if (p.level_set)
+        k_weno_scales<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->wenoC, c->wenoE, 1.0 / p.h[0],
+                                                     1.0 / p.h[1], 1.0 / p.h[2], n);
     EMIX_CUDA_TRY(cudaGetLastError());
     EMIX_CUDA_TRY(cudaStreamSynchronize(st));
     c->static_set = true;

@@ -10,10 +10,12 @@ namespace {
 
 // Jiang-Peng WENO5 reconstruction from five differences (Phi_x_WENO,
 // src/LevelSet/lsTools.cu:9-50).  Same weights 0.1/0.6/0.3 and
-// epsilon = 1e-6 on (beta + eps)^2; rearranged to one division:
+// epsilon = 1e-6 on (beta + eps)^2; rearranged to one reciprocal:
 //   12*beta_k = 13 d_k^2 + 3 e_k^2,  alpha_k ~ c_k / (12 beta_k + 12 eps)^2,
 //   result = sum(w_k q_k) / (6 sum w_k),  w_1 = 0.1 t_2 t_3, ...
-EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5) {
+// eps12 is 12*epsilon for differences already scaled by the metric, or
+// 12*epsilon/C^2 for unscaled differences (WENO(C v; eps) = C WENO(v; eps/C^2)).
+EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5, double eps12) {
     const double d1 = fma(-2.0, v2, v1 + v3);
     const double e1 = fma(-4.0, v2, fma(3.0, v3, v1));
     const double d2 = fma(-2.0, v3, v2 + v4);
@@ -23,7 +25,6 @@ EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5) {
     const double s1 = fma(13.0 * d1, d1, (3.0 * e1) * e1);
     const double s2 = fma(13.0 * d2, d2, (3.0 * e2) * e2);
     const double s3 = fma(13.0 * d3, d3, (3.0 * e3) * e3);
-    constexpr double eps12 = 12.0e-6;
     double t1 = s1 + eps12; t1 *= t1;
     double t2 = s2 + eps12; t2 *= t2;
     double t3 = s3 + eps12; t3 *= t3;
@@ -35,7 +36,7 @@ EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5) {
     const double q3 = fma(5.0, v4, fma(2.0, v3, -v5));
     const double num = fma(w1, q1, fma(w2, q2, w3 * q3));
     const double den = 6.0 * (w1 + w2 + w3);
-    return num / den;
+    return num * rcp_newton(den);
 }
 
 // Positions (0..n-1) of the five differences for the left-biased (u >= 0)
@@ -78,7 +79,9 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
     __shared__ double Dz[kWZ + 5][kWY][kWX];
 
     const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
-    const int x0 = blockIdx.x * kWX, y0 = blockIdx.y * kWY, z0 = blockIdx.z * kWZ;
+    const int x0 = a.r0[0] + blockIdx.x * kWX, y0 = a.r0[1] + blockIdx.y * kWY,
+              z0 = a.r0[2] + blockIdx.z * kWZ;
+    const int xe = a.r0[0] + a.rn[0], ye = a.r0[1] + a.rn[1], ze = a.r0[2] + a.rn[2];
     const long sxy = (long)nxg * nyg;
     const double *__restrict__ phi = a.phi;
     const int tid = threadIdx.x + kWX * (threadIdx.y + kWY * threadIdx.z);
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
 
     const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
     const int X = x0 + tx, Y = y0 + ty, Z = z0 + tz;
-    if (X >= nxg || Y >= nyg || Z >= nzg) return;
+    if (X >= xe || Y >= ye || Z >= ze) return;
     const long id = X + (long)nxg * Y + sxy * Z;
 
     // velocity and metric at the cell
@@ -136,7 +139,20 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
         nv = sxy * nzg;
     }
     const double ux = a.vel[iv], uy = a.vel[nv + iv], uz = a.vel[2 * nv + iv];
-    const double cx = a.jbn[iv] * a.sx, cy = a.jbn[4 * nv + iv] * a.sy, cz = a.jbn[8 * nv + iv] * a.sz;
+    // scale of the differences: either multiply the five differences by
+    // C = jbn/h (as the reference does) or use the precomputed per-cell
+    // factors and rescale epsilon instead (one multiply per direction)
+    const bool pre = a.wc != nullptr;
+    double cx, cy, cz, ex, ey, ez, mx, my, mz;
+    if (pre) {
+        cx = 1.0; cy = 1.0; cz = 1.0;
+        mx = a.wc[iv]; my = a.wc[nv + iv]; mz = a.wc[2 * nv + iv];
+        ex = a.we[iv]; ey = a.we[nv + iv]; ez = a.we[2 * nv + iv];
+    } else {
+        cx = a.jbn[iv] * a.sx; cy = a.jbn[4 * nv + iv] * a.sy; cz = a.jbn[8 * nv + iv] * a.sz;
+        mx = 1.0; my = 1.0; mz = 1.0;
+        ex = 12.0e-6; ey = 12.0e-6; ez = 12.0e-6;
+    }
 
     int p[5];
     double rs;
@@ -145,17 +161,25 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
         if (__double_as_longlong(ux) >= 0) stencil_left(X, nxg, p); else stencil_right(X, nxg, p);
         const double *d = &Dx[tz][ty][0];
         const int o = x0 - 2;
-        const double phx = weno5(d[p[0] - o] * cx, d[p[1] - o] * cx, d[p[2] - o] * cx,
-                                 d[p[3] - o] * cx, d[p[4] - o] * cx);
+        double phx;
+        if (pre)
+            phx = mx * weno5(d[p[0] - o], d[p[1] - o], d[p[2] - o], d[p[3] - o], d[p[4] - o], ex);
+        else
+            phx = weno5(d[p[0] - o] * cx, d[p[1] - o] * cx, d[p[2] - o] * cx, d[p[3] - o] * cx,
+                        d[p[4] - o] * cx, ex);
         rs = ux * phx;
     }
     // y
     {
         if (__double_as_longlong(uy) >= 0) stencil_left(Y, nyg, p); else stencil_right(Y, nyg, p);
         const int o = y0 - 2;
-        const double phy = weno5(Dy[tz][p[0] - o][tx] * cy, Dy[tz][p[1] - o][tx] * cy,
-                                 Dy[tz][p[2] - o][tx] * cy, Dy[tz][p[3] - o][tx] * cy,
-                                 Dy[tz][p[4] - o][tx] * cy);
+        const double v1 = Dy[tz][p[0] - o][tx], v2 = Dy[tz][p[1] - o][tx], v3 = Dy[tz][p[2] - o][tx],
+                     v4 = Dy[tz][p[3] - o][tx], v5 = Dy[tz][p[4] - o][tx];
+        double phy;
+        if (pre)
+            phy = my * weno5(v1, v2, v3, v4, v5, ey);
+        else
+            phy = weno5(v1 * cy, v2 * cy, v3 * cy, v4 * cy, v5 * cy, ey);
         rs = rs + uy * phy;
     }
     // z
@@ -171,8 +195,13 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
             const long ib = X + (long)nxg * Yb + sxy * Z;
             v5 = phi[ib] - phi[ib - sxy];
         }
-        const double phz = weno5(Dz[p[0] - o][ty][tx] * cz, Dz[p[1] - o][ty][tx] * cz,
-                                 Dz[p[2] - o][ty][tx] * cz, Dz[p[3] - o][ty][tx] * cz, v5 * cz);
+        const double v1 = Dz[p[0] - o][ty][tx], v2 = Dz[p[1] - o][ty][tx], v3 = Dz[p[2] - o][ty][tx],
+                     v4 = Dz[p[3] - o][ty][tx];
+        double phz;
+        if (pre)
+            phz = mz * weno5(v1, v2, v3, v4, v5, ez);
+        else
+            phz = weno5(v1 * cz, v2 * cz, v3 * cz, v4 * cz, v5 * cz, ez);
         rs = rs + uz * phz;
     }
 
@@ -194,6 +223,17 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
             a.out[I + (long)nx * (J + (long)ny * K)] = v;
     } else {
         a.out[id] = v;
+    }
+}
+
+__global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
+                              double *__restrict__ we, double sx, double sy, double sz, long n) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double c[3] = {jbn[q] * sx, jbn[4 * n + q] * sy, jbn[8 * n + q] * sz};
+        for (int d = 0; d < 3; ++d) {
+            wc[d * n + q] = c[d];
+            we[d * n + q] = 12.0e-6 / (c[d] * c[d]);
+        }
     }
 }
 
@@ -224,9 +264,15 @@ __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict
     }
 }
 
-int launch_weno_stage(const WenoArgs &a, cudaStream_t st) {
+int launch_weno_stage(const WenoArgs &a_in, cudaStream_t st) {
+    WenoArgs a = a_in;
+    const int dims[3] = {a.nxg, a.nyg, a.nzg};
+    for (int d = 0; d < 3; ++d) {
+        if (a.rn[d] <= 0) { a.r0[d] = 0; a.rn[d] = dims[d]; }   // default: whole padded grid
+        if (a.r0[d] < 0 || a.r0[d] + a.rn[d] > dims[d]) return EMIX_ERR_ARG;
+    }
     dim3 block(kWX, kWY, kWZ);
-    dim3 grid((a.nxg + kWX - 1) / kWX, (a.nyg + kWY - 1) / kWY, (a.nzg + kWZ - 1) / kWZ);
+    dim3 grid((a.rn[0] + kWX - 1) / kWX, (a.rn[1] + kWY - 1) / kWY, (a.rn[2] + kWZ - 1) / kWZ);
     if (grid.y > 65535 || grid.z > 65535) return EMIX_ERR_ARG;
     k_weno_stage<<<grid, block, 0, st>>>(a);
     EMIX_CUDA_TRY(cudaGetLastError());
