@@ -183,6 +183,51 @@ def run_reference(args):
     return 0
 
 
+def ensemble_leg(steps: int, warmup: int, stream=None):
+    """The uneven 48-grid ensemble (seed 7): batched persistent launches (autotuned,
+    graph-replayed) against the same grids stepped one by one (each grid's own
+    graph).  Returns a dict for the JSON line."""
+    import torch
+    from emix_gb300 import fields as F
+    from emix_gb300 import ops
+    ws = F.ensemble(ngrids=48, seed=7)
+    b = ops.Batch(ws)
+    s = stream or torch.cuda.Stream()
+    b.set_stream(s.cuda_stream)
+    tuned_ms = b.autotune(nsteps=2)
+    ncell = b.ncell
+
+    def timed(fn):
+        b.upload()
+        fn(warmup)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        fn(steps)
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_b = timed(lambda k: b.step(k, use_graph=True))
+    ms_g = timed(lambda k: b.step_per_grid(k, use_graph=True))
+    # the batched result agrees with the per-grid result (to rounding)
+    b.upload(); b.step(1, use_graph=True); a0 = b.download(0)[0]
+    b.upload(); b.step_per_grid(1, use_graph=True); a1 = b.download(0)[0]
+    diff = float(np.max(np.abs(a0 - a1)) / np.max(np.abs(a1)))
+    tune = b.tuning()
+    b.close()
+    return {
+        "workload": "48 periodic grids, nx,ny,nz each from {32,48,...,160} (seed 7), omega~U[0.5,2]",
+        "cells": ncell, "steps": steps,
+        "batched": {"value": round(ncell / (ms_b * 1e-3) / 1e6, 3), "ms_per_step": round(ms_b, 3)},
+        "per_grid": {"value": round(ncell / (ms_g * 1e-3) / 1e6, 3), "ms_per_step": round(ms_g, 3)},
+        "speedup": round(ms_g / ms_b, 3), "max_rel_diff_vs_per_grid": diff,
+        "tuning": {"cells_per_thread": tune[0], "yz_block": tune[1], "ctas_per_sm": tune[2],
+                   "autotune_best_ms": round(tuned_ms, 3)},
+    }
+
+
 def config_dict(w):
     return {
         "workload": f"stirred tank {N_GRID}^3 walls, RK3 step with WENO5 level set",
@@ -202,6 +247,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="emix", choices=["emix", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -318,6 +364,8 @@ def main():
         "kernels": kernels,
         "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
     }
+    if not args.no_ensemble:
+        line["ensemble"] = ensemble_leg(min(args.steps, 10), 3, stream)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sec, thr = cpu_sample(2, 1)
         line["cpu_baseline"] = {

@@ -35,6 +35,7 @@ class EmixParams(C.Structure):
         ("cs", C.c_double), ("amu0", C.c_double), ("c4", C.c_double),
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
+        ("bc_walls", C.c_int),
     ]
 
 
@@ -79,6 +80,22 @@ PROTOTYPES = {
     "emix_profile_class_count": (C.c_int, []),
     "emix_profile_class_name": (C.c_char_p, [C.c_int]),
     "emix_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "emix_bc_walls_dev": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, vp]),
+    "emix_cfl_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int,
+                               C.POINTER(C.c_double), vp]),
+    "emix_tstep_dt": (C.c_int, [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+    "emix_metrics_dev": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                   C.c_int, C.c_int, C.c_int, vp]),
+    "emix_batch_create": (C.c_int, [C.c_int, C.POINTER(EmixParams), C.POINTER(vp)]),
+    "emix_batch_destroy": (C.c_int, [vp]),
+    "emix_batch_grid": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+    "emix_batch_set_stream": (C.c_int, [vp, vp]),
+    "emix_batch_step": (C.c_int, [vp, C.c_int, C.c_int]),
+    "emix_batch_step_per_grid": (C.c_int, [vp, C.c_int, C.c_int]),
+    "emix_batch_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+    "emix_batch_get_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]),
+    "emix_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -1,0 +1,519 @@
+// batch.cu -- many independent grids of uneven size advanced together.
+//
+// A batch owns one context per grid (each with its own arena, tables and
+// plan).  Position k of every plan is the same kernel kind, so a batched step
+// issues one launch per position: a persistent kernel whose CTAs walk a work
+// list of (grid, virtual block) items covering every grid's launch of that
+// position.  Small grids, which alone fill a fraction of the GPU and are
+// bound by launch overhead, then share the machine.  The step is captured in
+// a CUDA graph.  The work-list granularity (pencils per y/z block, cells per
+// pointwise item, resident CTAs per SM) is chosen by a timing autotuner.
+#include "plan.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+// the single-grid context (step.cu)
+struct emix_ctx;
+namespace emix {
+const std::vector<Launch> &ctx_plan(emix_ctx *c);
+int ctx_ready(emix_ctx *c);
+} // namespace emix
+
+namespace emix {
+namespace {
+
+// grid owning virtual block vb: largest g with start[g] <= vb
+EMIX_DEV int find_grid(const long *__restrict__ start, int ngrid, long vb) {
+    int lo = 0, hi = ngrid - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= vb) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct Shape {
+    int gx, gy, gz, aux;
+};
+
+// pointwise bodies over `cpb` x 256 cells per virtual block
+struct PrimOp { using A = PrimArgs; static EMIX_DEV void cell(const A &a, long q) { prim_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct PadOp { using A = PadArgs; static EMIX_DEV void cell(const A &a, long q) { pad_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.ng; } };
+struct SmagOp { using A = SmagArgs; static EMIX_DEV void cell(const A &a, long q) { smag_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct SfOp { using A = SfArgs; static EMIX_DEV void cell(const A &a, long q) { sf_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct VortOp { using A = VortArgs; static EMIX_DEV void cell(const A &a, long q) { vort_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct SelOp { using A = SelArgs; static EMIX_DEV void cell(const A &a, long q) { select_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct FluxOp { using A = FluxArgs; static EMIX_DEV void cell(const A &a, long q) { flux_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct BcOp { using A = BcArgs; static EMIX_DEV void cell(const A &a, long q) { bc_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return bc_count(a); } };
+struct RkOp { using A = RkArgs; static EMIX_DEV void cell(const A &a, long q) { rk_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+
+template <class Op>
+__global__ void __launch_bounds__(256, 2)
+k_batch_cells(const typename Op::A *__restrict__ args, const long *__restrict__ start, int ngrid,
+              int cpb) {
+    const long total = start[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int g = find_grid(start, ngrid, vb);
+        const typename Op::A &a = args[g];
+        const long n = Op::cnt(a);
+        const long q0 = (vb - start[g]) * 256L * cpb + threadIdx.x;
+        for (int k = 0; k < cpb; ++k) {
+            const long q = q0 + 256L * k;
+            if (q < n) Op::cell(a, q);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kWX *kWY *kWZ)
+k_batch_weno(const WenoArgs *__restrict__ args, const long *__restrict__ start,
+             const Shape *__restrict__ shape, int ngrid) {
+    const long total = start[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int g = find_grid(start, ngrid, vb);
+        const long local = vb - start[g];
+        const Shape sh = shape[g];
+        const uint3 bid = make_uint3((unsigned)(local % sh.gx), (unsigned)((local / sh.gx) % sh.gy),
+                                     (unsigned)(local / ((long)sh.gx * sh.gy)));
+        weno_stage_body(args[g], bid, threadIdx);
+        __syncthreads();   // the difference tiles are refilled by the next item
+    }
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128)
+k_batch_deriv_x(const DerivArgs *__restrict__ args, const long *__restrict__ start,
+                const Shape *__restrict__ shape, int ngrid) {
+    extern __shared__ double smem[];
+    const long total = start[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int g = find_grid(start, ngrid, vb);
+        const long local = vb - start[g];
+        const Shape sh = shape[g];
+        const DerivArgs &a = args[g];
+        const uint3 bid = make_uint3((unsigned)(local % sh.gx), 0u, (unsigned)(local / sh.gx));
+        deriv_x_body<EPI>(a.T, a.F, (long)a.ny * a.nz, bid, threadIdx.x, blockDim.x >> 5, smem);
+    }
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128)
+k_batch_deriv_yz(const DerivArgs *__restrict__ args, const long *__restrict__ start,
+                 const Shape *__restrict__ shape, int ngrid) {
+    const long total = start[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int g = find_grid(start, ngrid, vb);
+        const long local = vb - start[g];
+        const Shape sh = shape[g];
+        const DerivArgs &a = args[g];
+        const uint3 bid = make_uint3((unsigned)(local % sh.gx), (unsigned)((local / sh.gx) % sh.gy),
+                                     (unsigned)(local / ((long)sh.gx * sh.gy)));
+        const int nx = a.nx;
+        const int nother = a.axis == 1 ? a.nz : a.ny;
+        const long s = a.axis == 1 ? (long)nx : (long)nx * a.ny;
+        const long os = a.axis == 1 ? (long)nx * a.ny : (long)nx;
+        deriv_yz_body<EPI>(a.T, a.F, nx, nother, s, os, bid, threadIdx.x, blockDim.x);
+    }
+}
+
+} // namespace
+
+// Launch configuration shared by all positions of a batch.
+struct BatchTune {
+    int cpb;       // cells per thread in pointwise items (x 256 per item)
+    int yz_bs;     // threads per y/z pencil block
+    int ctas_sm;   // resident CTAs per SM for the persistent grids
+};
+
+struct BatchPos {
+    int kind, cls, epi;
+    void *args;        // device array of ngrid argument structs
+    long *start;       // device prefix sums of virtual blocks, ngrid + 1
+    Shape *shape;      // device per-grid virtual launch shapes
+    long total;
+};
+
+} // namespace emix
+
+using namespace emix;
+
+struct emix_batch {
+    std::vector<emix_ctx *> grids;
+    cudaStream_t stream = nullptr, own = nullptr;
+    std::vector<BatchPos> pos;
+    void *dmem = nullptr;           // one device allocation for all position tables
+    BatchTune tune{4, 64, 4};
+    bool built = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int sms = 152;
+};
+
+namespace {
+
+size_t args_size(int kind) {
+    switch (kind) {
+    case LK_PRIM: return sizeof(PrimArgs);
+    case LK_PAD: return sizeof(PadArgs);
+    case LK_WENO: return sizeof(WenoArgs);
+    case LK_DERIV_X: case LK_DERIV_YZ: return sizeof(DerivArgs);
+    case LK_SMAG: return sizeof(SmagArgs);
+    case LK_SF: return sizeof(SfArgs);
+    case LK_VORT: return sizeof(VortArgs);
+    case LK_SELECT: return sizeof(SelArgs);
+    case LK_FLUX: return sizeof(FluxArgs);
+    case LK_RK: return sizeof(RkArgs);
+    case LK_BC: return sizeof(BcArgs);
+    default: return 0;
+    }
+}
+
+const void *args_ptr(const Launch &L) {
+    switch (L.kind) {
+    case LK_PRIM: return &L.prim;
+    case LK_PAD: return &L.pad;
+    case LK_WENO: return &L.weno;
+    case LK_DERIV_X: case LK_DERIV_YZ: return &L.deriv;
+    case LK_SMAG: return &L.smag;
+    case LK_SF: return &L.sf;
+    case LK_VORT: return &L.vort;
+    case LK_SELECT: return &L.sel;
+    case LK_FLUX: return &L.flux;
+    case LK_RK: return &L.rk;
+    case LK_BC: return &L.bc;
+    default: return nullptr;
+    }
+}
+
+long point_count(const Launch &L) {
+    switch (L.kind) {
+    case LK_PRIM: return L.prim.n;
+    case LK_PAD: return L.pad.ng;
+    case LK_SMAG: return L.smag.n;
+    case LK_SF: return L.sf.n;
+    case LK_VORT: return L.vort.n;
+    case LK_SELECT: return L.sel.n;
+    case LK_FLUX: return L.flux.n;
+    case LK_RK: return L.rk.n;
+    case LK_BC: return bc_count(L.bc);
+    default: return 0;
+    }
+}
+
+// virtual launch shape of one grid's launch under the tuning `t`
+Shape shape_of(const Launch &L, const BatchTune &t) {
+    Shape s{1, 1, 1, 0};
+    if (L.kind == LK_WENO) {
+        s.gx = (L.weno.rn[0] + kWX - 1) / kWX;
+        s.gy = (L.weno.rn[1] + kWY - 1) / kWY;
+        s.gz = (L.weno.rn[2] + kWZ - 1) / kWZ;
+    } else if (L.kind == LK_DERIV_X) {
+        const long np = (long)L.deriv.ny * L.deriv.nz;
+        s.gx = (int)((np + 127) / 128);
+        s.gz = L.deriv.nf;
+    } else if (L.kind == LK_DERIV_YZ) {
+        s.gx = (L.deriv.nx + t.yz_bs - 1) / t.yz_bs;
+        s.gy = L.deriv.axis == 1 ? L.deriv.nz : L.deriv.ny;
+        s.gz = L.deriv.nf;
+    } else {
+        const long per = 256L * t.cpb;
+        s.gx = (int)((point_count(L) + per - 1) / per);
+    }
+    return s;
+}
+
+int build(emix_batch *b) {
+    const int G = (int)b->grids.size();
+    std::vector<const std::vector<Launch> *> plans(G);
+    for (int g = 0; g < G; ++g) {
+        if (!ctx_ready(b->grids[g])) {
+            set_last_message("emix_batch_step: static fields of a grid not set");
+            return EMIX_ERR_ARG;
+        }
+        plans[g] = &ctx_plan(b->grids[g]);
+        if (plans[g]->size() != plans[0]->size()) {
+            set_last_message("emix_batch: grids must share level-set and SGS options");
+            return EMIX_ERR_ARG;
+        }
+    }
+    const size_t np = plans[0]->size();
+    // host image of every position's tables, laid out back to back
+    std::vector<unsigned char> host;
+    std::vector<size_t> off_args(np), off_start(np), off_shape(np);
+    std::vector<long> totals(np);
+    auto align = [&](size_t a) { host.resize((host.size() + a - 1) / a * a); };
+    for (size_t k = 0; k < np; ++k) {
+        const Launch &L0 = (*plans[0])[k];
+        const size_t as = args_size(L0.kind);
+        align(256);
+        off_args[k] = host.size();
+        host.resize(host.size() + as * G);
+        std::vector<long> start(G + 1, 0);
+        std::vector<Shape> sh(G);
+        for (int g = 0; g < G; ++g) {
+            const Launch &L = (*plans[g])[k];
+            if (L.kind != L0.kind || (L.kind == LK_DERIV_X || L.kind == LK_DERIV_YZ ? L.deriv.epi != L0.deriv.epi : false)) {
+                set_last_message("emix_batch: plans of the grids differ");
+                return EMIX_ERR_ARG;
+            }
+            std::memcpy(host.data() + off_args[k] + as * g, args_ptr(L), as);
+            sh[g] = shape_of(L, b->tune);
+            start[g + 1] = start[g] + (long)sh[g].gx * sh[g].gy * sh[g].gz;
+        }
+        totals[k] = start[G];
+        align(256);
+        off_start[k] = host.size();
+        host.resize(host.size() + sizeof(long) * (G + 1));
+        std::memcpy(host.data() + off_start[k], start.data(), sizeof(long) * (G + 1));
+        align(256);
+        off_shape[k] = host.size();
+        host.resize(host.size() + sizeof(Shape) * G);
+        std::memcpy(host.data() + off_shape[k], sh.data(), sizeof(Shape) * G);
+    }
+    if (b->dmem) cudaFree(b->dmem);
+    b->dmem = nullptr;
+    if (cudaMalloc(&b->dmem, host.size()) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_message("cudaMalloc of the batch tables failed");
+        return EMIX_ERR_ALLOC;
+    }
+    EMIX_CUDA_TRY(cudaMemcpy(b->dmem, host.data(), host.size(), cudaMemcpyHostToDevice));
+    b->pos.assign(np, BatchPos{});
+    unsigned char *base = static_cast<unsigned char *>(b->dmem);
+    for (size_t k = 0; k < np; ++k) {
+        const Launch &L0 = (*plans[0])[k];
+        BatchPos &P = b->pos[k];
+        P.kind = L0.kind;
+        P.cls = L0.cls;
+        P.epi = (L0.kind == LK_DERIV_X || L0.kind == LK_DERIV_YZ) ? L0.deriv.epi : 0;
+        P.args = base + off_args[k];
+        P.start = reinterpret_cast<long *>(base + off_start[k]);
+        P.shape = reinterpret_cast<Shape *>(base + off_shape[k]);
+        P.total = totals[k];
+    }
+    b->built = true;
+    return EMIX_OK;
+}
+
+int ctas(const emix_batch *b, long total) {
+    long c = (long)b->sms * b->tune.ctas_sm;
+    if (c > total) c = total;
+    return (int)(c < 1 ? 1 : c);
+}
+
+int issue(emix_batch *b) {
+    const int G = (int)b->grids.size();
+    cudaStream_t st = b->stream;
+    for (const BatchPos &P : b->pos) {
+        const int nb = ctas(b, P.total);
+        switch (P.kind) {
+        case LK_PRIM: k_batch_cells<PrimOp><<<nb, 256, 0, st>>>((const PrimArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_PAD: k_batch_cells<PadOp><<<nb, 256, 0, st>>>((const PadArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_SMAG: k_batch_cells<SmagOp><<<nb, 256, 0, st>>>((const SmagArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_SF: k_batch_cells<SfOp><<<nb, 256, 0, st>>>((const SfArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_VORT: k_batch_cells<VortOp><<<nb, 256, 0, st>>>((const VortArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_SELECT: k_batch_cells<SelOp><<<nb, 256, 0, st>>>((const SelArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_FLUX: k_batch_cells<FluxOp><<<nb, 256, 0, st>>>((const FluxArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_RK: k_batch_cells<RkOp><<<nb, 256, 0, st>>>((const RkArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_BC: k_batch_cells<BcOp><<<nb, 256, 0, st>>>((const BcArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_WENO:
+            k_batch_weno<<<nb, dim3(kWX, kWY, kWZ), 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
+            break;
+        case LK_DERIV_X: {
+            const size_t shm = 4 * kXTile * sizeof(double);
+            if (P.epi == EPI_STORE)
+                k_batch_deriv_x<EPI_STORE><<<nb, 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+            else
+                k_batch_deriv_x<EPI_ACCUM><<<nb, 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+            break;
+        }
+        case LK_DERIV_YZ:
+            if (P.epi == EPI_STORE)
+                k_batch_deriv_yz<EPI_STORE><<<nb, b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+            else
+                k_batch_deriv_yz<EPI_ACCUM><<<nb, b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+            break;
+        default:
+            return EMIX_ERR_ARG;
+        }
+    }
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
+
+void drop_graph(emix_batch *b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->gexec = nullptr;
+    b->graph = nullptr;
+}
+
+int step_impl(emix_batch *b, int nsteps, int use_graph) {
+    if (!b->built) {
+        int rc = build(b);
+        if (rc) return rc;
+    }
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; ++s) {
+            int rc = issue(b);
+            if (rc) return rc;
+        }
+        return EMIX_OK;
+    }
+    if (!b->gexec) {
+        EMIX_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = issue(b);
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &gr);
+        if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+        if (e != cudaSuccess) { set_last_error(e, "cudaStreamEndCapture", __FILE__, __LINE__); return EMIX_ERR_CUDA; }
+        b->graph = gr;
+        e = cudaGraphInstantiate(&b->gexec, gr, 0);
+        if (e != cudaSuccess) {
+            drop_graph(b);
+            set_last_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+            return EMIX_ERR_CUDA;
+        }
+    }
+    for (int s = 0; s < nsteps; ++s) EMIX_CUDA_TRY(cudaGraphLaunch(b->gexec, b->stream));
+    return EMIX_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
+    if (!out || !params || ngrid < 1) return EMIX_ERR_ARG;
+    *out = nullptr;
+    for (int g = 1; g < ngrid; ++g)
+        if (params[g].level_set != params[0].level_set || params[g].sgs_model != params[0].sgs_model ||
+            params[g].bc_walls != params[0].bc_walls ||
+            (params[0].level_set && params[g].ls_ghost != params[0].ls_ghost))
+            return EMIX_ERR_ARG;
+    emix_batch *b = new (std::nothrow) emix_batch();
+    if (!b) return EMIX_ERR_ALLOC;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int g = 0; g < ngrid; ++g) {
+        emix_ctx *c = nullptr;
+        int rc = emix_ctx_create(&params[g], &c);
+        if (rc) {
+            for (emix_ctx *x : b->grids) emix_ctx_destroy(x);
+            delete b;
+            return rc;
+        }
+        b->grids.push_back(c);
+    }
+    if (cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        for (emix_ctx *x : b->grids) emix_ctx_destroy(x);
+        delete b;
+        return EMIX_ERR_CUDA;
+    }
+    b->stream = b->own;
+    for (emix_ctx *c : b->grids) emix_ctx_set_stream(c, b->stream);
+    *out = b;
+    return EMIX_OK;
+}
+
+int emix_batch_destroy(emix_batch *b) {
+    if (!b) return EMIX_ERR_ARG;
+    cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    for (emix_ctx *c : b->grids) emix_ctx_destroy(c);
+    if (b->dmem) cudaFree(b->dmem);
+    if (b->own) cudaStreamDestroy(b->own);
+    delete b;
+    return EMIX_OK;
+}
+
+int emix_batch_grid(emix_batch *b, int g, emix_ctx **ctx) {
+    if (!b || !ctx || g < 0 || g >= (int)b->grids.size()) return EMIX_ERR_ARG;
+    *ctx = b->grids[g];
+    return EMIX_OK;
+}
+
+int emix_batch_set_stream(emix_batch *b, void *stream) {
+    if (!b) return EMIX_ERR_ARG;
+    b->stream = stream ? (cudaStream_t)stream : b->own;
+    for (emix_ctx *c : b->grids) emix_ctx_set_stream(c, b->stream);
+    drop_graph(b);
+    return EMIX_OK;
+}
+
+int emix_batch_step(emix_batch *b, int nsteps, int use_graph) {
+    if (!b || nsteps < 0) return EMIX_ERR_ARG;
+    return step_impl(b, nsteps, use_graph);
+}
+
+int emix_batch_step_per_grid(emix_batch *b, int nsteps, int use_graph) {
+    if (!b || nsteps < 0) return EMIX_ERR_ARG;
+    for (int s = 0; s < nsteps; ++s)
+        for (emix_ctx *c : b->grids) {
+            int rc = emix_step(c, 1, use_graph);
+            if (rc) return rc;
+        }
+    return EMIX_OK;
+}
+
+int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int ctas_per_sm) {
+    if (!b || cells_per_thread < 1 || cells_per_thread > 64 || ctas_per_sm < 1 || ctas_per_sm > 64 ||
+        (yz_block != 32 && yz_block != 64 && yz_block != 128))
+        return EMIX_ERR_ARG;
+    b->tune = BatchTune{cells_per_thread, yz_block, ctas_per_sm};
+    b->built = false;
+    drop_graph(b);
+    return EMIX_OK;
+}
+
+int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, int *ctas_per_sm) {
+    if (!b) return EMIX_ERR_ARG;
+    if (cells_per_thread) *cells_per_thread = b->tune.cpb;
+    if (yz_block) *yz_block = b->tune.yz_bs;
+    if (ctas_per_sm) *ctas_per_sm = b->tune.ctas_sm;
+    return EMIX_OK;
+}
+
+int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms) {
+    // Times every candidate launch configuration on the real batch (the state
+    // advances; callers re-upload their initial state afterwards) and keeps
+    // the fastest.
+    if (!b || nsteps < 1) return EMIX_ERR_ARG;
+    const int cpbs[] = {1, 4};
+    const int bss[] = {32, 64, 128};
+    const int ctass[] = {2, 4, 8};
+    BatchTune best = b->tune;
+    float best_t = 1e30f;
+    cudaEvent_t e0, e1;
+    EMIX_CUDA_TRY(cudaEventCreate(&e0));
+    EMIX_CUDA_TRY(cudaEventCreate(&e1));
+    int rc = EMIX_OK;
+    for (int cpb : cpbs)
+        for (int bs : bss)
+            for (int cs : ctass) {
+                if ((rc = emix_batch_set_tuning(b, cpb, bs, cs))) goto done;
+                if ((rc = step_impl(b, 1, 0))) goto done;   // build + warm
+                cudaEventRecord(e0, b->stream);
+                if ((rc = step_impl(b, nsteps, 0))) goto done;
+                cudaEventRecord(e1, b->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) { rc = EMIX_ERR_CUDA; goto done; }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best_t) { best_t = ms; best = b->tune; }
+            }
+done:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    rc = emix_batch_set_tuning(b, best.cpb, best.yz_bs, best.ctas_sm);
+    if (best_ms) *best_ms = best_t / nsteps;
+    return rc;
+}
+
+} // extern "C"

@@ -76,15 +76,15 @@ EMIX_DEV double rhs_row(const DerivTable &T, const double *__restrict__ fp, long
 //   axis 2 (z): pencils (x, y), element stride nx*ny, other stride nx
 // grid: (ceil(nx/blockDim.x), nother, nf)
 // ---------------------------------------------------------------------------
-// grid: (ceil(nx/blockDim.x), nother, nf); blockIdx.z = field
+// Body for one (virtual) block: bid = (x block, pencil row, field).
 template <int EPI>
-__global__ void __launch_bounds__(128)
-k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int o = blockIdx.y;
+EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, int nother, long s,
+                            long os, uint3 bid, int tid, int bdim) {
+    const int x = bid.x * bdim + tid;
+    const int o = bid.y;
     if (x >= nx || o >= nother) return;
     const long base = x + (long)o * os;
-    const int f = blockIdx.z;
+    const int f = bid.z;
     const double *__restrict__ in = pick(F.in, f) + base;
     double *w = pick(F.w, f) + base;
     double *out = pick(F.out, f) + base;
@@ -153,6 +153,13 @@ k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
     }
 }
 
+// grid: (ceil(nx/blockDim.x), nother, nf); blockIdx.z = field
+template <int EPI>
+__global__ void __launch_bounds__(128)
+k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
+    deriv_yz_body<EPI>(T, F, nx, nother, s, os, blockIdx, threadIdx.x, blockDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // x pencils: a warp owns 32 consecutive pencils (flattened (j,k)).  Rows are
 // staged 32 at a time (plus a 2-row look-ahead) through a per-warp shared tile
@@ -166,16 +173,16 @@ constexpr int kXRows = 34;          // 32 rows + 2 look-ahead
 constexpr int kXLd = kXRows + 1;    // padded leading dimension (odd: no bank conflicts)
 constexpr int kXTile = 32 * kXLd;
 
+// Body for one (virtual) block of `nwarps` warps: bid = (pencil group, -, field).
 template <int EPI>
-__global__ void __launch_bounds__(128)
-k_deriv_x(DerivTable T, PencilFields F, long npencil) {
-    extern __shared__ double smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npencil, uint3 bid,
+                           int tid, int nwarps, double *smem) {
+    const int warp = tid >> 5, lane = tid & 31;
     double *tile = smem + warp * kXTile;
-    const long p0 = ((long)blockIdx.x * (blockDim.x >> 5) + warp) * 32;
+    const long p0 = ((long)bid.x * nwarps + warp) * 32;
     if (p0 >= npencil) return;  // whole warp
     const int npw = (int)min((long)32, npencil - p0);
-    const int f = blockIdx.z;
+    const int f = bid.z;
     const int n = T.n;
     const double *__restrict__ in = pick(F.in, f) + p0 * n;
     double *w = pick(F.w, f) + p0 * n;
@@ -279,6 +286,13 @@ k_deriv_x(DerivTable T, PencilFields F, long npencil) {
         }
         __syncwarp();
     }
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128)
+k_deriv_x(DerivTable T, PencilFields F, long npencil) {
+    extern __shared__ double smem[];
+    deriv_x_body<EPI>(T, F, npencil, blockIdx, threadIdx.x, blockDim.x >> 5, smem);
 }
 
 // Launch helper: derivative of nf fields along axis; w may equal out when

@@ -1,0 +1,55 @@
+// plan.cuh -- a step as a list of kernel-argument records.
+//
+// A context builds its RK3 step once as a plan: one record per launch, with
+// every pointer and constant the kernel needs.  A single grid executes the
+// plan with ordinary launches (launch_single).  A batch of grids executes
+// position k of all plans as one persistent launch over every grid's work
+// (batch.cu), which is possible because the kernel bodies take explicit block
+// indices.
+#pragma once
+
+#include "boundary.cuh"
+#include "deriv.cuh"
+#include "pointwise.cuh"
+#include "weno.cuh"
+
+namespace emix {
+
+enum LaunchKind {
+    LK_PRIM, LK_PAD, LK_WENO, LK_DERIV_X, LK_DERIV_YZ, LK_SMAG, LK_SF, LK_VORT, LK_SELECT,
+    LK_FLUX, LK_RK, LK_BC, LK_COUNT
+};
+
+// profile classes (emix_ctx_profile)
+enum {
+    CLS_PRIM, CLS_PAD, CLS_WENO, CLS_GRADX, CLS_GRADY, CLS_GRADZ, CLS_SGS, CLS_FLUX,
+    CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_COUNT
+};
+
+struct DerivArgs {
+    DerivTable T;
+    PencilFields F;
+    int axis, epi, nf, nx, ny, nz;
+};
+
+struct Launch {
+    int kind;
+    int cls;
+    union {
+        PrimArgs prim;
+        PadArgs pad;
+        WenoArgs weno;
+        DerivArgs deriv;
+        SmagArgs smag;
+        SfArgs sf;
+        VortArgs vort;
+        SelArgs sel;
+        FluxArgs flux;
+        RkArgs rk;
+        BcArgs bc;
+    };
+};
+
+int launch_single(const Launch &L, cudaStream_t st);
+
+} // namespace emix

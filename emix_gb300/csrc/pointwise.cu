@@ -64,47 +64,6 @@ __global__ void k_flux_one(int neq, double *__restrict__ e, double *__restrict__
     }
 }
 
-__global__ void __launch_bounds__(256, 2) k_flux_all(FluxArgs a) {
-    const long n = a.n;
-    EMIX_FOR_CELLS(q, n) {
-        const double r = a.um[q];
-        (void)r;
-        const double um2 = a.um[n + q], um3 = a.um[2 * n + q], um4 = a.um[3 * n + q],
-                     um5 = a.um[4 * n + q];
-        const double u1 = a.u[q], u2 = a.u[n + q], u3 = a.u[2 * n + q];
-        const double p = a.pres[q], vs = a.vis[q];
-        const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
-        const double *dv = a.dvel + q;
-        const double JX = a.jx[q], JY = a.jy[q], JZ = a.jz[q];
-        // strain pieces shared by the viscous fluxes of equations 2..4
-        const double sxx = j1 * dv[0], syy = j5 * dv[4 * n], szz = j9 * dv[8 * n];
-        const double sxy = j1 * dv[n] + j5 * dv[3 * n];        // p1+p2 of :68-70 and :102-104
-        const double sxz = j1 * dv[2 * n] + j9 * dv[6 * n];    // :79-81 and :147-149
-        const double syz = j9 * dv[7 * n] + j5 * dv[5 * n];    // :123-125 and :157-159
-        const double vxy = vs * sxy, vxz = vs * sxz, vyz = vs * syz;
-        // equation 1
-        a.F[0][q] = JX * (-um2);
-        a.F[1][q] = JY * (-um3);
-        a.F[2][q] = JZ * (-um4);
-        // equation 2
-        a.F[3][q] = JX * ((-um2 * u1 - p) + vs * (2.0 * sxx));
-        a.F[4][q] = JY * (-um3 * u1 + vxy);
-        a.F[5][q] = JZ * (-um4 * u1 + vxz);
-        // equation 3
-        a.F[6][q] = JX * (-um2 * u2 + vxy);
-        a.F[7][q] = JY * ((-um3 * u2 - p) + vs * (2.0 * syy));
-        a.F[8][q] = JZ * (-um4 * u2 + vyz);
-        // equation 4
-        a.F[9][q] = JX * (-um2 * u3 + vxz);
-        a.F[10][q] = JY * (-um3 * u3 + vyz);
-        a.F[11][q] = JZ * ((-um4 * u3 - p) + vs * (2.0 * szz));
-        // equation 5
-        a.F[12][q] = JX * (-u1 * um5);
-        a.F[13][q] = JY * (-u2 * um5);
-        a.F[14][q] = JZ * (-u3 * um5);
-    }
-}
-
 __global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__ dxyz,
                             double *__restrict__ ratios, int nx, int ny, int nz) {
     const long n = (long)nx * ny * nz;
@@ -135,160 +94,13 @@ __global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__
     }
 }
 
-__global__ void k_sgs_smag(const double *__restrict__ dvel, const double *__restrict__ jbn,
-                           const double *__restrict__ dxyz, double cs, double c4,
-                           double *__restrict__ amut, double *__restrict__ vis, long n) {
-    EMIX_FOR_CELLS(q, n) {
-        const double j1 = jbn[q], j5 = jbn[4 * n + q], j9 = jbn[8 * n + q];
-        const double *dv = dvel + q;
-        const double ux = j1 * dv[0], vx = j1 * dv[n], wx = j1 * dv[2 * n];
-        const double uy = j5 * dv[3 * n], vy = j5 * dv[4 * n], wy = j5 * dv[5 * n];
-        const double uz = j9 * dv[6 * n], vz = j9 * dv[7 * n], wz = j9 * dv[8 * n];
-        const double s12 = 0.5 * (uy + vx), s13 = 0.5 * (uz + wx), s23 = 0.5 * (vz + wy);
-        const double ss = ux * ux + vy * vy + wz * wz + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23);
-        const double cd = cs * dxyz[q];
-        const double a = cd * cd * sqrt(2.0 * ss);
-        if (amut) amut[q] = a;
-        vis[q] = c4 * 1.0 + a;
-    }
-}
-
-__global__ void k_sgs_sf(const double *__restrict__ u, const double *__restrict__ ratios,
-                         const double *__restrict__ dxyz, double amu0,
-                         double *__restrict__ amut, int nx, int ny, int nz) {
-    const long n = (long)nx * ny * nz;
-    const double *U = u, *V = u + n, *W = u + 2 * n;
-    const long sy = nx, sz = (long)nx * ny;
-    EMIX_FOR_CELLS(q, n) {
-        const int i = (int)(q % nx);
-        const int j = (int)((q / nx) % ny);
-        const int k = (int)(q / sz);
-        double a, b, c, s;
-        long p, m;
-        // the six one-sided increments in the order of f_structura
-        p = i < nx - 1 ? q + 1 : q; m = i < nx - 1 ? q : q - 1;
-        double r = ratios[q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = a * a + b * b + c * c;
-        if (i > 0) { p = q - 1; m = q; } else { p = q + 1; m = q; }
-        r = ratios[n + q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = s + a * a + b * b + c * c;
-        if (j < ny - 1) { p = q + sy; m = q; } else { p = q; m = q - sy; }
-        r = ratios[2 * n + q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = s + a * a + b * b + c * c;
-        if (j > 0) { p = q - sy; m = q; } else { p = q; m = q + sy; }
-        r = ratios[3 * n + q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = s + a * a + b * b + c * c;
-        if (k < nz - 1) { p = q + sz; m = q; } else { p = q; m = q - sz; }
-        r = ratios[4 * n + q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = s + a * a + b * b + c * c;
-        if (k > 0) { p = q - sz; m = q; } else { p = q; m = q + sz; }
-        r = ratios[5 * n + q];
-        a = (U[p] - U[m]) * r; b = (V[p] - V[m]) * r; c = (W[p] - W[m]) * r;
-        s = s + a * a + b * b + c * c;
-        s = s * (1.0 / 6.0);
-        amut[q] = amu0 * sqrt(s) * dxyz[q];
-    }
-}
-
-__global__ void k_vort(const double *__restrict__ dvel, const double *__restrict__ jbn,
-                       double *__restrict__ w, long n) {
-    EMIX_FOR_CELLS(q, n) {
-        const double j1 = jbn[q], j5 = jbn[4 * n + q], j9 = jbn[8 * n + q];
-        const double *dv = dvel + q;
-        w[q] = j5 * dv[7 * n] - j9 * dv[5 * n];
-        w[n + q] = j9 * dv[2 * n] - j1 * dv[6 * n];
-        w[2 * n + q] = j1 * dv[3 * n] - j5 * dv[n];
-    }
-}
-
-__global__ void k_selective(const double *__restrict__ w, double *__restrict__ amut,
-                            double *__restrict__ vis, double cutoff, double c4,
-                            int nx, int ny, int nz) {
-    const long n = (long)nx * ny * nz;
-    const double *wx = w, *wy = w + n, *wz = w + 2 * n;
-    const long sy = nx, sz = (long)nx * ny;
-    EMIX_FOR_CELLS(q, n) {
-        const int i = (int)(q % nx);
-        const int j = (int)((q / nx) % ny);
-        const int k = (int)(q / sz);
-        const long a1 = i < nx - 1 ? q + 1 : q, a2 = i > 0 ? q - 1 : q;
-        const long a3 = k < nz - 1 ? q + sz : q, a4 = k > 0 ? q - sz : q;
-        const long a5 = j < ny - 1 ? q + sy : q, a6 = j > 0 ? q - sy : q;
-        const double wxn = wx[a1] + wx[a2] + wx[a3] + wx[a4] + wx[a5] + wx[a6];
-        const double wyn = wy[a1] + wy[a2] + wy[a3] + wy[a4] + wy[a5] + wy[a6];
-        const double wzn = wz[a1] + wz[a2] + wz[a3] + wz[a4] + wz[a5] + wz[a6];
-        const double x = wx[q], y = wy[q], z = wz[q];
-        double wn = x * x + y * y + z * z;
-        wn = sqrt(wn * (wxn * wxn + wyn * wyn + wzn * wzn));
-        const double s1 = (x * wxn + y * wyn + z * wzn) / wn;
-        double a = amut[q];
-        if (s1 > cutoff) a = 0.0;
-        amut[q] = a;
-        vis[q] = c4 * 1.0 + a;
-    }
-}
-
-__global__ void k_prim(const double *__restrict__ um, double *__restrict__ u,
-                       double *__restrict__ pres, double inv_m2, long n) {
-    EMIX_FOR_CELLS(q, n) {
-        const double r = um[q];
-        const double rr = 1.0 / r;
-        pres[q] = r * inv_m2;
-        u[q] = um[n + q] * rr;
-        u[n + q] = um[2 * n + q] * rr;
-        u[2 * n + q] = um[3 * n + q] * rr;
-    }
-}
-
-__global__ void k_rk_post(RkArgs a) {
-    const long n = a.n;
-    const double dt = a.dt;
-    EMIX_FOR_CELLS(q, n) {
-        const double j11 = a.jbn[10 * n + q];
-        double v[5];
-#pragma unroll
-        for (int m = 0; m < 5; ++m) {
-            const double rs = j11 * a.R[m * n + q];
-            const double u0 = a.um0[m * n + q];
-            if (a.stage == 1) {          // rungek_ico.f90:89-90
-                v[m] = u0 + dt * rs;
-            } else if (a.stage == 2) {   // :153-154
-                v[m] = 0.75 * u0 + 0.25 * a.um[m * n + q] + (0.25 * dt) * rs;
-            } else {                     // :217-220
-                v[m] = (1.0 / 3.0) * u0 + (2.0 / 3.0) * a.um[m * n + q] + ((2.0 / 3.0) * dt) * rs;
-            }
-        }
-        // varc_to_varnc + clip + mask + varc_to_varnc (:104-124)
-        const double r = v[0];
-        const double rr = 1.0 / r;
-        const double mk = a.mask[q];
-        double uu[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            double x = v[d + 1] * rr;
-            x = fmin(6.0, x);
-            x = fmax(-6.0, x);
-            const double mom = x * r * mk;
-            uu[d] = mom * rr;
-        }
-        const double p = r * a.inv_m2;
-        // rebuild after the level-set call site (:127-138)
-        const double r1 = p * a.mach * a.mach;
-        a.out[q] = r1;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            a.out[(d + 1) * n + q] = uu[d] * r1;
-            a.u[d * n + q] = uu[d];
-        }
-        a.out[4 * n + q] = v[4];
-        a.pres[q] = p;
-    }
-}
+__global__ void k_prim(PrimArgs a) { EMIX_FOR_CELLS(q, a.n) prim_cell(a, q); }
+__global__ void __launch_bounds__(256, 2) k_flux_all(FluxArgs a) { EMIX_FOR_CELLS(q, a.n) flux_cell(a, q); }
+__global__ void k_sgs_smag(SmagArgs a) { EMIX_FOR_CELLS(q, a.n) smag_cell(a, q); }
+__global__ void k_sgs_sf(SfArgs a) { EMIX_FOR_CELLS(q, a.n) sf_cell(a, q); }
+__global__ void k_vort(VortArgs a) { EMIX_FOR_CELLS(q, a.n) vort_cell(a, q); }
+__global__ void k_selective(SelArgs a) { EMIX_FOR_CELLS(q, a.n) select_cell(a, q); }
+__global__ void k_rk_post(RkArgs a) { EMIX_FOR_CELLS(q, a.n) rk_cell(a, q); }
 
 } // namespace emix
 
@@ -325,8 +137,8 @@ int emix_sgs_viscosity_dev(int model, double coef, double c4, const double *u, c
     const long n = (long)ncell(nx, ny, nz);
     cudaStream_t st = (cudaStream_t)stream;
     if (model == EMIX_SGS_NONE || model == EMIX_SGS_SMAGORINSKY) {
-        k_sgs_smag<<<cells_grid(n), 256, 0, st>>>(dvel, jbn, dxyzsgd,
-                                                  model == EMIX_SGS_NONE ? 0.0 : coef, c4, amut, vis, n);
+        SmagArgs sa{dvel, jbn, dxyzsgd, model == EMIX_SGS_NONE ? 0.0 : coef, c4, amut, vis, n};
+        k_sgs_smag<<<cells_grid(n), 256, 0, st>>>(sa);
         EMIX_CUDA_TRY(cudaGetLastError());
         return EMIX_OK;
     }
@@ -337,10 +149,13 @@ int emix_sgs_viscosity_dev(int model, double coef, double c4, const double *u, c
     if (rc) return rc;
     double *w = scr;
     double *am = amut ? amut : scr + 3 * n;
-    k_sgs_sf<<<cells_grid(n), 256, 0, st>>>(u, ratios, dxyzsgd, coef, am, nx, ny, nz);
-    k_vort<<<cells_grid(n), 256, 0, st>>>(dvel, jbn, w, n);
+    SfArgs fa{u, ratios, dxyzsgd, coef, am, nx, ny, nz, n};
+    VortArgs va{dvel, jbn, w, n};
     const double cutoff = cos(20.0 * atan(1.0) / 45.0);   // sgdm_incomp.f90:18
-    k_selective<<<cells_grid(n), 256, 0, st>>>(w, am, vis, cutoff, c4, nx, ny, nz);
+    SelArgs la{w, am, vis, cutoff, c4, nx, ny, nz, n};
+    k_sgs_sf<<<cells_grid(n), 256, 0, st>>>(fa);
+    k_vort<<<cells_grid(n), 256, 0, st>>>(va);
+    k_selective<<<cells_grid(n), 256, 0, st>>>(la);
     EMIX_CUDA_TRY(cudaGetLastError());
     return EMIX_OK;
 }

@@ -1,5 +1,8 @@
-// pointwise.cuh -- cell-local kernels of the RK3 substep: fluxes, SGS
-// viscosity, RK update and the variable conversions.
+// pointwise.cuh -- cell-local pieces of the RK3 substep: fluxes, SGS
+// viscosity, RK update and the variable conversions.  Each piece is an
+// argument struct plus a per-cell device function, so that the same body runs
+// from a single-grid kernel (grid-stride loop) and from the batched
+// persistent kernels that cover many grids in one launch.
 #pragma once
 
 #include "common.cuh"
@@ -17,16 +20,27 @@ inline int cells_grid(long n, int bs = 256) {
     return (int)(b < 1 ? 1 : b);
 }
 
-// ---- flujos(neq), solver/flujos_compact.f90:21-217 -------------------------
-__global__ void k_flux_one(int neq, double *__restrict__ e, double *__restrict__ f,
-                           double *__restrict__ g, double *__restrict__ ev,
-                           double *__restrict__ fv, double *__restrict__ gv,
-                           const double *__restrict__ um, const double *__restrict__ u,
-                           const double *__restrict__ pres, const double *__restrict__ dvel,
-                           const double *__restrict__ jbn, const double *__restrict__ vis, long n);
+// ---- primitive variables: u = um(2..4)/um(1), pres = um(1)/Mach^2 ------------
+// (varc_to_varnc, src/MSVSingle/herramientas_incomp2.f90:16-27)
+struct PrimArgs {
+    const double *um;
+    double *u, *pres;
+    double inv_m2;
+    long n;
+};
 
-// Fused flux of all five equations for the RK3 step, inviscid plus viscous,
-// already projected by J*dxi/dx (x), J*deta/dy (y), J*dzeta/dz (z):
+EMIX_DEV void prim_cell(const PrimArgs &a, long q) {
+    const long n = a.n;
+    const double r = a.um[q];
+    const double rr = 1.0 / r;
+    a.pres[q] = r * a.inv_m2;
+    a.u[q] = a.um[n + q] * rr;
+    a.u[n + q] = a.um[2 * n + q] * rr;
+    a.u[2 * n + q] = a.um[3 * n + q] * rr;
+}
+
+// ---- fluxes of all five equations (flujos, solver/flujos_compact.f90:21-217) --
+// Inviscid plus viscous, projected by J*dxi/dx (x), J*deta/dy (y), J*dzeta/dz (z):
 //   F[3*m + d] = Jd * (inviscid_{m,d} + viscous_{m,d}),  m = 0..4, d = 0..2.
 // jx/jy/jz are the static products jbn10*jbn1, jbn10*jbn5, jbn10*jbn9.
 struct FluxArgs {
@@ -40,35 +54,167 @@ struct FluxArgs {
     const double *jx, *jy, *jz;
     long n;
 };
-__global__ void k_flux_all(FluxArgs a);
 
-// ---- SGS ---------------------------------------------------------------------
-// INISGDM (solver/sgdm_incomp.f90:20-108)
-__global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__ dxyz,
-                            double *__restrict__ ratios, int nx, int ny, int nz);
+EMIX_DEV void flux_cell(const FluxArgs &a, long q) {
+    const long n = a.n;
+    const double um2 = a.um[n + q], um3 = a.um[2 * n + q], um4 = a.um[3 * n + q],
+                 um5 = a.um[4 * n + q];
+    const double u1 = a.u[q], u2 = a.u[n + q], u3 = a.u[2 * n + q];
+    const double p = a.pres[q], vs = a.vis[q];
+    const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
+    const double *dv = a.dvel + q;
+    const double JX = a.jx[q], JY = a.jy[q], JZ = a.jz[q];
+    // strain pieces shared by the viscous fluxes of equations 2..4
+    const double sxx = j1 * dv[0], syy = j5 * dv[4 * n], szz = j9 * dv[8 * n];
+    const double sxy = j1 * dv[n] + j5 * dv[3 * n];        // p1+p2 of :68-70 and :102-104
+    const double sxz = j1 * dv[2 * n] + j9 * dv[6 * n];    // :79-81 and :147-149
+    const double syz = j9 * dv[7 * n] + j5 * dv[5 * n];    // :123-125 and :157-159
+    const double vxy = vs * sxy, vxz = vs * sxz, vyz = vs * syz;
+    // equation 1
+    a.F[0][q] = JX * (-um2);
+    a.F[1][q] = JY * (-um3);
+    a.F[2][q] = JZ * (-um4);
+    // equation 2
+    a.F[3][q] = JX * ((-um2 * u1 - p) + vs * (2.0 * sxx));
+    a.F[4][q] = JY * (-um3 * u1 + vxy);
+    a.F[5][q] = JZ * (-um4 * u1 + vxz);
+    // equation 3
+    a.F[6][q] = JX * (-um2 * u2 + vxy);
+    a.F[7][q] = JY * ((-um3 * u2 - p) + vs * (2.0 * syy));
+    a.F[8][q] = JZ * (-um4 * u2 + vyz);
+    // equation 4
+    a.F[9][q] = JX * (-um2 * u3 + vxz);
+    a.F[10][q] = JY * (-um3 * u3 + vyz);
+    a.F[11][q] = JZ * ((-um4 * u3 - p) + vs * (2.0 * szz));
+    // equation 5
+    a.F[12][q] = JX * (-u1 * um5);
+    a.F[13][q] = JY * (-u2 * um5);
+    a.F[14][q] = JZ * (-u3 * um5);
+}
 
-// Smagorinsky: amut = (Cs*Delta)^2 sqrt(2 S_ij S_ij), vis = c4 + amut
-__global__ void k_sgs_smag(const double *__restrict__ dvel, const double *__restrict__ jbn,
-                           const double *__restrict__ dxyz, double cs, double c4,
-                           double *__restrict__ amut, double *__restrict__ vis, long n);
+// ---- Smagorinsky: amut = (Cs*Delta)^2 sqrt(2 S_ij S_ij), vis = c4 + amut ------
+struct SmagArgs {
+    const double *dvel, *jbn, *dxyz;
+    double cs, c4;
+    double *amut, *vis;
+    long n;
+};
 
-// structure function (f_structura + amu0*sqrt*Delta), solver/sgdm_incomp.f90:131-137,166-298
-__global__ void k_sgs_sf(const double *__restrict__ u, const double *__restrict__ ratios,
-                         const double *__restrict__ dxyz, double amu0,
-                         double *__restrict__ amut, int nx, int ny, int nz);
-// VORT, :330-341
-__global__ void k_vort(const double *__restrict__ dvel, const double *__restrict__ jbn,
-                       double *__restrict__ w, long n);
+EMIX_DEV void smag_cell(const SmagArgs &a, long q) {
+    const long n = a.n;
+    const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
+    const double *dv = a.dvel + q;
+    const double ux = j1 * dv[0], vx = j1 * dv[n], wx = j1 * dv[2 * n];
+    const double uy = j5 * dv[3 * n], vy = j5 * dv[4 * n], wy = j5 * dv[5 * n];
+    const double uz = j9 * dv[6 * n], vz = j9 * dv[7 * n], wz = j9 * dv[8 * n];
+    const double s12 = 0.5 * (uy + vx), s13 = 0.5 * (uz + wx), s23 = 0.5 * (vz + wy);
+    const double ss = ux * ux + vy * vy + wz * wz + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23);
+    const double cd = a.cs * a.dxyz[q];
+    const double am = cd * cd * sqrt(2.0 * ss);
+    if (a.amut) a.amut[q] = am;
+    a.vis[q] = a.c4 * 1.0 + am;
+}
+
+// ---- selective structure-function model (solver/sgdm_incomp.f90) ------------
+// f_structura + amu0*sqrt*Delta (:131-137, :166-298)
+struct SfArgs {
+    const double *u, *ratios, *dxyz;
+    double amu0;
+    double *amut;
+    int nx, ny, nz;
+    long n;
+};
+
+EMIX_DEV void sf_cell(const SfArgs &a, long q) {
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const long n = a.n;
+    const double *U = a.u, *V = a.u + n, *W = a.u + 2 * n;
+    const double *ratios = a.ratios;
+    const long sy = nx, sz = (long)nx * ny;
+    const int i = (int)(q % nx);
+    const int j = (int)((q / nx) % ny);
+    const int k = (int)(q / sz);
+    double x, y, z, s;
+    long p, m;
+    // the six one-sided increments in the order of f_structura
+    p = i < nx - 1 ? q + 1 : q; m = i < nx - 1 ? q : q - 1;
+    double r = ratios[q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = x * x + y * y + z * z;
+    if (i > 0) { p = q - 1; m = q; } else { p = q + 1; m = q; }
+    r = ratios[n + q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = s + x * x + y * y + z * z;
+    if (j < ny - 1) { p = q + sy; m = q; } else { p = q; m = q - sy; }
+    r = ratios[2 * n + q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = s + x * x + y * y + z * z;
+    if (j > 0) { p = q - sy; m = q; } else { p = q; m = q + sy; }
+    r = ratios[3 * n + q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = s + x * x + y * y + z * z;
+    if (k < nz - 1) { p = q + sz; m = q; } else { p = q; m = q - sz; }
+    r = ratios[4 * n + q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = s + x * x + y * y + z * z;
+    if (k > 0) { p = q - sz; m = q; } else { p = q; m = q + sz; }
+    r = ratios[5 * n + q];
+    x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
+    s = s + x * x + y * y + z * z;
+    s = s * (1.0 / 6.0);
+    a.amut[q] = a.amu0 * sqrt(s) * a.dxyz[q];
+}
+
+// VORT (:330-341)
+struct VortArgs {
+    const double *dvel, *jbn;
+    double *w;
+    long n;
+};
+
+EMIX_DEV void vort_cell(const VortArgs &a, long q) {
+    const long n = a.n;
+    const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
+    const double *dv = a.dvel + q;
+    a.w[q] = j5 * dv[7 * n] - j9 * dv[5 * n];
+    a.w[n + q] = j9 * dv[2 * n] - j1 * dv[6 * n];
+    a.w[2 * n + q] = j1 * dv[3 * n] - j5 * dv[n];
+}
+
 // SELECTIVO (:346-395) and viscosidad (vis = c4 + amut)
-__global__ void k_selective(const double *__restrict__ w, double *__restrict__ amut,
-                            double *__restrict__ vis, double cutoff, double c4,
-                            int nx, int ny, int nz);
+struct SelArgs {
+    const double *w;
+    double *amut, *vis;
+    double cutoff, c4;
+    int nx, ny, nz;
+    long n;
+};
 
-// ---- RK3 step pieces -----------------------------------------------------------
-// primitive variables from um: u = um(2..4)/um(1), pres = um(1)/Mach^2
-__global__ void k_prim(const double *__restrict__ um, double *__restrict__ u,
-                       double *__restrict__ pres, double inv_m2, long n);
+EMIX_DEV void select_cell(const SelArgs &a, long q) {
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const long n = a.n;
+    const double *wx = a.w, *wy = a.w + n, *wz = a.w + 2 * n;
+    const long sy = nx, sz = (long)nx * ny;
+    const int i = (int)(q % nx);
+    const int j = (int)((q / nx) % ny);
+    const int k = (int)(q / sz);
+    const long a1 = i < nx - 1 ? q + 1 : q, a2 = i > 0 ? q - 1 : q;
+    const long a3 = k < nz - 1 ? q + sz : q, a4 = k > 0 ? q - sz : q;
+    const long a5 = j < ny - 1 ? q + sy : q, a6 = j > 0 ? q - sy : q;
+    const double wxn = wx[a1] + wx[a2] + wx[a3] + wx[a4] + wx[a5] + wx[a6];
+    const double wyn = wy[a1] + wy[a2] + wy[a3] + wy[a4] + wy[a5] + wy[a6];
+    const double wzn = wz[a1] + wz[a2] + wz[a3] + wz[a4] + wz[a5] + wz[a6];
+    const double x = wx[q], y = wy[q], z = wz[q];
+    double wn = x * x + y * y + z * z;
+    wn = sqrt(wn * (wxn * wxn + wyn * wyn + wzn * wzn));
+    const double s1 = (x * wxn + y * wyn + z * wzn) / wn;
+    double am = a.amut[q];
+    if (s1 > a.cutoff) am = 0.0;
+    a.amut[q] = am;
+    a.vis[q] = a.c4 * 1.0 + am;
+}
 
+// ---- RK stage + conversions ------------------------------------------------------
 // rs = jbn11*R; RK stage s; varc_to_varnc, clip to [-6,6], mask, varc_to_varnc;
 // rebuild um1(1) = pres*Mach*Mach, um1(2..4) = u*um1(1)
 // (solver/rungek_ico.f90:83-138,150-198,210-267)
@@ -83,8 +229,82 @@ struct RkArgs {
     const double *mask;
     double dt, mach, inv_m2;
     int stage;
+    int mode;             // 0: RK + conversions; 1: RK only (um1 -> out); 2: conversions of out
     long n;
 };
+
+EMIX_DEV void rk_cell(const RkArgs &a, long q) {
+    const long n = a.n;
+    const double dt = a.dt;
+    double v[5];
+    if (a.mode == 2) {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) v[m] = a.out[m * n + q];
+    } else {
+    const double j11 = a.jbn[10 * n + q];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        const double rs = j11 * a.R[m * n + q];
+        const double u0 = a.um0[m * n + q];
+        if (a.stage == 1) {          // rungek_ico.f90:89-90
+            v[m] = u0 + dt * rs;
+        } else if (a.stage == 2) {   // :153-154
+            v[m] = 0.75 * u0 + 0.25 * a.um[m * n + q] + (0.25 * dt) * rs;
+        } else {                     // :217-220
+            v[m] = (1.0 / 3.0) * u0 + (2.0 / 3.0) * a.um[m * n + q] + ((2.0 / 3.0) * dt) * rs;
+        }
+    }
+    if (a.mode == 1) {
+#pragma unroll
+        for (int m = 0; m < 5; ++m) a.out[m * n + q] = v[m];
+        return;
+    }
+    }
+    // varc_to_varnc + clip + mask + varc_to_varnc (:104-124)
+    const double r = v[0];
+    const double rr = 1.0 / r;
+    const double mk = a.mask[q];
+    double uu[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double x = v[d + 1] * rr;
+        x = fmin(6.0, x);
+        x = fmax(-6.0, x);
+        const double mom = x * r * mk;
+        uu[d] = mom * rr;
+    }
+    const double p = r * a.inv_m2;
+    // rebuild after the level-set call site (:127-138)
+    const double r1 = p * a.mach * a.mach;
+    a.out[q] = r1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        a.out[(d + 1) * n + q] = uu[d] * r1;
+        a.u[d * n + q] = uu[d];
+    }
+    a.out[4 * n + q] = v[4];
+    a.pres[q] = p;
+}
+
+// ---- kernels ------------------------------------------------------------------
+__global__ void k_prim(PrimArgs a);
+__global__ void k_flux_all(FluxArgs a);
+__global__ void k_sgs_smag(SmagArgs a);
+__global__ void k_sgs_sf(SfArgs a);
+__global__ void k_vort(VortArgs a);
+__global__ void k_selective(SelArgs a);
 __global__ void k_rk_post(RkArgs a);
+
+// flujos(neq) one equation at a time (the emix_flux_dev entry point)
+__global__ void k_flux_one(int neq, double *__restrict__ e, double *__restrict__ f,
+                           double *__restrict__ g, double *__restrict__ ev,
+                           double *__restrict__ fv, double *__restrict__ gv,
+                           const double *__restrict__ um, const double *__restrict__ u,
+                           const double *__restrict__ pres, const double *__restrict__ dvel,
+                           const double *__restrict__ jbn, const double *__restrict__ vis, long n);
+
+// INISGDM (solver/sgdm_incomp.f90:20-108)
+__global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__ dxyz,
+                            double *__restrict__ ratios, int nx, int ny, int nz);
 
 } // namespace emix

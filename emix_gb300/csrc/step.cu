@@ -16,13 +16,12 @@
 // The level set is advanced as part of the same SSP-RK3 step (one TVD stage
 // per flow substep, each with the velocity the flow stage uses); with a
 // frozen velocity this is exactly one cuAdvectLsJB step.
-#include "deriv.cuh"
-#include "pointwise.cuh"
-#include "weno.cuh"
+#include "plan.cuh"
 
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace emix {
 int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
@@ -36,6 +35,47 @@ __global__ void k_metric_products(const double *__restrict__ jbn, double *__rest
         jy[q] = j10 * jbn[4 * n + q];
         jz[q] = j10 * jbn[8 * n + q];
     }
+}
+int launch_single(const Launch &L, cudaStream_t st) {
+    switch (L.kind) {
+    case LK_PRIM:
+        k_prim<<<cells_grid(L.prim.n), 256, 0, st>>>(L.prim);
+        break;
+    case LK_PAD:
+        k_ghost_pad<<<cells_grid(L.pad.ng), 256, 0, st>>>(L.pad);
+        break;
+    case LK_WENO:
+        return launch_weno_stage(L.weno, st);
+    case LK_DERIV_X:
+    case LK_DERIV_YZ:
+        return launch_deriv(L.deriv.T, L.deriv.axis, L.deriv.epi, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
+                            L.deriv.F.out, L.deriv.nx, L.deriv.ny, L.deriv.nz, st);
+    case LK_SMAG:
+        k_sgs_smag<<<cells_grid(L.smag.n), 256, 0, st>>>(L.smag);
+        break;
+    case LK_SF:
+        k_sgs_sf<<<cells_grid(L.sf.n), 256, 0, st>>>(L.sf);
+        break;
+    case LK_VORT:
+        k_vort<<<cells_grid(L.vort.n), 256, 0, st>>>(L.vort);
+        break;
+    case LK_SELECT:
+        k_selective<<<cells_grid(L.sel.n), 256, 0, st>>>(L.sel);
+        break;
+    case LK_FLUX:
+        k_flux_all<<<cells_grid(L.flux.n), 256, 0, st>>>(L.flux);
+        break;
+    case LK_RK:
+        k_rk_post<<<cells_grid(L.rk.n), 256, 0, st>>>(L.rk);
+        break;
+    case LK_BC:
+        k_bc<<<cells_grid(bc_count(L.bc)), 256, 0, st>>>(L.bc);
+        break;
+    default:
+        return EMIX_ERR_ARG;
+    }
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
 }
 } // namespace emix
 
@@ -61,13 +101,17 @@ struct emix_ctx {
     int prof_n = 0;
     cudaEvent_t prof_ev[2 * 64] = {};
     int prof_cls[64] = {};
+    std::vector<Launch> plan;   // one RK3 step
 };
 
 static const char *kClassNames[] = {
     "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
     "div_x", "div_y", "div_z", "rk_post"};
-enum { CLS_PRIM, CLS_PAD, CLS_WENO, CLS_GRADX, CLS_GRADY, CLS_GRADZ, CLS_SGS, CLS_FLUX,
-       CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_COUNT };
+
+namespace emix {
+const std::vector<Launch> &ctx_plan(emix_ctx *c) { return c->plan; }
+int ctx_ready(emix_ctx *c) { return c->static_set ? 1 : 0; }
+} // namespace emix
 
 namespace {
 
@@ -86,33 +130,51 @@ struct ProfScope {
     }
 };
 
-int issue_step(emix_ctx *c) {
+Launch make(int kind, int cls) {
+    Launch L;
+    std::memset(&L, 0, sizeof L);
+    L.kind = kind;
+    L.cls = cls;
+    return L;
+}
+
+Launch deriv_launch(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
+                    double *const *w, double *const *out, int nx, int ny, int nz, int cls) {
+    Launch L = make(axis == 0 ? LK_DERIV_X : LK_DERIV_YZ, cls);
+    L.deriv.T = T;
+    for (int f = 0; f < nf; ++f) {
+        L.deriv.F.in[f] = in[f];
+        L.deriv.F.w[f] = w[f];
+        L.deriv.F.out[f] = out[f];
+    }
+    L.deriv.axis = axis; L.deriv.epi = epi; L.deriv.nf = nf;
+    L.deriv.nx = nx; L.deriv.ny = ny; L.deriv.nz = nz;
+    return L;
+}
+
+// The launches of one RK3 step, in order.
+void build_plan(emix_ctx *c) {
     const emix_params &p = c->p;
     const long n = c->n;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    cudaStream_t st = c->stream;
-    const int gb = cells_grid(n);
-    int launches = 0;
-    int rc;
     const double inv_m2 = 1.0 / (p.mach * p.mach);
-
+    std::vector<Launch> &P = c->plan;
+    P.clear();
     {
-        ProfScope ps(c, CLS_PRIM);
-        k_prim<<<gb, 256, 0, st>>>(c->um0, c->u, c->pres, inv_m2, n);
+        Launch L = make(LK_PRIM, CLS_PRIM);
+        L.prim = PrimArgs{c->um0, c->u, c->pres, inv_m2, n};
+        P.push_back(L);
     }
-    ++launches;
     if (p.level_set) {
-        const long ngc = c->ng;
-        ProfScope ps(c, CLS_PAD);
-        k_ghost_pad<<<cells_grid(ngc), 256, 0, st>>>(c->phig0, c->phi, p.ls_ghost, 1.0, nx, ny, nz);
-        ++launches;
+        Launch L = make(LK_PAD, CLS_PAD);
+        L.pad = PadArgs{c->phig0, c->phi, p.ls_ghost, 1.0, nx, ny, nz, c->ng};
+        P.push_back(L);
     }
-    EMIX_CUDA_TRY(cudaGetLastError());
-
     for (int s = 1; s <= 3; ++s) {
         const double *umcur = s == 1 ? c->um0 : c->um;
         if (p.level_set) {
-            WenoArgs a{};
+            Launch L = make(LK_WENO, CLS_WENO);
+            WenoArgs &a = L.weno;
             const int g = p.ls_ghost;
             a.phi = s == 1 ? c->phig0 : (s == 2 ? c->phigA : c->phigB);
             a.phi0 = c->phig0;
@@ -129,49 +191,46 @@ int issue_step(emix_ctx *c) {
             // the 3-cell reach of the WENO5 stencil around it, and stage 3 only on
             // the interior (stage 1 covers the whole padded grid)
             const int dims[3] = {nx, ny, nz};
+            const int gd[3] = {a.nxg, a.nyg, a.nzg};
             for (int d = 0; d < 3; ++d) {
+                a.r0[d] = 0; a.rn[d] = gd[d];
                 if (s == 2) { a.r0[d] = g - 3; a.rn[d] = dims[d] + 6; }
                 if (s == 3) { a.r0[d] = g; a.rn[d] = dims[d]; }
             }
-            ProfScope ps(c, CLS_WENO);
-            if ((rc = launch_weno_stage(a, st))) return rc;
-            ++launches;
+            P.push_back(L);
         }
         // velocity gradients (cudaDeriv; dT/dx_i feeds nothing on this path:
         // the m=5 viscous fluxes are zero, flujos_compact.f90:187-214)
         for (int ax = 0; ax < 3; ++ax) {
             const double *in[3] = {c->u, c->u + n, c->u + 2 * n};
             double *out[3] = {c->dvel + 3 * ax * n, c->dvel + (3 * ax + 1) * n, c->dvel + (3 * ax + 2) * n};
-            ProfScope ps(c, CLS_GRADX + ax);
-            if ((rc = launch_deriv(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, st))) return rc;
-            ++launches;
+            P.push_back(deriv_launch(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, CLS_GRADX + ax));
         }
         // SGS viscosity
         if (p.sgs_model == EMIX_SGS_STRUCTURE) {
-            ProfScope ps(c, CLS_SGS);
-            k_sgs_sf<<<gb, 256, 0, st>>>(c->u, c->ratios, c->dxyz, p.amu0, c->amut, nx, ny, nz);
-            k_vort<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->vort, n);
             const double cutoff = cos(20.0 * atan(1.0) / 45.0);
-            k_selective<<<gb, 256, 0, st>>>(c->vort, c->amut, c->vis, cutoff, p.c4, nx, ny, nz);
-            launches += 3;
+            Launch a = make(LK_SF, CLS_SGS), b = make(LK_VORT, CLS_SGS), d = make(LK_SELECT, CLS_SGS);
+            a.sf = SfArgs{c->u, c->ratios, c->dxyz, p.amu0, c->amut, nx, ny, nz, n};
+            b.vort = VortArgs{c->dvel, c->jbn, c->vort, n};
+            d.sel = SelArgs{c->vort, c->amut, c->vis, cutoff, p.c4, nx, ny, nz, n};
+            P.push_back(a);
+            P.push_back(b);
+            P.push_back(d);
         } else {
-            ProfScope ps(c, CLS_SGS);
-            k_sgs_smag<<<gb, 256, 0, st>>>(c->dvel, c->jbn, c->dxyz,
-                                           p.sgs_model == EMIX_SGS_NONE ? 0.0 : p.cs, p.c4, nullptr,
-                                           c->vis, n);
-            ++launches;
+            Launch L = make(LK_SMAG, CLS_SGS);
+            L.smag = SmagArgs{c->dvel, c->jbn, c->dxyz, p.sgs_model == EMIX_SGS_NONE ? 0.0 : p.cs, p.c4,
+                              nullptr, c->vis, n};
+            P.push_back(L);
         }
         // fluxes
-        FluxArgs fa{};
-        for (int q = 0; q < 15; ++q) fa.F[q] = c->flux + q * n;
-        fa.um = umcur; fa.u = c->u; fa.pres = c->pres; fa.dvel = c->dvel; fa.vis = c->vis;
-        fa.jbn = c->jbn; fa.jx = c->jx; fa.jy = c->jy; fa.jz = c->jz; fa.n = n;
         {
-            ProfScope ps(c, CLS_FLUX);
-            k_flux_all<<<gb, 256, 0, st>>>(fa);
+            Launch L = make(LK_FLUX, CLS_FLUX);
+            FluxArgs &fa = L.flux;
+            for (int q = 0; q < 15; ++q) fa.F[q] = c->flux + q * n;
+            fa.um = umcur; fa.u = c->u; fa.pres = c->pres; fa.dvel = c->dvel; fa.vis = c->vis;
+            fa.jbn = c->jbn; fa.jx = c->jx; fa.jy = c->jy; fa.jz = c->jz; fa.n = n;
+            P.push_back(L);
         }
-        ++launches;
-        EMIX_CUDA_TRY(cudaGetLastError());
         // divergence: R_m = sum over directions of the compact derivative
         for (int ax = 0; ax < 3; ++ax) {
             const double *in[5];
@@ -181,28 +240,45 @@ int issue_step(emix_ctx *c) {
                 out[m] = c->R + m * n;
                 wb[m] = c->W + m * n;
             }
-            ProfScope ps(c, CLS_DIVX + ax);
             if (ax == 0)
-                rc = launch_deriv(c->T[ax], ax, EPI_STORE, 5, in, out, out, nx, ny, nz, st);
+                P.push_back(deriv_launch(c->T[ax], ax, EPI_STORE, 5, in, out, out, nx, ny, nz, CLS_DIVX));
             else
-                rc = launch_deriv(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, st);
-            if (rc) return rc;
-            ++launches;
+                P.push_back(deriv_launch(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, CLS_DIVX + ax));
         }
-        // RK update and conversions
-        RkArgs ra{};
-        ra.R = c->R; ra.um0 = c->um0; ra.um = c->um;
-        ra.out = s == 3 ? c->um0 : c->um;
-        ra.u = c->u; ra.pres = c->pres; ra.jbn = c->jbn; ra.mask = c->mask;
-        ra.dt = p.dt; ra.mach = p.mach; ra.inv_m2 = inv_m2; ra.stage = s; ra.n = n;
+        // RK update and conversions; with walls the boundary conditions go
+        // between the RK combination and the conversions (rungek_ico.f90:98-104)
         {
-            ProfScope ps(c, CLS_RK);
-            k_rk_post<<<gb, 256, 0, st>>>(ra);
+            Launch L = make(LK_RK, CLS_RK);
+            RkArgs &ra = L.rk;
+            ra.R = c->R; ra.um0 = c->um0; ra.um = c->um;
+            ra.out = s == 3 ? c->um0 : c->um;
+            ra.u = c->u; ra.pres = c->pres; ra.jbn = c->jbn; ra.mask = c->mask;
+            ra.dt = p.dt; ra.mach = p.mach; ra.inv_m2 = inv_m2; ra.stage = s; ra.n = n;
+            ra.mode = 0;
+            if (!p.bc_walls) {
+                P.push_back(L);
+            } else {
+                L.rk.mode = 1;
+                P.push_back(L);
+                for (int axis = 2; axis >= 0; --axis) {
+                    Launch B = make(LK_BC, CLS_RK);
+                    B.bc = BcArgs{ra.out, axis, nx, ny, nz, n};
+                    P.push_back(B);
+                }
+                L.rk.mode = 2;
+                P.push_back(L);
+            }
         }
-        ++launches;
-        EMIX_CUDA_TRY(cudaGetLastError());
     }
-    c->launches = launches;
+}
+
+int issue_step(emix_ctx *c) {
+    for (const Launch &L : c->plan) {
+        ProfScope ps(c, L.cls);
+        int rc = launch_single(L, c->stream);
+        if (rc) return rc;
+    }
+    c->launches = (int)c->plan.size();
     return EMIX_OK;
 }
 
@@ -216,6 +292,7 @@ bool params_ok(const emix_params *p) {
         if (!(p->h[a] > 0.0)) return false;
     }
     if (p->sgs_model < EMIX_SGS_NONE || p->sgs_model > EMIX_SGS_STRUCTURE) return false;
+    if (p->bc_walls != 0 && p->bc_walls != 1) return false;
     if (!(p->mach > 0.0) || !(p->dt > 0.0)) return false;
     if (p->level_set && (p->ls_ghost < 3 || p->ls_ghost > p->nx || p->ls_ghost > p->ny ||
                          p->ls_ghost > p->nz))
@@ -294,6 +371,7 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
         set_last_message("clearing the context arena failed");
         return EMIX_ERR_CUDA;
     }
+    build_plan(c);
     *out = c;
     return EMIX_OK;
 }
@@ -417,13 +495,7 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
 
 int emix_ctx_launches_per_step(emix_ctx *c) {
     if (!c) return -1;
-    if (c->launches == 0) {
-        // count without launching: 2 + 3*(ls + 3 + sgs + 1 + 3 + 1)
-        const int ls = c->p.level_set ? 1 : 0;
-        const int sgs = c->p.sgs_model == EMIX_SGS_STRUCTURE ? 3 : 1;
-        return 1 + ls + 3 * (ls + 3 + sgs + 1 + 3 + 1);
-    }
-    return c->launches;
+    return (int)c->plan.size();
 }
 
 long long emix_ctx_device_bytes(emix_ctx *c) { return c ? (long long)c->arena_bytes : -1; }

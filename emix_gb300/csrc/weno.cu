@@ -6,224 +6,8 @@ namespace emix {
 
 int device_scratch(size_t bytes, double **out);
 
-namespace {
-
-// Jiang-Peng WENO5 reconstruction from five differences (Phi_x_WENO,
-// src/LevelSet/lsTools.cu:9-50).  Same weights 0.1/0.6/0.3 and
-// epsilon = 1e-6 on (beta + eps)^2; rearranged to one reciprocal:
-//   12*beta_k = 13 d_k^2 + 3 e_k^2,  alpha_k ~ c_k / (12 beta_k + 12 eps)^2,
-//   result = sum(w_k q_k) / (6 sum w_k),  w_1 = 0.1 t_2 t_3, ...
-// eps12 is 12*epsilon for differences already scaled by the metric, or
-// 12*epsilon/C^2 for unscaled differences (WENO(C v; eps) = C WENO(v; eps/C^2)).
-EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5, double eps12) {
-    const double d1 = fma(-2.0, v2, v1 + v3);
-    const double e1 = fma(-4.0, v2, fma(3.0, v3, v1));
-    const double d2 = fma(-2.0, v3, v2 + v4);
-    const double e2 = v2 - v4;
-    const double d3 = fma(-2.0, v4, v3 + v5);
-    const double e3 = fma(-4.0, v4, fma(3.0, v3, v5));
-    const double s1 = fma(13.0 * d1, d1, (3.0 * e1) * e1);
-    const double s2 = fma(13.0 * d2, d2, (3.0 * e2) * e2);
-    const double s3 = fma(13.0 * d3, d3, (3.0 * e3) * e3);
-    double t1 = s1 + eps12; t1 *= t1;
-    double t2 = s2 + eps12; t2 *= t2;
-    double t3 = s3 + eps12; t3 *= t3;
-    const double w1 = (0.1 * t2) * t3;
-    const double w2 = (0.6 * t1) * t3;
-    const double w3 = (0.3 * t1) * t2;
-    const double q1 = fma(11.0, v3, fma(-7.0, v2, 2.0 * v1));
-    const double q2 = fma(2.0, v4, fma(5.0, v3, -v2));
-    const double q3 = fma(5.0, v4, fma(2.0, v3, -v5));
-    const double num = fma(w1, q1, fma(w2, q2, w3 * q3));
-    const double den = 6.0 * (w1 + w2 + w3);
-    return num * rcp_newton(den);
-}
-
-// Positions (0..n-1) of the five differences for the left-biased (u >= 0)
-// and right-biased (u < 0) reconstruction at index i, with the edge rules
-// of PhiDevPlusParameterJB / PhiDevMinusParameterJB (lsTools.cu:623-636,
-// 716-734).
-EMIX_DEV void stencil_left(int i, int n, int p[5]) {
-    p[0] = i - 2; p[1] = i - 1; p[2] = i; p[3] = i + 1; p[4] = i + 2;
-    if (i == 0) { p[1] = i; p[0] = i + 1; }
-    if (i == 1) { p[0] = p[1]; }
-    if (i == n - 1) { p[3] = i; p[4] = p[1]; }
-    if (i == n - 2) { p[4] = p[3]; }
-}
-
-EMIX_DEV void stencil_right(int i, int n, int p[5]) {
-    // v1..v5 = D(i+3), D(i+2), D(i+1), D(i), D(i-1)
-    int im1 = i - 1, im2 = i - 2, ip1 = i + 1, ip2 = i + 2, ip3 = i + 3;
-    if (i == 0) { im1 = i; }
-    if (i == n - 1) { ip1 = i; ip2 = im1; ip3 = im2; }
-    if (i == n - 2) { ip2 = ip1; ip3 = i; }
-    if (i == n - 3) { ip3 = ip2; }
-    p[0] = ip3; p[1] = ip2; p[2] = ip1; p[3] = i; p[4] = im1;
-}
-
-// mirrored interior index of padded coordinate G (ghost width g, interior n)
-EMIX_DEV int mirror(int G, int g, int n) {
-    int I = G - g;
-    if (I < 0) I = -I - 1;
-    else if (I >= n) I = 2 * n - 1 - I;
-    return I;
-}
-
-} // namespace
-
 __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
-    // backward differences phi(p) - phi(p-1) (D(0) = phi(1) - phi(0)),
-    // unscaled, for the tile plus the [-2, +3] stencil halo of each axis
-    __shared__ double Dx[kWZ][kWY][kWX + 5];
-    __shared__ double Dy[kWZ][kWY + 5][kWX];
-    __shared__ double Dz[kWZ + 5][kWY][kWX];
-
-    const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
-    const int x0 = a.r0[0] + blockIdx.x * kWX, y0 = a.r0[1] + blockIdx.y * kWY,
-              z0 = a.r0[2] + blockIdx.z * kWZ;
-    const int xe = a.r0[0] + a.rn[0], ye = a.r0[1] + a.rn[1], ze = a.r0[2] + a.rn[2];
-    const long sxy = (long)nxg * nyg;
-    const double *__restrict__ phi = a.phi;
-    const int tid = threadIdx.x + kWX * (threadIdx.y + kWY * threadIdx.z);
-    constexpr int NT = kWX * kWY * kWZ;
-
-    for (int t = tid; t < kWZ * kWY * (kWX + 5); t += NT) {
-        const int xi = t % (kWX + 5), yz = t / (kWX + 5);
-        const int yi = yz % kWY, zi = yz / kWY;
-        const int X = x0 - 2 + xi, Y = y0 + yi, Z = z0 + zi;
-        double v = 0.0;
-        if (X >= 0 && X < nxg && Y < nyg && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = X == 0 ? phi[id + 1] - phi[id] : phi[id] - phi[id - 1];
-        }
-        Dx[zi][yi][xi] = v;
-    }
-    for (int t = tid; t < kWZ * (kWY + 5) * kWX; t += NT) {
-        const int xi = t % kWX, yz = t / kWX;
-        const int yi = yz % (kWY + 5), zi = yz / (kWY + 5);
-        const int X = x0 + xi, Y = y0 - 2 + yi, Z = z0 + zi;
-        double v = 0.0;
-        if (X < nxg && Y >= 0 && Y < nyg && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = Y == 0 ? phi[id + nxg] - phi[id] : phi[id] - phi[id - nxg];
-        }
-        Dy[zi][yi][xi] = v;
-    }
-    for (int t = tid; t < (kWZ + 5) * kWY * kWX; t += NT) {
-        const int xi = t % kWX, yz = t / kWX;
-        const int yi = yz % kWY, zi = yz / kWY;
-        const int X = x0 + xi, Y = y0 + yi, Z = z0 - 2 + zi;
-        double v = 0.0;
-        if (X < nxg && Y < nyg && Z >= 0 && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = Z == 0 ? phi[id + sxy] - phi[id] : phi[id] - phi[id - sxy];
-        }
-        Dz[zi][yi][xi] = v;
-    }
-    __syncthreads();
-
-    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
-    const int X = x0 + tx, Y = y0 + ty, Z = z0 + tz;
-    if (X >= xe || Y >= ye || Z >= ze) return;
-    const long id = X + (long)nxg * Y + sxy * Z;
-
-    // velocity and metric at the cell
-    long iv;
-    long nv;
-    if (a.reflect) {
-        const int nx = nxg - 2 * a.g, ny = nyg - 2 * a.g, nz = nzg - 2 * a.g;
-        iv = mirror(X, a.g, nx) + (long)nx * (mirror(Y, a.g, ny) + (long)ny * mirror(Z, a.g, nz));
-        nv = (long)nx * ny * nz;
-    } else {
-        iv = id;
-        nv = sxy * nzg;
-    }
-    const double ux = a.vel[iv], uy = a.vel[nv + iv], uz = a.vel[2 * nv + iv];
-    // scale of the differences: either multiply the five differences by
-    // C = jbn/h (as the reference does) or use the precomputed per-cell
-    // factors and rescale epsilon instead (one multiply per direction)
-    const bool pre = a.wc != nullptr;
-    double cx, cy, cz, ex, ey, ez, mx, my, mz;
-    if (pre) {
-        cx = 1.0; cy = 1.0; cz = 1.0;
-        mx = a.wc[iv]; my = a.wc[nv + iv]; mz = a.wc[2 * nv + iv];
-        ex = a.we[iv]; ey = a.we[nv + iv]; ez = a.we[2 * nv + iv];
-    } else {
-        cx = a.jbn[iv] * a.sx; cy = a.jbn[4 * nv + iv] * a.sy; cz = a.jbn[8 * nv + iv] * a.sz;
-        mx = 1.0; my = 1.0; mz = 1.0;
-        ex = 12.0e-6; ey = 12.0e-6; ez = 12.0e-6;
-    }
-
-    int p[5];
-    double rs;
-    // x
-    {
-        if (__double_as_longlong(ux) >= 0) stencil_left(X, nxg, p); else stencil_right(X, nxg, p);
-        const double *d = &Dx[tz][ty][0];
-        const int o = x0 - 2;
-        double phx;
-        if (pre)
-            phx = mx * weno5(d[p[0] - o], d[p[1] - o], d[p[2] - o], d[p[3] - o], d[p[4] - o], ex);
-        else
-            phx = weno5(d[p[0] - o] * cx, d[p[1] - o] * cx, d[p[2] - o] * cx, d[p[3] - o] * cx,
-                        d[p[4] - o] * cx, ex);
-        rs = ux * phx;
-    }
-    // y
-    {
-        if (__double_as_longlong(uy) >= 0) stencil_left(Y, nyg, p); else stencil_right(Y, nyg, p);
-        const int o = y0 - 2;
-        const double v1 = Dy[tz][p[0] - o][tx], v2 = Dy[tz][p[1] - o][tx], v3 = Dy[tz][p[2] - o][tx],
-                     v4 = Dy[tz][p[3] - o][tx], v5 = Dy[tz][p[4] - o][tx];
-        double phy;
-        if (pre)
-            phy = my * weno5(v1, v2, v3, v4, v5, ey);
-        else
-            phy = weno5(v1 * cy, v2 * cy, v3 * cy, v4 * cy, v5 * cy, ey);
-        rs = rs + uy * phy;
-    }
-    // z
-    {
-        const bool left = __double_as_longlong(uz) >= 0;
-        if (left) stencil_left(Z, nzg, p); else stencil_right(Z, nzg, p);
-        const int o = z0 - 2;
-        double v5 = Dz[p[4] - o][ty][tx];
-        if (left && a.ref_bugs && Z == nzg - 1) {
-            // lsTools.cu:636: id_kp2 = id_jm1 -- the z-difference one row
-            // down in y (same cell when Y == 0) at the top layer
-            const int Yb = Y == 0 ? Y : Y - 1;
-            const long ib = X + (long)nxg * Yb + sxy * Z;
-            v5 = phi[ib] - phi[ib - sxy];
-        }
-        const double v1 = Dz[p[0] - o][ty][tx], v2 = Dz[p[1] - o][ty][tx], v3 = Dz[p[2] - o][ty][tx],
-                     v4 = Dz[p[3] - o][ty][tx];
-        double phz;
-        if (pre)
-            phz = mz * weno5(v1, v2, v3, v4, v5, ez);
-        else
-            phz = weno5(v1 * cz, v2 * cz, v3 * cz, v4 * cz, v5 * cz, ez);
-        rs = rs + uz * phz;
-    }
-
-    // TVD-RK3 stage (extrapol.cu:155-212)
-    const double pin = phi[id];
-    double v;
-    if (a.stage == 1) {
-        v = fma(-a.dt, rs, pin);
-    } else {
-        const double t = fma(-a.dt, rs, pin);
-        const double p0 = a.phi0[id];
-        v = a.stage == 2 ? fma(0.25, t, 0.75 * p0) : fma(2.0, t, p0) * (1.0 / 3.0);
-    }
-    if (a.out_interior) {
-        const int g = a.g;
-        const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
-        const int I = X - g, J = Y - g, K = Z - g;
-        if (I >= 0 && I < nx && J >= 0 && J < ny && K >= 0 && K < nz)
-            a.out[I + (long)nx * (J + (long)ny * K)] = v;
-    } else {
-        a.out[id] = v;
-    }
+    weno_stage_body(a, blockIdx, threadIdx);
 }
 
 __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
@@ -237,19 +21,9 @@ __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict
     }
 }
 
-__global__ void k_ghost_pad(double *__restrict__ ghost, const double *__restrict__ val, int g,
-                            double dir, int nx, int ny, int nz) {
-    const int nxg = nx + 2 * g, nyg = ny + 2 * g, nzg = nz + 2 * g;
-    const long ng = (long)nxg * nyg * nzg;
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < ng; q += (long)gridDim.x * blockDim.x) {
-        const int X = (int)(q % nxg);
-        const int Y = (int)((q / nxg) % nyg);
-        const int Z = (int)(q / ((long)nxg * nyg));
-        const int cnt = (X < g || X >= nx + g) + (Y < g || Y >= ny + g) + (Z < g || Z >= nz + g);
-        double v = val[mirror(X, g, nx) + (long)nx * (mirror(Y, g, ny) + (long)ny * mirror(Z, g, nz))];
-        for (int c = 0; c < cnt; ++c) v *= dir;
-        ghost[q] = v;
-    }
+__global__ void k_ghost_pad(PadArgs a) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < a.ng; q += (long)gridDim.x * blockDim.x)
+        pad_cell(a, q);
 }
 
 __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict__ ghost, int g,
@@ -365,7 +139,8 @@ int emix_ghost_pad_dev(double *ghost, const double *val, int g, double direction
     if (!ghost || !val || g < 0 || g > nx || g > ny || g > nz || nx < 1 || ny < 1 || nz < 1)
         return EMIX_ERR_ARG;
     const long ng = (long)(nx + 2 * g) * (ny + 2 * g) * (nz + 2 * g);
-    k_ghost_pad<<<pad_grid(ng), 256, 0, (cudaStream_t)stream>>>(ghost, val, g, direction, nx, ny, nz);
+    PadArgs pa{ghost, val, g, direction, nx, ny, nz, ng};
+    k_ghost_pad<<<pad_grid(ng), 256, 0, (cudaStream_t)stream>>>(pa);
     EMIX_CUDA_TRY(cudaGetLastError());
     return EMIX_OK;
 }

@@ -267,6 +267,41 @@ def random_box(nx, ny, nz, seed=5, periodic=False, scheme=None, mach=0.1) -> Wor
     return w
 
 
+ENSEMBLE_SIZES = tuple(range(32, 161, 16))   # {32, 48, ..., 160}
+
+
+def ensemble(ngrids=48, seed=7, cfl=0.3, mach=0.1, scheme=SCHEME_BPER, sizes=ENSEMBLE_SIZES,
+             noise=1e-3) -> list:
+    """Uneven ensemble: grid g has nx, ny, nz drawn independently from
+    ``sizes`` and its own rotation rate omega_g ~ U[0.5, 2.0] (seeded), with
+    the periodic Taylor-Green fields of the 64^3 configuration scaled by
+    omega_g."""
+    draws = uniform(seed, 100, (ngrids, 4))
+    out = []
+    L = 2.0 * math.pi
+    for g in range(ngrids):
+        idx = np.minimum(((draws[g, :3] + 1.0) * 0.5 * len(sizes)).astype(int), len(sizes) - 1)
+        nx, ny, nz = (sizes[i] for i in idx)
+        omega = 0.5 + 1.5 * 0.5 * (draws[g, 3] + 1.0)
+        grid = Grid(int(nx), int(ny), int(nz), (L, L, L), (0.0, 0.0, 0.0), (True, True, True))
+        X, Y, Z = grid.coords()
+        u = omega * np.stack([
+            np.sin(X) * np.cos(Y) * np.cos(Z) + noise * uniform(seed + g, 1, grid.shape),
+            -np.cos(X) * np.sin(Y) * np.cos(Z) + noise * uniform(seed + g, 2, grid.shape),
+            noise * uniform(seed + g, 3, grid.shape),
+        ])
+        p = omega * omega * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
+        temp = 1.0 + 0.1 * np.sin(X) * np.sin(Y) * np.sin(Z)
+        um = _conserved(p, u, temp, mach)
+        c = L / 2.0
+        phi = np.sqrt((X - c) ** 2 + (Y - c) ** 2 + (Z - c) ** 2) - 0.25 * L
+        w = Workload(grid, (scheme,) * 3, um, phi, grid.jbn(), np.ones(grid.shape), mach=mach,
+                     name=f"ensemble_{g}_{nx}x{ny}x{nz}", extra={"omega": omega})
+        w.dt = cfl_dt(grid, u, mach, cfl)
+        out.append(w)
+    return out
+
+
 def sgs_geometry(grid: Grid):
     """Coordinates (3, nz, ny, nx) used by INISGDM (solver/sgdm_incomp.f90:2-114)."""
     return grid.coords()

@@ -29,7 +29,7 @@ def _ptr(a) -> int:
     if a is None:
         return None
     # torch tensor
-    if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
+    if str(a.dtype) != "torch.float64" or not a.is_contiguous():
         raise ValueError("tensors must be contiguous float64")
     return a.data_ptr()
 
@@ -212,6 +212,41 @@ def weno5_advect_dev_noalloc(phi, vel, jbn, h, dt, ref_bugs=0):
     return phi
 
 
+def bc_walls_dev(um):
+    """frontera_z/y/x_val in place on a (5, nz, ny, nx) device tensor."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(um)
+    check(lib.emix_bc_walls_dev(_ptr(um), nx, ny, nz, _stream()), "emix_bc_walls_dev")
+    return um
+
+
+def cfl_dev(u, xyz, mach):
+    """CFL number of TSTEP (maximum over cells), from device tensors."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(u)
+    out = C.c_double()
+    check(lib.emix_cfl_dev(_ptr(u), _ptr(xyz), mach, nx, ny, nz, C.byref(out), _stream()),
+          "emix_cfl_dev")
+    return out.value
+
+
+def tstep_dt(cfla, olddt, cfl=0.3):
+    out = C.c_double()
+    check(_lib.load().emix_tstep_dt(cfla, olddt, cfl, C.byref(out)), "emix_tstep_dt")
+    return out.value
+
+
+def metrics_dev(xyz, h, scheme=SCHEME_A):
+    """JACOBEANO: jbn (11, nz, ny, nx) from coordinates (3, nz, ny, nx) on the device."""
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(xyz)
+    jbn = torch.empty((11, nz, ny, nx), dtype=torch.float64, device=xyz.device)
+    check(lib.emix_metrics_dev(_ptr(xyz), _ptr(jbn), scheme, h[0], h[1], h[2], nx, ny, nz,
+                               _stream()), "emix_metrics_dev")
+    return jbn
+
+
 def ghost_pad_dev(val, g, direction=1.0):
     import torch
     lib = _lib.load()
@@ -247,7 +282,7 @@ class Context:
     """One grid resident in device memory; wraps ``emix_ctx``."""
 
     def __init__(self, workload=None, *, params: EmixParams | None = None, level_set=True,
-                 ref_bugs=0, ls_ghost=5):
+                 ref_bugs=0, ls_ghost=5, bc_walls=0):
         lib = _lib.load()
         if params is None:
             w = workload
@@ -266,6 +301,7 @@ class Context:
             params.level_set = 1 if level_set else 0
             params.ls_ghost = ls_ghost
             params.ref_bugs = ref_bugs
+            params.bc_walls = bc_walls
         self.params = params
         self._h = C.c_void_p()
         check(lib.emix_ctx_create(C.byref(params), C.byref(self._h)), "emix_ctx_create")
@@ -336,3 +372,103 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def _params_of(w, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0) -> EmixParams:
+    g = w.grid
+    p = EmixParams()
+    p.nx, p.ny, p.nz = g.nx, g.ny, g.nz
+    for a in range(3):
+        p.scheme[a] = w.schemes[a]
+        p.h[a] = g.h(a)
+    p.sgs_model = w.sgs_model
+    p.cs = w.cs
+    p.amu0 = w.amu0
+    p.c4 = 1.0 / w.reynolds
+    p.mach = w.mach
+    p.dt = w.dt
+    p.level_set = 1 if level_set else 0
+    p.ls_ghost = ls_ghost
+    p.ref_bugs = ref_bugs
+    p.bc_walls = bc_walls
+    return p
+
+
+class Batch:
+    """Independent grids of uneven size advanced together (``emix_batch``)."""
+
+    def __init__(self, workloads, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0):
+        lib = _lib.load()
+        self.lib = lib
+        self.workloads = list(workloads)
+        arr = (EmixParams * len(self.workloads))(
+            *[_params_of(w, level_set, ref_bugs, ls_ghost, bc_walls) for w in self.workloads])
+        self._h = C.c_void_p()
+        check(lib.emix_batch_create(len(self.workloads), arr, C.byref(self._h)), "emix_batch_create")
+        self.level_set = level_set
+        self.ctx = []
+        for g, w in enumerate(self.workloads):
+            h = C.c_void_p()
+            check(lib.emix_batch_grid(self._h, g, C.byref(h)), "emix_batch_grid")
+            self.ctx.append(h)
+            jbn = np.ascontiguousarray(w.jbn)
+            mask = np.ascontiguousarray(w.mask)
+            xyz = np.ascontiguousarray(w.grid.coords())
+            check(lib.emix_ctx_set_static(h, _ptr(jbn), _ptr(mask), _ptr(xyz)), "emix_ctx_set_static")
+        self.upload()
+
+    @property
+    def ncell(self):
+        return sum(w.grid.ncell for w in self.workloads)
+
+    def upload(self):
+        for h, w in zip(self.ctx, self.workloads):
+            um = np.ascontiguousarray(w.um)
+            phi = np.ascontiguousarray(w.phi) if self.level_set else None
+            check(self.lib.emix_ctx_upload(h, _ptr(um), _ptr(phi)), "emix_ctx_upload")
+
+    def download(self, g):
+        w = self.workloads[g]
+        nz, ny, nx = w.grid.shape
+        um = np.empty((5, nz, ny, nx))
+        phi = np.empty((nz, ny, nx)) if self.level_set else None
+        check(self.lib.emix_ctx_download(self.ctx[g], _ptr(um), _ptr(phi)), "emix_ctx_download")
+        return um, phi
+
+    def set_stream(self, stream_ptr):
+        check(self.lib.emix_batch_set_stream(self._h, C.c_void_p(stream_ptr)), "emix_batch_set_stream")
+
+    def step(self, nsteps=1, use_graph=False):
+        check(self.lib.emix_batch_step(self._h, nsteps, 1 if use_graph else 0), "emix_batch_step")
+
+    def step_per_grid(self, nsteps=1, use_graph=False):
+        check(self.lib.emix_batch_step_per_grid(self._h, nsteps, 1 if use_graph else 0),
+              "emix_batch_step_per_grid")
+
+    def set_tuning(self, cells_per_thread, yz_block, ctas_per_sm):
+        check(self.lib.emix_batch_set_tuning(self._h, cells_per_thread, yz_block, ctas_per_sm),
+              "emix_batch_set_tuning")
+
+    def tuning(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.emix_batch_get_tuning(self._h, C.byref(a), C.byref(b), C.byref(c)),
+              "emix_batch_get_tuning")
+        return a.value, b.value, c.value
+
+    def autotune(self, nsteps=2):
+        ms = C.c_double()
+        check(self.lib.emix_batch_autotune(self._h, nsteps, C.byref(ms)), "emix_batch_autotune")
+        self.upload()
+        return ms.value
+
+    def close(self):
+        if self._h:
+            self.lib.emix_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -182,6 +182,33 @@ int emix_ghost_unpad_dev(double *val, const double *ghost, int g,
                          int nx, int ny, int nz, void *stream);
 
 /* ========================================================================
+ * Boundary conditions, time step and metrics
+ * ======================================================================== */
+
+/* frontera_z_val, frontera_y_val, frontera_x_val in that order on um[5]
+ * (src/MSVSingle/frontera_z.f90:219-262, frontera_y.f90:220-247,
+ * frontera_x.f90:223-255).  Device pointers. */
+int emix_bc_walls_dev(double *um, int nx, int ny, int nz, void *stream);
+
+/* CFL number of TSTEP (src/MSVSingle/tstep_incomp.f90:99-136): the maximum
+ * over cells and axes of (|u_d| + sqrt(cs^2 + u_d^2)) / dx_d with dx_d the
+ * smaller neighbour spacing (INITSTEP) and cs = sqrt(1/Mach).  u[3], xyz[3]
+ * device pointers; *cfla is written on the host (synchronous). */
+int emix_cfl_dev(const double *u, const double *xyz, double mach, int nx, int ny, int nz,
+                 double *cfla, void *stream);
+
+/* New time step from the CFL number as TSTEP (:138-153): dt = cfl/cfla,
+ * smoothed against olddt with up = 0.5, down = 1.2. */
+int emix_tstep_dt(double cfla, double olddt, double cfl, double *dt);
+
+/* JACOBEANO (solver/jacob_malla.f90:1-171): jbn[11] from grid coordinates
+ * xyz[3] with the compact derivative of `scheme` (the reference uses
+ * EMIX_SCHEME_A) and spacings h.  Synchronous; EMIX_ERR_ARG when the
+ * Jacobian vanishes somewhere (|det| <= 1e-20). */
+int emix_metrics_dev(const double *xyz, double *jbn, int scheme, double hx, double hy, double hz,
+                     int nx, int ny, int nz, void *stream);
+
+/* ========================================================================
  * Device-resident RK3 step (solver/rungek_ico.f90:61-313)
  * ======================================================================== */
 
@@ -198,6 +225,7 @@ typedef struct emix_params {
     int level_set;      /* 1: advance the level set with the flow (WENO5, SSP-RK3) */
     int ls_ghost;       /* ghost layers of the level-set grid (5 in the reference) */
     int ref_bugs;       /* 1: keep the reference's z-top WENO neighbour index      */
+    int bc_walls;       /* 1: apply frontera_z/y/x_val after each RK combination   */
 } emix_params;
 
 typedef struct emix_ctx emix_ctx;
@@ -243,6 +271,44 @@ long long emix_ctx_device_bytes(emix_ctx *ctx);
 int emix_ctx_profile(emix_ctx *ctx, int nsteps, double *ms, int *launches);
 int emix_profile_class_count(void);
 const char *emix_profile_class_name(int cls);
+
+/* ========================================================================
+ * Batched ensemble: many independent grids of uneven size in one launch
+ * per kernel position (no counterpart in the reference, which advances one
+ * grid per process)
+ * ======================================================================== */
+
+typedef struct emix_batch emix_batch;
+
+/* One context per params[g]; all grids must share level_set, ls_ghost and
+ * sgs_model (their steps then issue the same kernel sequence). */
+int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out);
+int emix_batch_destroy(emix_batch *b);
+
+/* Member context g, for emix_ctx_set_static / _upload / _download / _state. */
+int emix_batch_grid(emix_batch *b, int g, emix_ctx **ctx);
+
+int emix_batch_set_stream(emix_batch *b, void *stream);
+
+/* Advance every grid nsteps RK3 steps: one persistent launch per kernel
+ * position over the work of all grids; use_graph = 1 replays a captured
+ * graph of one batched step. */
+int emix_batch_step(emix_batch *b, int nsteps, int use_graph);
+
+/* The same steps issued grid by grid (each grid's own launches), the
+ * comparison point for the batched form. */
+int emix_batch_step_per_grid(emix_batch *b, int nsteps, int use_graph);
+
+/* Work-list granularity of the batched launches: cells per thread of the
+ * pointwise items (x256 per item), threads per y/z pencil block (32, 64 or
+ * 128) and resident CTAs per SM of the persistent grids. */
+int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int ctas_per_sm);
+int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, int *ctas_per_sm);
+
+/* Autotuner: times every candidate tuning over nsteps batched steps and keeps
+ * the fastest (advances the state; re-upload it afterwards).  best_ms may be
+ * NULL. */
+int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms);
 
 /* Diagnostic: measured FP64 fused-multiply-add throughput of the current
  * device in lane operations per second (a short dependent-chain kernel). */

@@ -714,6 +714,114 @@ int orc_weno_advect(double *phi, const double *vel, const double *jbn,
     return 0;
 }
 
+int orc_bc_walls(double *um, int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+    double *U[5] = {um, um + n, um + 2 * n, um + 3 * n, um + 4 * n};
+    /* frontera_z_val (src/MSVSingle/frontera_z.f90:231-259) */
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            size_t k0 = lin(i, j, 0, nx, ny), k1 = lin(i, j, 1, nx, ny);
+            size_t kn = lin(i, j, nz - 1, nx, ny), kn1 = lin(i, j, nz - 2, nx, ny), kn2 = lin(i, j, nz - 3, nx, ny);
+            U[0][k0] = U[0][k1];
+            U[1][k0] = U[1][k1];
+            U[2][k0] = U[2][k1];
+            U[3][k0] = 0.0;
+            U[4][k0] = U[4][k1];
+            U[0][kn] = 1.0;
+            U[0][kn1] = 1.0;
+            U[1][kn] = U[1][kn2];
+            U[1][kn1] = U[1][kn2];
+            U[2][kn] = U[2][kn2];
+            U[2][kn1] = U[2][kn2];
+            U[3][kn] = 0.0;
+            U[3][kn1] = 0.0;
+            U[4][kn] = U[4][kn2];
+            U[4][kn1] = U[4][kn2];
+        }
+    /* frontera_y_val (frontera_y.f90:231-244) */
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nx; ++i) {
+            size_t a = lin(i, 0, k, nx, ny), a1 = lin(i, 1, k, nx, ny);
+            size_t b = lin(i, ny - 1, k, nx, ny), b1 = lin(i, ny - 2, k, nx, ny);
+            U[0][a] = U[0][a1];
+            U[0][b] = U[0][b1];
+            U[1][a] = 0.0; U[1][b] = 0.0;
+            U[2][a] = 0.0; U[2][b] = 0.0;
+            U[3][a] = 0.0; U[3][b] = 0.0;
+            U[4][a] = U[4][a1];
+            U[4][b] = U[4][b1];
+        }
+    /* frontera_x_val (frontera_x.f90:238-252) */
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j) {
+            size_t a = lin(0, j, k, nx, ny), b = lin(nx - 1, j, k, nx, ny);
+            U[1][a] = 0.0; U[2][a] = 0.0; U[3][a] = 0.0;
+            U[4][a] = U[4][a + 1];
+            U[0][a] = U[0][a + 1];
+            U[1][b] = 0.0; U[2][b] = 0.0; U[3][b] = 0.0;
+            U[4][b] = U[4][b - 1];
+            U[0][b] = U[0][b - 1];
+        }
+    return 0;
+}
+
+double orc_cfl(const double *u, const double *xyz, double mach, int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+    const double cs = std::sqrt(1. / mach);   /* source_incomp.f90:11 */
+    const int dims[3] = {nx, ny, nz};
+    const size_t st[3] = {1, (size_t)nx, (size_t)nx * ny};
+    double cfla = 0.;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t q = lin(i, j, k, nx, ny);
+                const int idx[3] = {i, j, k};
+                double c[3];
+                for (int d = 0; d < 3; ++d) {
+                    /* INITSTEP spacings (tstep_incomp.f90:11-70), inverted (:74-80) */
+                    const double *X = xyz + d * n;
+                    double h;
+                    if (idx[d] == 0) h = X[q + st[d]] - X[q];
+                    else if (idx[d] == dims[d] - 1) h = X[q] - X[q - st[d]];
+                    else h = std::fmin(X[q] - X[q - st[d]], X[q + st[d]] - X[q]);
+                    double a = std::fabs(u[d * n + q]);
+                    a = a + std::sqrt(cs * cs + a * a);   /* tstep_incomp.f90:118-123 */
+                    c[d] = (1. / h) * a;
+                }
+                cfla = std::fmax(cfla, std::fmax(c[0], std::fmax(c[1], c[2])));
+            }
+    return cfla;
+}
+
+int orc_jacobeano(const double *xyz, double *jbn, int scheme, double hx, double hy, double hz,
+                  int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+    const double h[3] = {hx, hy, hz};
+    /* jacob_malla.f90:10-123: d/dxi -> (1),(4),(7), d/deta -> (2),(5),(8), d/dzeta -> (3),(6),(9) */
+    for (int ax = 0; ax < 3; ++ax)
+        for (int c = 0; c < 3; ++c)
+            if (orc_deriv3d(scheme, ax, nx, ny, nz, h[ax], xyz + c * n, jbn + (3 * c + ax) * n)) return 1;
+    for (size_t q = 0; q < n; ++q) {
+        double j[10];
+        for (int c = 1; c <= 9; ++c) j[c] = jbn[(c - 1) * n + q];
+        const double det = j[1] * j[5] * j[9] - j[1] * j[6] * j[8] + j[2] * j[6] * j[7] -
+                           j[2] * j[4] * j[9] + j[3] * j[4] * j[8] - j[3] * j[5] * j[7];
+        if (std::fabs(det) <= 1.e-20) return 2;   /* :136-139 */
+        const double inv = 1. / det;
+        const double t1 = j[5] * j[9] - j[6] * j[8], t4 = j[3] * j[8] - j[2] * j[9],
+                     t7 = j[2] * j[6] - j[3] * j[5], t2 = j[6] * j[7] - j[4] * j[9],
+                     t5 = j[1] * j[9] - j[3] * j[7], t8 = j[3] * j[4] - j[1] * j[6],
+                     t3 = j[4] * j[8] - j[5] * j[7], t6 = j[2] * j[7] - j[1] * j[8],
+                     t9 = j[1] * j[5] - j[2] * j[4];
+        jbn[9 * n + q] = det;
+        jbn[10 * n + q] = inv;
+        jbn[q] = t1 * inv; jbn[n + q] = -t2 * inv; jbn[2 * n + q] = t3 * inv;
+        jbn[3 * n + q] = -t4 * inv; jbn[4 * n + q] = t5 * inv; jbn[5 * n + q] = -t6 * inv;
+        jbn[6 * n + q] = t7 * inv; jbn[7 * n + q] = -t8 * inv; jbn[8 * n + q] = t9 * inv;
+    }
+    return 0;
+}
+
 int orc_step(const orc_step_params *p, double *um0, double *phi,
              const double *jbn, const double *mask,
              const double *dxyzsgd, const double *ratios) {
@@ -794,6 +902,7 @@ int orc_step(const orc_step_params *p, double *um0, double *phi,
                     o[q] = (1.0 / 3.0) * a0[q] + (2.0 / 3.0) * a[q] + (2.0 / 3.0) * dt * (rs[q] + rsv[q]);
             }
         }
+        if (p->bc_walls) orc_bc_walls(um1.data(), nx, ny, nz);   /* rungek_ico.f90:98-100 */
         /* varc_to_varnc, clip to [-6,6], mask, varc_to_varnc
          * (rungek_ico.f90:104-124, herramientas_incomp2.f90:16-27) */
         for (size_t q = 0; q < n; ++q) {

@@ -115,6 +115,7 @@ typedef struct {
     int level_set;        /* 1: advance the level set with the flow: one WENO5 TVD stage per substep */
     int ls_ghost;         /* ghost layers for the level set (5 in the reference) */
     int ref_bugs;         /* 1: reproduce the reference's z-top WENO index */
+    int bc_walls;         /* 1: frontera_z/y/x_val after each RK combination */
 } orc_step_params;
 
 /* One RK3 step.  State in/out: um (5 fields) and phi (1 field, may be NULL
@@ -123,6 +124,19 @@ typedef struct {
 int orc_step(const orc_step_params *p, double *um, double *phi,
              const double *jbn, const double *mask,
              const double *dxyzsgd, const double *ratios);
+
+/* frontera_z_val, frontera_y_val, frontera_x_val in that order on um[5]
+ * (src/MSVSingle/frontera_z.f90:219-262, frontera_y.f90:220-247,
+ * frontera_x.f90:223-255). */
+int orc_bc_walls(double *um, int nx, int ny, int nz);
+
+/* CFL number of TSTEP with the spacings of INITSTEP
+ * (src/MSVSingle/tstep_incomp.f90:1-136). */
+double orc_cfl(const double *u, const double *xyz, double mach, int nx, int ny, int nz);
+
+/* JACOBEANO (solver/jacob_malla.f90:1-171) with the given scheme and spacing. */
+int orc_jacobeano(const double *xyz, double *jbn, int scheme, double hx, double hy, double hz,
+                  int nx, int ny, int nz);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

@@ -27,6 +27,7 @@ class StepParams(C.Structure):
         ("sgs_model", C.c_int), ("cs", C.c_double), ("amu0", C.c_double), ("c4", C.c_double),
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
+        ("bc_walls", C.c_int),
     ]
 
 
@@ -65,6 +66,9 @@ def load():
         "orc_weno_advect": [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double,
                             C.c_int, C.c_int, C.c_int, C.c_int],
         "orc_step": [C.POINTER(StepParams), vp, vp, vp, vp, vp, vp],
+        "orc_bc_walls": [vp, C.c_int, C.c_int, C.c_int],
+        "orc_jacobeano": [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double,
+                          C.c_int, C.c_int, C.c_int],
         "orc_set_threads": [C.c_int],
         "orc_get_threads": [],
     }
@@ -72,6 +76,8 @@ def load():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    lib.orc_cfl.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int]
+    lib.orc_cfl.restype = C.c_double
     lib.orc_phi_x_weno.argtypes = [C.c_double] * 5
     lib.orc_phi_x_weno.restype = C.c_double
     lib.orc_set_threads.restype = None
@@ -214,7 +220,27 @@ def weno_advect(phi, vel, jbn, h, dt, ref_bugs=0):
     return phi
 
 
-def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5):
+def bc_walls(um):
+    um = np.array(um, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(um)
+    _ok(load().orc_bc_walls(_p(um), nx, ny, nz), "orc_bc_walls")
+    return um
+
+
+def cfl(u, xyz, mach):
+    nx, ny, nz = _dims(xyz)
+    return load().orc_cfl(_p(np.ascontiguousarray(u)), _p(np.ascontiguousarray(xyz)), mach, nx, ny, nz)
+
+
+def jacobeano(xyz, scheme, h):
+    nx, ny, nz = _dims(xyz)
+    jbn = np.empty((11, nz, ny, nx))
+    _ok(load().orc_jacobeano(_p(np.ascontiguousarray(xyz)), _p(jbn), scheme, h[0], h[1], h[2],
+                             nx, ny, nz), "orc_jacobeano")
+    return jbn
+
+
+def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0):
     w = workload
     p = StepParams()
     p.nx, p.ny, p.nz = w.grid.nx, w.grid.ny, w.grid.nz
@@ -230,6 +256,7 @@ def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5):
     p.level_set = 1 if level_set else 0
     p.ls_ghost = ls_ghost
     p.ref_bugs = ref_bugs
+    p.bc_walls = bc_walls
     return p
 
 
