@@ -61,6 +61,13 @@ PROTOTYPES = {
                                [C.c_int] * 3 + [vp]),
     "emix_weno5_advect_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4 + [vp]),
     "emix_weno5_advect": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4),
+    "advect_CUDA": (None, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 + [C.c_double]),
+    "emix_advect_extrapolate": (C.c_int, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 +
+                                [C.c_double]),
+    "emix_advect_extrapolate_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 +
+                                    [C.c_double, vp]),
+    "emix_extrapolate_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 +
+                             [C.c_double, C.c_int, C.c_int, vp]),
     "emix_weno5_advect_dev_noalloc": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4
                                       + [vp]),
     "emix_ghost_pad_dev": (C.c_int, [vp, vp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, vp]),

@@ -112,6 +112,31 @@ def weno5_advect(phi: np.ndarray, vel: np.ndarray, jbn: np.ndarray, h, dt: float
     return out
 
 
+def advect_extrapolate(press: np.ndarray, jbn: np.ndarray, sobject: np.ndarray, delta,
+                       deltamin: float) -> np.ndarray:
+    """advect_CUDA as the reference links it: the pressure extrapolated into
+    the solid object (sobject > 0).  delta = (deltaX, deltaY, deltaZ) as the
+    Fortran passes them (the spacings h).  Returns the new pressure."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(press)
+    out = np.array(press, dtype=np.float64, copy=True, order="C")
+    rc = lib.emix_advect_extrapolate(_ptr(out), _ptr(np.ascontiguousarray(jbn)),
+                                     _ptr(np.ascontiguousarray(sobject)), delta[0], delta[1],
+                                     delta[2], nx, ny, nz, deltamin)
+    check(rc, "emix_advect_extrapolate")
+    return out
+
+
+def advect_CUDA_legacy(press: np.ndarray, jbn: np.ndarray, sobject: np.ndarray, delta,
+                       deltamin: float) -> None:
+    """The reference's void symbol advect_CUDA, in place on press."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(press)
+    assert press.dtype == np.float64 and press.flags["C_CONTIGUOUS"]
+    lib.advect_CUDA(_ptr(press), _ptr(np.ascontiguousarray(jbn)), _ptr(np.ascontiguousarray(sobject)),
+                    delta[0], delta[1], delta[2], nx, ny, nz, deltamin)
+
+
 # --------------------------------------------------------------------------
 # device forms (torch tensors)
 # --------------------------------------------------------------------------
@@ -196,6 +221,27 @@ def weno5_advect_dev(phi, vel, jbn, h, dt, ref_bugs=0):
                                     nx, ny, nz, ref_bugs, _stream()),
           "emix_weno5_advect_dev")
     return phi
+
+
+def advect_extrapolate_dev(press, jbn, sobject, delta, deltamin):
+    """advect_CUDA on device tensors, in place on press."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(press)
+    check(lib.emix_advect_extrapolate_dev(_ptr(press), _ptr(jbn), _ptr(sobject), delta[0], delta[1],
+                                          delta[2], nx, ny, nz, deltamin, _stream()),
+          "emix_advect_extrapolate_dev")
+    return press
+
+
+def extrapolate_dev(ext, phiS, jbn, delta, dtext, flag=1, iters=10):
+    """cuExtrapolation on the 5-layer mirrored padding of device tensors, in
+    place on ext."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(ext)
+    check(lib.emix_extrapolate_dev(_ptr(ext), _ptr(phiS), _ptr(jbn), delta[0], delta[1], delta[2],
+                                   nx, ny, nz, dtext, flag, iters, _stream()),
+          "emix_extrapolate_dev")
+    return ext
 
 
 def weno5_advect_dev_noalloc(phi, vel, jbn, h, dt, ref_bugs=0):

@@ -182,6 +182,42 @@ int emix_ghost_unpad_dev(double *val, const double *ghost, int g,
                          int nx, int ny, int nz, void *stream);
 
 /* ========================================================================
+ * Pressure extrapolation into the solid (the linked advect_CUDA)
+ * ======================================================================== */
+
+/* The reference's symbol advect_CUDA (src/LevelSet/lsTransportEc.cu:24-35;
+ * Fortran interface include/LevelSet/interfaceAdvect.h:3-16, called from
+ * solver/advectLS.f90:19 with deltaX = h).  As linked, it extrapolates the
+ * pressure into the solid object sobject > 0: 5 mirrored ghost layers, the
+ * direction field of DevFirstOrder_LS, 10 TVD-RK3 pseudo-steps of
+ * deltamin/2 (src/LevelSet/interface.cu:341-436).  Host buffers, synchronous,
+ * current device; errors are printed and the call returns. */
+void advect_CUDA(double *press, double *jbn, double *sobject,
+                 double deltaX, double deltaY, double deltaZ,
+                 int Nx, int Ny, int Nz, double deltamin);
+
+/* advect_CUDA with a status code (host buffers, synchronous). */
+int emix_advect_extrapolate(double *press, const double *jbn, const double *sobject,
+                            double deltaX, double deltaY, double deltaZ,
+                            int nx, int ny, int nz, double deltamin);
+
+/* advect_CUDA on device pointers, queued on `stream`.  Uses the library's
+ * per-device scratch (6 padded fields): calls that overlap on one device race. */
+int emix_advect_extrapolate_dev(double *press, const double *jbn, const double *sobject,
+                                double deltaX, double deltaY, double deltaZ,
+                                int nx, int ny, int nz, double deltamin, void *stream);
+
+/* cuExtrapolation (src/LevelSet/interface.cu:341-436) on the grid padded with
+ * 5 mirrored layers: ext extrapolated across phiS > 0 (flag > 0) or
+ * phiS <= 0 (flag <= 0) by `iters` TVD-RK3 pseudo-steps of dtext; the kernels
+ * use 1/deltaX as the reference's do.  Device pointers; jbn 11 components
+ * (1, 5, 9 read).  Same scratch caveat as above. */
+int emix_extrapolate_dev(double *ext, const double *phiS, const double *jbn,
+                         double deltaX, double deltaY, double deltaZ,
+                         int nx, int ny, int nz, double dtext, int flag, int iters,
+                         void *stream);
+
+/* ========================================================================
  * Boundary conditions, time step and metrics
  * ======================================================================== */
 

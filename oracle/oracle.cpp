@@ -714,6 +714,124 @@ int orc_weno_advect(double *phi, const double *vel, const double *jbn,
     return 0;
 }
 
+/* DevFirstOrder_LS (src/LevelSet/extrapol.cu:100-153): central differences of
+ * the solid level set times the centre metric, with the factor 1 (one-sided
+ * difference) on every boundary cell of the grid, whichever axis it borders. */
+static void dev_first_order_ls(double *dphi, const double *phiS, const double *j0, const double *j4,
+                               const double *j8, double sx, double sy, double sz,
+                               int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t id = lin(i, j, k, nx, ny);
+                size_t ip = id + 1, im = id - 1, jp = id + nx, jm = id - nx,
+                       kp = id + (size_t)nx * ny, km = id - (size_t)nx * ny;
+                double factor = 0.5;
+                if (i == 0) { im = id; factor = 1.0; }
+                if (j == 0) { jm = id; factor = 1.0; }
+                if (k == 0) { km = id; factor = 1.0; }
+                if (i == nx - 1) { ip = id; factor = 1.0; }
+                if (j == ny - 1) { jp = id; factor = 1.0; }
+                if (k == nz - 1) { kp = id; factor = 1.0; }
+                dphi[id] = factor * sx * j0[id] * (phiS[ip] - phiS[im]);
+                dphi[n + id] = factor * sy * j4[id] * (phiS[jp] - phiS[jm]);
+                dphi[2 * n + id] = factor * sz * j8[id] * (phiS[kp] - phiS[km]);
+            }
+}
+
+/* extrapolKernel (src/LevelSet/extrapol.cu:5-98): upwind right-hand side of
+ * the extrapolation equation, rs = sum_d (so dphi_d) D_d ext, where D_d is the
+ * one-sided difference on the upwind side of so*dphi_d.  On boundary cells the
+ * centre value is replaced by a neighbour (id2), the last applicable of the
+ * six boundary rules winning, as the reference writes them. */
+static void extrapol_rhs(double *rs, const double *ext, const double *phiS, const double *j0,
+                         const double *j4, const double *j8, const double *dphi, double sx,
+                         double sy, double sz, int nx, int ny, int nz, int flag) {
+    const size_t n = (size_t)nx * ny * nz;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t id = lin(i, j, k, nx, ny);
+                size_t ip = id + 1, im = id - 1, jp = id + nx, jm = id - nx,
+                       kp = id + (size_t)nx * ny, km = id - (size_t)nx * ny;
+                size_t id2 = id;
+                if (i == 0) { id2 = ip; im = id; }
+                if (j == 0) { id2 = jp; jm = id; }
+                if (k == 0) { id2 = kp; km = id; }
+                if (i == nx - 1) { id2 = im; ip = id; }
+                if (j == ny - 1) { id2 = jm; jp = id; }
+                if (k == nz - 1) { id2 = km; kp = id; }
+                const double so = flag > 0 ? (double)(phiS[id] > 0.0) : -1.0 * (double)(phiS[id] <= 0.0);
+                const double px = so * dphi[id], py = so * dphi[n + id], pz = so * dphi[2 * n + id];
+                const double xd = sx * j0[id] * (ext[id2] - ext[im]);
+                const double yd = sy * j4[id] * (ext[id2] - ext[jm]);
+                const double zd = sz * j8[id] * (ext[id2] - ext[km]);
+                const double xu = sx * j0[id] * (ext[ip] - ext[id2]);
+                const double yu = sy * j4[id] * (ext[jp] - ext[id2]);
+                const double zu = sz * j8[id] * (ext[kp] - ext[id2]);
+                double m = (double)(px > 0.0) - (double)(px < 0.0);
+                double r = (0.5 * (m + 1.0) * xd + 0.5 * std::fabs(m - 1.0) * xu) * px;
+                m = (double)(py > 0.0) - (double)(py < 0.0);
+                r += (0.5 * (m + 1.0) * yd + 0.5 * std::fabs(m - 1.0) * yu) * py;
+                m = (double)(pz > 0.0) - (double)(pz < 0.0);
+                r += (0.5 * (m + 1.0) * zd + 0.5 * std::fabs(m - 1.0) * zu) * pz;
+                rs[id] = r;
+            }
+}
+
+int orc_extrapolation(double *ext, const double *phiS, const double *j0, const double *j4,
+                      const double *j8, double sx, double sy, double sz, int nx, int ny, int nz,
+                      double dtext, int flag, int iters) {
+    /* cuExtrapolation (src/LevelSet/interface.cu:341-436): the gradient of the
+     * solid level set once, then `iters` TVD-RK3 pseudo-steps (10 in the
+     * reference) of the extrapolation equation with RunGK_First/Second/ThirdS
+     * (src/LevelSet/extrapol.cu:155-212). */
+    if (nx < 2 || ny < 2 || nz < 2 || iters < 0) return 1;
+    const size_t n = (size_t)nx * ny * nz;
+    std::vector<double> dphi(3 * n), rs(n), d(n);
+    dev_first_order_ls(dphi.data(), phiS, j0, j4, j8, sx, sy, sz, nx, ny, nz);
+    for (int it = 0; it < iters; ++it) {
+        extrapol_rhs(rs.data(), ext, phiS, j0, j4, j8, dphi.data(), sx, sy, sz, nx, ny, nz, flag);
+        for (size_t q = 0; q < n; ++q) d[q] = ext[q] - dtext * rs[q];
+        extrapol_rhs(rs.data(), d.data(), phiS, j0, j4, j8, dphi.data(), sx, sy, sz, nx, ny, nz, flag);
+        for (size_t q = 0; q < n; ++q) d[q] = 0.75 * ext[q] + 0.25 * (d[q] - dtext * rs[q]);
+        extrapol_rhs(rs.data(), d.data(), phiS, j0, j4, j8, dphi.data(), sx, sy, sz, nx, ny, nz, flag);
+        for (size_t q = 0; q < n; ++q) ext[q] = (ext[q] + 2.0 * (d[q] - dtext * rs[q])) / 3.0;
+    }
+    return 0;
+}
+
+int orc_advect_extrapolate(double *press, const double *jbn, const double *sobject,
+                           double deltaX, double deltaY, double deltaZ, int nx, int ny, int nz,
+                           double deltamin) {
+    /* advect_CUDA as linked (src/LevelSet/lsTransportEc.cu:24-197): pad
+     * pressure, the solid level set and the metric components 1, 5, 9 with 5
+     * mirrored ghost layers (:91-157), extrapolate the pressure across the
+     * solid with dtext = deltamin/2 and Flag = 1 (:161-162), then copy the
+     * interior back (:164-168).  The kernels get 1/deltaX (interface.cu:372-377). */
+    const int g = 5;
+    if (nx < g || ny < g || nz < g) return 1;
+    const int nxg = nx + 2 * g, nyg = ny + 2 * g, nzg = nz + 2 * g;
+    const size_t n = (size_t)nx * ny * nz, ng = (size_t)nxg * nyg * nzg;
+    std::vector<double> P(ng, 0.0), S(ng, 0.0), J(3 * ng, 0.0);
+    orc_to_ghost(P.data(), press, g, nx, ny, nz);
+    orc_mirror_ghost(P.data(), g, nx, ny, nz, 1.0);
+    orc_to_ghost(S.data(), sobject, g, nx, ny, nz);
+    orc_mirror_ghost(S.data(), g, nx, ny, nz, 1.0);
+    for (int c = 0; c < 3; ++c) {
+        orc_to_ghost(&J[c * ng], jbn + (size_t)(4 * c) * n, g, nx, ny, nz);
+        orc_mirror_ghost(&J[c * ng], g, nx, ny, nz, 1.0);
+    }
+    int rc = orc_extrapolation(P.data(), S.data(), &J[0], &J[ng], &J[2 * ng], 1.0 / deltaX,
+                               1.0 / deltaY, 1.0 / deltaZ, nxg, nyg, nzg, deltamin * 0.5, 1, 10);
+    if (rc) return rc;
+    orc_from_ghost(press, P.data(), g, nx, ny, nz);
+    return 0;
+}
+
 int orc_bc_walls(double *um, int nx, int ny, int nz) {
     const size_t n = (size_t)nx * ny * nz;
     double *U[5] = {um, um + n, um + 2 * n, um + 3 * n, um + 4 * n};

@@ -17,8 +17,8 @@
  *
  * Parity pinning: the reference has no tests, golden vectors or fixtures,
  * and its Fortran CPU path cannot be compiled here (no Fortran compiler).
- * Scheme C, cuDivergence, the WENO5 TVD-RK3 step and the ghost padding are
- * pinned against outputs of the reference's own CUDA kernels run on a GPU
+ * Scheme C, cuDivergence, the WENO5 TVD-RK3 step, the ghost padding and the
+ * pressure extrapolation of advect_CUDA are pinned against outputs of the reference's own CUDA kernels run on a GPU
  * (tests/golden/reference_cuda.npz); the Fortran-only parts (schemes A, B and
  * cyclic B, flujos, the SGS models, the RK loop) are pinned by analytic
  * known-answer tests only -- parity against the reference's own outputs is
@@ -137,6 +137,21 @@ double orc_cfl(const double *u, const double *xyz, double mach, int nx, int ny, 
 /* JACOBEANO (solver/jacob_malla.f90:1-171) with the given scheme and spacing. */
 int orc_jacobeano(const double *xyz, double *jbn, int scheme, double hx, double hy, double hz,
                   int nx, int ny, int nz);
+
+/* cuExtrapolation (src/LevelSet/interface.cu:341-436) on an (already padded)
+ * grid: ext is extrapolated across the region phiS > 0 (flag > 0) or
+ * phiS <= 0 (flag <= 0); j0, j4, j8 are metric components 1, 5, 9; sx, sy, sz
+ * the inverse spacings the kernels receive; iters TVD-RK3 pseudo-steps. */
+int orc_extrapolation(double *ext, const double *phiS, const double *j0, const double *j4,
+                      const double *j8, double sx, double sy, double sz, int nx, int ny, int nz,
+                      double dtext, int flag, int iters);
+
+/* advect_CUDA as linked (src/LevelSet/lsTransportEc.cu:24-197): pressure
+ * extrapolation into the solid object sobject, with 5 mirrored ghost layers;
+ * press in/out, jbn 11 components (1, 5, 9 read). */
+int orc_advect_extrapolate(double *press, const double *jbn, const double *sobject,
+                           double deltaX, double deltaY, double deltaZ, int nx, int ny, int nz,
+                           double deltamin);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

@@ -69,6 +69,10 @@ def load():
         "orc_bc_walls": [vp, C.c_int, C.c_int, C.c_int],
         "orc_jacobeano": [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double,
                           C.c_int, C.c_int, C.c_int],
+        "orc_extrapolation": [vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                              C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int],
+        "orc_advect_extrapolate": [vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                                   C.c_int, C.c_int, C.c_int, C.c_double],
         "orc_set_threads": [C.c_int],
         "orc_get_threads": [],
     }
@@ -218,6 +222,26 @@ def weno_advect(phi, vel, jbn, h, dt, ref_bugs=0):
     _ok(load().orc_weno_advect(_p(phi), _p(np.ascontiguousarray(vel)), _p(np.ascontiguousarray(jbn)),
                                h[0], h[1], h[2], dt, nx, ny, nz, ref_bugs), "orc_weno_advect")
     return phi
+
+
+def extrapolation(ext, phiS, j0, j4, j8, s, dtext, flag=1, iters=10):
+    """cuExtrapolation on a given (padded) grid; returns the extrapolated field."""
+    ext = np.array(ext, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(ext)
+    c = np.ascontiguousarray
+    _ok(load().orc_extrapolation(_p(ext), _p(c(phiS)), _p(c(j0)), _p(c(j4)), _p(c(j8)), s[0], s[1],
+                                 s[2], nx, ny, nz, dtext, flag, iters), "orc_extrapolation")
+    return ext
+
+
+def advect_extrapolate(press, jbn, sobject, delta, deltamin):
+    """advect_CUDA as linked: pressure extrapolated into the solid object."""
+    press = np.array(press, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(press)
+    c = np.ascontiguousarray
+    _ok(load().orc_advect_extrapolate(_p(press), _p(c(jbn)), _p(c(sobject)), delta[0], delta[1],
+                                      delta[2], nx, ny, nz, deltamin), "orc_advect_extrapolate")
+    return press
 
 
 def bc_walls(um):

@@ -7,6 +7,8 @@
 //   div    : cuDivergence                 solver/cuDivergence.cu:107-189
 //   weno   : cuAdvectLsJB                 src/LevelSet/lsTransportEc.cu:201-418
 //   pad    : cuSwapToGhost + mirrors      src/LevelSet/lsTransportEc.cu:91-127
+//   extrap : advect_CUDA as linked        src/LevelSet/lsTransportEc.cu:24-197
+//            with cuExtrapolation         src/LevelSet/interface.cu:341-436
 // with two deliberate differences: the z grid of the level-set kernels is
 // NzG/5 (the reference writes NxG/5, :232), and grids are only used where they
 // tile the arrays exactly (the level-set kernels have no bounds checks).
@@ -16,6 +18,7 @@
 //   ref_harness div <nx> <ny> <nz> <hx> <hy> <hz> e f g ev fv gv jbn rs rsv   (.bin paths)
 //   ref_harness weno <nxg> <nyg> <nzg> <hx> <hy> <hz> <dt> phi vel jbn out
 //   ref_harness pad <nx> <ny> <nz> <g> val out
+//   ref_harness extrap <nx> <ny> <nz> <dX> <dY> <dZ> <deltamin> press jbn sobject out
 #include <cuda.h>
 #include <cxxabi.h>
 
@@ -306,6 +309,66 @@ int main(int argc, char **argv) {
         launch(kY, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, am);
         launch(kX, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, am);
         write_bin(argv[7], download(G, ng));
+    } else if (mode == "extrap" && argc == 13) {
+        int nx = atoi(argv[2]), ny = atoi(argv[3]), nz = atoi(argv[4]);
+        double dX = atof(argv[5]), dY = atof(argv[6]), dZ = atof(argv[7]), dmin = atof(argv[8]);
+        int g = 5;
+        const int nxg = nx + 2 * g, nyg = ny + 2 * g, nzg = nz + 2 * g;
+        if (nx % 10 || ny % 10 || nz % 5 || nxg != nyg || nyg != nzg) {
+            fprintf(stderr, "extrap: sizes must tile the reference grids exactly (cubic padded grid)\n");
+            return 5;
+        }
+        size_t n = (size_t)nx * ny * nz, ng = (size_t)nxg * nyg * nzg;
+        CUdeviceptr pW = upload(read_bin(argv[9], n)), jW = upload(read_bin(argv[10], 11 * n)),
+                    sW = upload(read_bin(argv[11], n));
+        CUdeviceptr pG = dalloc(ng), sG = dalloc(ng), jG = dalloc(11 * ng);
+        CUfunction kS = find_kernel("cuSwapToGhost"), kF = find_kernel("cuSwapFromGhost"),
+                   kZ = find_kernel("cuGhostCellsMirror3dZ"), kY = find_kernel("cuGhostCellsMirror3dY"),
+                   kX = find_kernel("cuGhostCellsMirror3dX"), kD = find_kernel("DevFirstOrder_LS"),
+                   kE = find_kernel("extrapolKernel"), k1 = find_kernel("RunGK_FirstS"),
+                   k2 = find_kernel("RunGK_SecondS"), k3 = find_kernel("RunGK_ThirdS");
+        // lsTransportEc.cu:99-157: pad, then mirror (press and sobject Z,Y,X; jbn X,Y,Z)
+        auto swap_to = [&](CUdeviceptr G, CUdeviceptr W) {
+            void *a[] = {&G, &W, &g, &nx, &ny, &nz};
+            launch(kS, nx / 10, ny / 10, nz / 5, 10, 10, 5, 0, a);
+        };
+        swap_to(pG, pW);
+        for (int c : {0, 4, 8}) swap_to(jG + c * ng * sizeof(double), jW + c * n * sizeof(double));
+        swap_to(sG, sW);
+        double dir = 1.0;
+        auto mirror = [&](CUfunction k, CUdeviceptr G) {
+            void *a[] = {&G, &g, &nx, &ny, &nz, &dir};
+            launch(k, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, a);
+        };
+        for (CUdeviceptr G : {pG, sG}) { mirror(kZ, G); mirror(kY, G); mirror(kX, G); }
+        for (int c : {0, 4, 8}) {
+            CUdeviceptr G = jG + c * ng * sizeof(double);
+            mirror(kX, G); mirror(kY, G); mirror(kZ, G);
+        }
+        // cuExtrapolation(d_press, d_sobject, d_jbn, dX, dY, dZ, NxG, NyG, NzG, deltamin*0.5, 1)
+        CUdeviceptr dPhi = dalloc(3 * ng), rs = dalloc(ng), d = dalloc(ng);
+        const int gx = nxg / 10, gy = nyg / 10, gz = nzg / 5;
+        double sx = 1.0 / dX, sy = 1.0 / dY, sz = 1.0 / dZ, dtext = dmin * 0.5;
+        unsigned ux = nxg, uy = nyg, uz = nzg;
+        int ix = nxg, iy = nyg, iz = nzg, flag = 1;
+        void *ad[] = {&dPhi, &sG, &jG, &sx, &sy, &sz, &ux, &uy, &uz};
+        launch(kD, gx, gy, gz, 10, 10, 5, 0, ad);
+        for (int it = 1; it <= 10; ++it) {
+            void *e1[] = {&rs, &pG, &sG, &jG, &dPhi, &sx, &sy, &sz, &ux, &uy, &uz, &flag};
+            launch(kE, gx, gy, gz, 10, 10, 5, 0, e1);
+            void *r1[] = {&d, &pG, &dtext, &rs, &ix, &iy, &iz};
+            launch(k1, gx, gy, gz, 10, 10, 5, 0, r1);
+            void *e2[] = {&rs, &d, &sG, &jG, &dPhi, &sx, &sy, &sz, &ux, &uy, &uz, &flag};
+            launch(kE, gx, gy, gz, 10, 10, 5, 0, e2);
+            void *r2[] = {&d, &pG, &d, &dtext, &rs, &ix, &iy, &iz};
+            launch(k2, gx, gy, gz, 10, 10, 5, 0, r2);
+            launch(kE, gx, gy, gz, 10, 10, 5, 0, e2);
+            void *r3[] = {&pG, &pG, &d, &dtext, &rs, &ix, &iy, &iz};
+            launch(k3, gx, gy, gz, 10, 10, 5, 0, r3);
+        }
+        void *af[] = {&pW, &pG, &g, &nx, &ny, &nz};
+        launch(kF, nx / 10, ny / 10, nz / 5, 10, 10, 5, 0, af);
+        write_bin(argv[12], download(pW, n));
     } else {
         fprintf(stderr, "bad arguments for mode %s\n", mode.c_str());
         return 1;

@@ -12,10 +12,11 @@ GPU machine:
     python tests/golden/make_reference_golden.py [out.npz]
 
 Cases: the variant-C compact derivative along each axis (cu::cs::dFdX/Y/Z),
-cuDivergence, one cuAdvectLsJB WENO5 TVD-RK3 step, and the ghost padding of
-advect_CUDA.  Only the reference's outputs are stored; the inputs are
-regenerated from seeds by deriv_cases(), div_case(), weno_case() and
-pad_case() below.
+cuDivergence, one cuAdvectLsJB WENO5 TVD-RK3 step, the ghost padding of
+advect_CUDA, and advect_CUDA itself (the pressure extrapolation into the
+solid).  Only the reference's outputs are stored; the inputs are regenerated
+from seeds by deriv_cases(), div_case(), weno_case(), pad_case() and
+extrap_case() below.
 """
 from __future__ import annotations
 
@@ -87,6 +88,22 @@ def pad_case():
     return np.ascontiguousarray(F.uniform(65, 0, (20, 20, 20)))
 
 
+def extrap_case():
+    """press, jbn (11), sobject (a sphere, > 0 inside the solid), delta, deltamin."""
+    n = 20
+    sh = (n, n, n)
+    z, y, x = np.meshgrid(*(np.arange(n) / (n - 1),) * 3, indexing="ij")
+    sobj = 0.32 - np.sqrt((x - 0.45) ** 2 + (y - 0.55) ** 2 + (z - 0.5) ** 2)
+    press = np.sin(3 * x) + np.cos(2 * y) * z + 0.01 * F.uniform(66, 0, sh)
+    jbn = np.zeros((11,) + sh)
+    for c in range(11):
+        jbn[c] = F.uniform(66, 1 + c, sh)
+    for c in (0, 4, 8):
+        jbn[c] = 1.0 + 0.1 * F.uniform(66, 20 + c, sh)
+    return (np.ascontiguousarray(press), np.ascontiguousarray(jbn), np.ascontiguousarray(sobj),
+            (0.05, 0.055, 0.06), 0.04)
+
+
 def main(out_path=None):
     out_path = Path(out_path) if out_path else Path(__file__).resolve().parent / "reference_cuda.npz"
     build_harness()
@@ -125,6 +142,10 @@ def main(out_path=None):
         val = pad_case()
         run("pad", 20, 20, 20, 5, wr("val", val), td / "pad.bin")
         res.update(pad_out=np.fromfile(td / "pad.bin").reshape(30, 30, 30))
+        press, jbn, sobj, delta, dmin = extrap_case()
+        run("extrap", 20, 20, 20, *map(repr, delta), repr(dmin), wr("press", press), wr("jbn", jbn),
+            wr("sobj", sobj), td / "extrap.bin")
+        res.update(extrap_out=np.fromfile(td / "extrap.bin").reshape(press.shape))
     np.savez_compressed(out_path, **res)
     print(f"wrote {out_path} ({out_path.stat().st_size} bytes, {len(res)} arrays)")
 

@@ -4,7 +4,8 @@ tests/golden/reference_cuda.npz holds outputs of the reference's kernels
 (compiled unmodified from its sources, run on a GB300 by
 tests/golden/make_reference_golden.py): the variant-C compact derivative
 (cu::cs::dFdX/Y/Z), cuDivergence, one cuAdvectLsJB WENO5 TVD-RK3 step (with
-the reference's own z-top neighbour index) and the advect_CUDA ghost padding.
+the reference's own z-top neighbour index), the advect_CUDA ghost padding and
+advect_CUDA itself (pressure extrapolation into the solid).
 The oracle must match them to 1e-12 (normwise relative L-inf), the padding
 bitwise.  The GPU test at the end checks the CUDA library against the same
 vectors.
@@ -37,6 +38,8 @@ def gold():
     g["div_jbn"] = jbn
     g["weno_phi"], g["weno_vel"], g["weno_jbn"], _, _ = mg.weno_case()
     g["pad_in"] = mg.pad_case()
+    g["extrap_press"], g["extrap_jbn"], g["extrap_sobj"], g["extrap_delta"], g["extrap_dmin"] = \
+        mg.extrap_case()
     return g
 
 
@@ -64,6 +67,32 @@ def test_oracle_weno_matches_reference_kernels(oracle, gold):
 
 def test_oracle_padding_matches_reference_kernels(oracle, gold):
     assert np.array_equal(oracle.ghost_pad(gold["pad_in"], 5, 1.0), gold["pad_out"])
+
+
+def test_oracle_extrapolation_matches_reference_kernels(oracle, gold):
+    if "extrap_out" not in gold:
+        pytest.skip("no advect_CUDA vectors in this golden file")
+    out = oracle.advect_extrapolate(gold["extrap_press"], gold["extrap_jbn"], gold["extrap_sobj"],
+                                    gold["extrap_delta"], gold["extrap_dmin"])
+    # the extrapolation moves only the solid side, so compare the change too
+    assert_close(out, gold["extrap_out"], tol=TOL, what="press")
+    assert_close(out - gold["extrap_press"], gold["extrap_out"] - gold["extrap_press"], tol=1e-11,
+                 what="change of press")
+
+
+@pytest.mark.gpu
+def test_cuda_extrapolation_matches_reference_kernels(emix, gold):
+    if "extrap_out" not in gold:
+        pytest.skip("no advect_CUDA vectors in this golden file")
+    out = emix.advect_extrapolate(gold["extrap_press"], gold["extrap_jbn"], gold["extrap_sobj"],
+                                  gold["extrap_delta"], gold["extrap_dmin"])
+    assert_close(out, gold["extrap_out"], tol=TOL, what="press")
+    assert_close(out - gold["extrap_press"], gold["extrap_out"] - gold["extrap_press"], tol=1e-11,
+                 what="change of press")
+    legacy = np.array(gold["extrap_press"], copy=True)
+    emix.advect_CUDA_legacy(legacy, gold["extrap_jbn"], gold["extrap_sobj"], gold["extrap_delta"],
+                            gold["extrap_dmin"])
+    assert np.array_equal(legacy, out)
 
 
 @pytest.mark.gpu
