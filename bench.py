@@ -44,13 +44,30 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+# Cells one launch of each kernel class covers, averaged over its launches in
+# a step.  The level-set stages cover the padded grid (stage 1), the grid
+# grown by the 3-cell WENO5 reach (stage 2) and the interior (stage 3).
+def cells_per_launch(name: str, dims, g: int) -> float:
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    if name == "weno_stage":
+        return ((nx + 2 * g) * (ny + 2 * g) * (nz + 2 * g) + (nx + 6) * (ny + 6) * (nz + 6) + n) / 3.0
+    if name == "ghost_pad":
+        return (nx + 2 * g) * (ny + 2 * g) * (nz + 2 * g)
+    return n
+
+
 # Algorithmic bytes per launch of each kernel class, per cell of the grid
 # (n = cells, ng = ghost-padded cells of the level-set grid): every field a
 # kernel must read or write, once.
-def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1) -> float:
+def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1, dims=None, g: int = 5) -> float:
     d = 8.0
-    if name == "weno_stage":       # phi_s (ng) + phi_0 (ng, stages 2,3) + u(3n) + jbn(3n) -> out
-        return d * ((1.0 + 2.0 / 3.0) * ng + 6 * n + (2.0 * ng + n) / 3.0)
+    if name == "weno_stage":
+        # per stage: phi_s over the stage's region, phi_0 (stages 2, 3), u (3n)
+        # and jbn (3n) read once, phi_out over the region written
+        nx, ny, nz = dims
+        r = ((nx + 2 * g) * (ny + 2 * g) * (nz + 2 * g), (nx + 6) * (ny + 6) * (nz + 6), n)
+        return d * (2 * r[0] + 6 * n + 3 * r[1] + 6 * n + 3 * r[2] + 6 * n) / 3.0
     if name in ("grad_x", "grad_y", "grad_z"):
         return d * 6 * n           # 3 in, 3 out
     if name == "div_x":
@@ -73,6 +90,9 @@ def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1) -> float:
 # FP64 lane operations per cell of each kernel class (per launch), counted
 # from the kernel source (adds, multiplies and FMAs; a divide or square root
 # counted as the 8 operations of its refinement sequence).
+# wall boundary conditions of the tank (frontera_z/y/x_val) in every substep
+WALLS = 1
+
 FP64_OPS_PER_CELL = {
     "weno_stage": 3 * 62 + 8, "grad_x": 3 * 6, "grad_y": 3 * 6, "grad_z": 3 * 6,
     "div_x": 5 * 6, "div_y": 5 * 7, "div_z": 5 * 7, "flux": 55, "sgs": 32,
@@ -147,7 +167,7 @@ def cpu_sample(steps: int, warmup: int):
     from emix_gb300 import fields as F
     from oracle import oracle_py as O
     w = F.stirred_tank(n=SAMPLE_N)
-    p = O.step_params(w)
+    p = O.step_params(w, bc_walls=WALLS)
     d, r = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
     um, phi = w.um, w.phi
     for _ in range(warmup):
@@ -234,6 +254,7 @@ def config_dict(w):
         "grid": [N_GRID, N_GRID, N_GRID],
         "scheme": "Lele-6 compact, 3rd/4th-order closures (derivada_incomp.f90)",
         "sgs": "Smagorinsky Cs=0.1", "level_set": "WENO5 TVD stage per substep",
+        "walls": "frontera_z/y/x_val after every RK combination" if WALLS else "none",
         "cfl": 0.3, "dt": None if w is None else w.dt, "precision": "fp64",
         "l2": "inputs larger than L2 (9 GB resident, 128 MiB per field)",
         "parallelism": "replicas (one independent grid per GPU)",
@@ -277,7 +298,7 @@ def main():
     w = F.stirred_tank(n=N_GRID)
     n = w.grid.ncell
     ng = (N_GRID + 2 * G) ** 3
-    ctx = ops.Context(w, level_set=True, ls_ghost=G)
+    ctx = ops.Context(w, level_set=True, ls_ghost=G, bc_walls=WALLS)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.step(args.warmup, use_graph=True)
@@ -331,8 +352,8 @@ def main():
     top_ms = prof[top][0] / prof[top][1]
     hbm_peak, peak_kind = _peaks()
     fp64_peak = ops.fp64_peak()
-    ab = algorithmic_bytes(top, n, ng)
-    cells_top = ng if top in ("weno_stage", "ghost_pad") else n
+    ab = algorithmic_bytes(top, n, ng, dims=(N_GRID,) * 3, g=G)
+    cells_top = cells_per_launch(top, (N_GRID,) * 3, G)
     fp64_ach = FP64_OPS_PER_CELL.get(top, 0) * cells_top / (top_ms * 1e-3)
     achieved = ab / (top_ms * 1e-3) / 1e9
     traffic = None

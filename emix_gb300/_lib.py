@@ -35,7 +35,7 @@ class EmixParams(C.Structure):
         ("cs", C.c_double), ("amu0", C.c_double), ("c4", C.c_double),
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
-        ("bc_walls", C.c_int),
+        ("bc_walls", C.c_int), ("filter_every", C.c_int), ("cfilt", C.c_double),
     ]
 
 
@@ -61,6 +61,9 @@ PROTOTYPES = {
                                [C.c_int] * 3 + [vp]),
     "emix_weno5_advect_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4 + [vp]),
     "emix_weno5_advect": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4),
+    "emix_filtrado_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
+    "emix_filter_dev": (C.c_int, [vp, C.c_int, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_int, vp]),
     "advect_CUDA": (None, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 + [C.c_double]),
     "emix_advect_extrapolate": (C.c_int, [vp, vp, vp] + [C.c_double] * 3 + [C.c_int] * 3 +
                                 [C.c_double]),
@@ -80,6 +83,8 @@ PROTOTYPES = {
     "emix_ctx_download": (C.c_int, [vp, vp, vp]),
     "emix_ctx_state": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "emix_step": (C.c_int, [vp, C.c_int, C.c_int]),
+    "emix_ctx_get_step_index": (C.c_int, [vp, C.POINTER(C.c_long)]),
+    "emix_ctx_set_step_index": (C.c_int, [vp, C.c_long]),
     "emix_step_host": (C.c_int, [vp, vp, vp, C.c_int]),
     "emix_ctx_launches_per_step": (C.c_int, [vp]),
     "emix_ctx_device_bytes": (C.c_longlong, [vp]),

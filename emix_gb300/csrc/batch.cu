@@ -50,7 +50,7 @@ struct VortOp { using A = VortArgs; static EMIX_DEV void cell(const A &a, long q
 struct SelOp { using A = SelArgs; static EMIX_DEV void cell(const A &a, long q) { select_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
 struct FluxOp { using A = FluxArgs; static EMIX_DEV void cell(const A &a, long q) { flux_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
 struct BcOp { using A = BcArgs; static EMIX_DEV void cell(const A &a, long q) { bc_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return bc_count(a); } };
-struct RkOp { using A = RkArgs; static EMIX_DEV void cell(const A &a, long q) { rk_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
+struct RkOp { using A = RkArgs; static EMIX_DEV void cell(const A &a, long q) { rk_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return rk_count(a); } };
 
 template <class Op>
 __global__ void __launch_bounds__(256, 2)
@@ -198,7 +198,7 @@ long point_count(const Launch &L) {
     case LK_VORT: return L.vort.n;
     case LK_SELECT: return L.sel.n;
     case LK_FLUX: return L.flux.n;
-    case LK_RK: return L.rk.n;
+    case LK_RK: return rk_count(L.rk);
     case LK_BC: return bc_count(L.bc);
     default: return 0;
     }
@@ -390,6 +390,11 @@ extern "C" {
 int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
     if (!out || !params || ngrid < 1) return EMIX_ERR_ARG;
     *out = nullptr;
+    for (int g = 0; g < ngrid; ++g)
+        if (params[g].filter_every != 0) {
+            set_last_message("emix_batch_create: the compact filter is not batched (filter_every must be 0)");
+            return EMIX_ERR_ARG;
+        }
     for (int g = 1; g < ngrid; ++g)
         if (params[g].level_set != params[0].level_set || params[g].sgs_model != params[0].sgs_model ||
             params[g].bc_walls != params[0].bc_walls ||

@@ -23,7 +23,7 @@ enum LaunchKind {
 // profile classes (emix_ctx_profile)
 enum {
     CLS_PRIM, CLS_PAD, CLS_WENO, CLS_GRADX, CLS_GRADY, CLS_GRADZ, CLS_SGS, CLS_FLUX,
-    CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_COUNT
+    CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_FILTER, CLS_COUNT
 };
 
 struct DerivArgs {
@@ -51,5 +51,11 @@ struct Launch {
 };
 
 int launch_single(const Launch &L, cudaStream_t st);
+
+// compact filter (filter.cu): filtrado on um[5] in place; the tables are
+// prepared on the host before any stream capture
+int launch_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, int nz,
+                    cudaStream_t st);
+int prepare_filtrado(double cfilt, int nx, int ny, int nz);
 
 } // namespace emix

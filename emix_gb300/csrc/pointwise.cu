@@ -100,7 +100,7 @@ __global__ void k_sgs_smag(SmagArgs a) { EMIX_FOR_CELLS(q, a.n) smag_cell(a, q);
 __global__ void k_sgs_sf(SfArgs a) { EMIX_FOR_CELLS(q, a.n) sf_cell(a, q); }
 __global__ void k_vort(VortArgs a) { EMIX_FOR_CELLS(q, a.n) vort_cell(a, q); }
 __global__ void k_selective(SelArgs a) { EMIX_FOR_CELLS(q, a.n) select_cell(a, q); }
-__global__ void k_rk_post(RkArgs a) { EMIX_FOR_CELLS(q, a.n) rk_cell(a, q); }
+__global__ void k_rk_post(RkArgs a) { EMIX_FOR_CELLS(q, rk_count(a)) rk_cell(a, q); }
 
 } // namespace emix
 

@@ -229,38 +229,45 @@ struct RkArgs {
     const double *mask;
     double dt, mach, inv_m2;
     int stage;
-    int mode;             // 0: RK + conversions; 1: RK only (um1 -> out); 2: conversions of out
+    int walls;            // 1: frontera_z/y/x_val between the RK combination and the conversions
+    int faces;            // with walls: 0 = cells no wall rule touches, 1 = the wall cells
+    int nx, ny, nz;
     long n;
 };
 
-EMIX_DEV void rk_cell(const RkArgs &a, long q) {
+// Wall cells: z = 0, nz-2, nz-1 (frontera_z), y = 0, ny-1 (frontera_y),
+// x = 0, nx-1 (frontera_x).  Enumerated as the three z planes, then the two
+// y planes for z in [1, nz-3], then the two x planes for y in [1, ny-2].
+__host__ __device__ inline long rk_face_count(int nx, int ny, int nz) {
+    return 3L * nx * ny + 2L * nx * (nz - 3) + 2L * (ny - 2) * (nz - 3);
+}
+
+__host__ __device__ inline long rk_count(const RkArgs &a) {
+    return (a.walls && a.faces) ? rk_face_count(a.nx, a.ny, a.nz) : a.n;
+}
+
+// RK3 combination of one cell (rungek_ico.f90:89-90, 153-154, 217-220)
+EMIX_DEV void rk_combine(const RkArgs &a, long q, double v[5]) {
     const long n = a.n;
     const double dt = a.dt;
-    double v[5];
-    if (a.mode == 2) {
-#pragma unroll
-        for (int m = 0; m < 5; ++m) v[m] = a.out[m * n + q];
-    } else {
     const double j11 = a.jbn[10 * n + q];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
         const double rs = j11 * a.R[m * n + q];
         const double u0 = a.um0[m * n + q];
-        if (a.stage == 1) {          // rungek_ico.f90:89-90
+        if (a.stage == 1)
             v[m] = u0 + dt * rs;
-        } else if (a.stage == 2) {   // :153-154
+        else if (a.stage == 2)
             v[m] = 0.75 * u0 + 0.25 * a.um[m * n + q] + (0.25 * dt) * rs;
-        } else {                     // :217-220
+        else
             v[m] = (1.0 / 3.0) * u0 + (2.0 / 3.0) * a.um[m * n + q] + ((2.0 / 3.0) * dt) * rs;
-        }
     }
-    if (a.mode == 1) {
-#pragma unroll
-        for (int m = 0; m < 5; ++m) a.out[m * n + q] = v[m];
-        return;
-    }
-    }
-    // varc_to_varnc + clip + mask + varc_to_varnc (:104-124)
+}
+
+// varc_to_varnc + clip + mask + varc_to_varnc (:104-124), then the rebuild
+// after the level-set call site (:127-138), of the combined values v
+EMIX_DEV void rk_convert(const RkArgs &a, long q, const double v[5]) {
+    const long n = a.n;
     const double r = v[0];
     const double rr = 1.0 / r;
     const double mk = a.mask[q];
@@ -274,7 +281,6 @@ EMIX_DEV void rk_cell(const RkArgs &a, long q) {
         uu[d] = mom * rr;
     }
     const double p = r * a.inv_m2;
-    // rebuild after the level-set call site (:127-138)
     const double r1 = p * a.mach * a.mach;
     a.out[q] = r1;
 #pragma unroll
@@ -284,6 +290,77 @@ EMIX_DEV void rk_cell(const RkArgs &a, long q) {
     }
     a.out[4 * n + q] = v[4];
     a.pres[q] = p;
+}
+
+// Values after frontera_z_val (src/MSVSingle/frontera_z.f90:231-259): z = 0
+// copies z = 1 with um(4) = 0; z = nz-2, nz-1 take um(1) = 1, um(4) = 0 and
+// the rest from z = nz-3.
+EMIX_DEV void wall_z(const RkArgs &a, int i, int j, int k, double v[5]) {
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int ks = k == 0 ? 1 : (k >= nz - 2 ? nz - 3 : k);
+    rk_combine(a, i + (long)nx * (j + (long)ny * ks), v);
+    if (k == 0) v[3] = 0.0;
+    else if (k >= nz - 2) { v[0] = 1.0; v[3] = 0.0; }
+}
+
+// then frontera_y_val (frontera_y.f90:231-245): y walls copy um(1), um(5)
+// from the neighbour plane, momentum 0
+EMIX_DEV void wall_y(const RkArgs &a, int i, int j, int k, double v[5]) {
+    const int ny = a.ny;
+    const bool w = j == 0 || j == ny - 1;
+    wall_z(a, i, j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j), k, v);
+    if (w) { v[1] = 0.0; v[2] = 0.0; v[3] = 0.0; }
+}
+
+// then frontera_x_val (frontera_x.f90:235-253): the same on the x walls
+EMIX_DEV void wall_x(const RkArgs &a, int i, int j, int k, double v[5]) {
+    const int nx = a.nx;
+    const bool w = i == 0 || i == nx - 1;
+    wall_y(a, i == 0 ? 1 : (i == nx - 1 ? nx - 2 : i), j, k, v);
+    if (w) { v[1] = 0.0; v[2] = 0.0; v[3] = 0.0; }
+}
+
+EMIX_DEV void rk_cell(const RkArgs &a, long q) {
+    double v[5];
+    if (!a.walls) {
+        rk_combine(a, q, v);
+        rk_convert(a, q, v);
+        return;
+    }
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    int i, j, k;
+    if (!a.faces) {
+        i = (int)(q % nx);
+        j = (int)((q / nx) % ny);
+        k = (int)(q / ((long)nx * ny));
+        if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || k == 0 || k >= nz - 2) return;
+        rk_combine(a, q, v);
+        rk_convert(a, q, v);
+        return;
+    }
+    const long pz = (long)nx * ny, py = (long)nx * (nz - 3);
+    if (q < 3 * pz) {
+        const int pl = (int)(q / pz);
+        const long r = q - pl * pz;
+        i = (int)(r % nx); j = (int)(r / nx); k = pl == 0 ? 0 : nz - 3 + pl;
+    } else if (q < 3 * pz + 2 * py) {
+        const long r0 = q - 3 * pz;
+        const int pl = (int)(r0 / py);
+        const long r = r0 - pl * py;
+        i = (int)(r % nx); k = 1 + (int)(r / nx); j = pl == 0 ? 0 : ny - 1;
+    } else {
+        const long px = (long)(ny - 2) * (nz - 3);
+        const long r0 = q - 3 * pz - 2 * py;
+        const int pl = (int)(r0 / px);
+        const long r = r0 - pl * px;
+        j = 1 + (int)(r % (ny - 2)); k = 1 + (int)(r / (ny - 2)); i = pl == 0 ? 0 : nx - 1;
+    }
+    // the wall rules read only cells no rule writes (k = 1, nz-3; j = 1,
+    // ny-2; i = 1, nx-2 after the earlier rules), recomputed here from the RK
+    // inputs, which this launch does not overwrite: it runs before the launch
+    // over the other cells, and writes only wall cells
+    wall_x(a, i, j, k, v);
+    rk_convert(a, i + (long)nx * (j + (long)ny * k), v);
 }
 
 // ---- kernels ------------------------------------------------------------------

@@ -66,7 +66,7 @@ int launch_single(const Launch &L, cudaStream_t st) {
         k_flux_all<<<cells_grid(L.flux.n), 256, 0, st>>>(L.flux);
         break;
     case LK_RK:
-        k_rk_post<<<cells_grid(L.rk.n), 256, 0, st>>>(L.rk);
+        k_rk_post<<<cells_grid(rk_count(L.rk)), 256, 0, st>>>(L.rk);
         break;
     case LK_BC:
         k_bc<<<cells_grid(bc_count(L.bc)), 256, 0, st>>>(L.bc);
@@ -94,6 +94,9 @@ struct emix_ctx {
     DerivTable T[3];
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t fgraph = nullptr;          // the filter (filtrado), when on
+    cudaGraphExec_t fgexec = nullptr;
+    long step_index = 0;
     bool static_set = false;
     int launches = 0;
     // optional per-launch timing (emix_ctx_profile): events around every launch
@@ -106,7 +109,7 @@ struct emix_ctx {
 
 static const char *kClassNames[] = {
     "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
-    "div_x", "div_y", "div_z", "rk_post"};
+    "div_x", "div_y", "div_z", "rk_post", "filter"};
 
 namespace emix {
 const std::vector<Launch> &ctx_plan(emix_ctx *c) { return c->plan; }
@@ -246,7 +249,9 @@ void build_plan(emix_ctx *c) {
                 P.push_back(deriv_launch(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, CLS_DIVX + ax));
         }
         // RK update and conversions; with walls the boundary conditions go
-        // between the RK combination and the conversions (rungek_ico.f90:98-104)
+        // between the RK combination and the conversions (rungek_ico.f90:98-104):
+        // the wall cells first, in a launch of their own that recomputes the
+        // RK values the wall rules copy, then every other cell
         {
             Launch L = make(LK_RK, CLS_RK);
             RkArgs &ra = L.rk;
@@ -254,20 +259,15 @@ void build_plan(emix_ctx *c) {
             ra.out = s == 3 ? c->um0 : c->um;
             ra.u = c->u; ra.pres = c->pres; ra.jbn = c->jbn; ra.mask = c->mask;
             ra.dt = p.dt; ra.mach = p.mach; ra.inv_m2 = inv_m2; ra.stage = s; ra.n = n;
-            ra.mode = 0;
-            if (!p.bc_walls) {
-                P.push_back(L);
-            } else {
-                L.rk.mode = 1;
-                P.push_back(L);
-                for (int axis = 2; axis >= 0; --axis) {
-                    Launch B = make(LK_BC, CLS_RK);
-                    B.bc = BcArgs{ra.out, axis, nx, ny, nz, n};
-                    P.push_back(B);
-                }
-                L.rk.mode = 2;
-                P.push_back(L);
+            ra.nx = nx; ra.ny = ny; ra.nz = nz;
+            ra.walls = p.bc_walls;
+            ra.faces = 0;
+            if (p.bc_walls) {
+                Launch F = L;
+                F.rk.faces = 1;
+                P.push_back(F);
             }
+            P.push_back(L);
         }
     }
 }
@@ -293,6 +293,8 @@ bool params_ok(const emix_params *p) {
     }
     if (p->sgs_model < EMIX_SGS_NONE || p->sgs_model > EMIX_SGS_STRUCTURE) return false;
     if (p->bc_walls != 0 && p->bc_walls != 1) return false;
+    if (p->filter_every < 0 || (p->filter_every > 0 && (p->nx < 11 || p->ny < 11 || p->nz < 11)))
+        return false;
     if (!(p->mach > 0.0) || !(p->dt > 0.0)) return false;
     if (p->level_set && (p->ls_ghost < 3 || p->ls_ghost > p->nx || p->ls_ghost > p->ny ||
                          p->ls_ghost > p->nz))
@@ -303,8 +305,39 @@ bool params_ok(const emix_params *p) {
 void drop_graph(emix_ctx *c) {
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->graph) cudaGraphDestroy(c->graph);
+    if (c->fgexec) cudaGraphExecDestroy(c->fgexec);
+    if (c->fgraph) cudaGraphDestroy(c->fgraph);
     c->gexec = nullptr;
     c->graph = nullptr;
+    c->fgexec = nullptr;
+    c->fgraph = nullptr;
+}
+
+bool filter_due(const emix_ctx *c) {
+    return c->p.filter_every > 0 && c->step_index % c->p.filter_every == 0;
+}
+
+int issue_filter(emix_ctx *c) {
+    return launch_filtrado(c->um0, c->jbn, c->p.cfilt, c->p.nx, c->p.ny, c->p.nz, c->stream);
+}
+
+// capture `issue` on the context stream into an executable graph
+template <class F>
+int capture(emix_ctx *c, F issue, cudaGraph_t *g, cudaGraphExec_t *ge) {
+    EMIX_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = issue();
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+    if (e != cudaSuccess) { set_last_error(e, "cudaStreamEndCapture", __FILE__, __LINE__); return EMIX_ERR_CUDA; }
+    e = cudaGraphInstantiate(ge, gr, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(gr);
+        set_last_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+        return EMIX_ERR_CUDA;
+    }
+    *g = gr;
+    return EMIX_OK;
 }
 
 } // namespace
@@ -326,6 +359,10 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     const int dims[3] = {p->nx, p->ny, p->nz};
     for (int a = 0; a < 3; ++a) {
         int rc = get_deriv_table(p->scheme[a], dims[a], p->h[a], &c->T[a]);
+        if (rc) { delete c; return rc; }
+    }
+    if (p->filter_every > 0) {
+        int rc = prepare_filtrado(p->cfilt, p->nx, p->ny, p->nz);
         if (rc) { delete c; return rc; }
     }
     const bool sf = p->sgs_model == EMIX_SGS_STRUCTURE;
@@ -451,29 +488,44 @@ int emix_step(emix_ctx *c, int nsteps, int use_graph) {
         set_last_message("emix_step: static fields not set (emix_ctx_set_static)");
         return EMIX_ERR_ARG;
     }
-    if (!use_graph) {
-        for (int s = 0; s < nsteps; ++s) {
+    if (use_graph && !c->gexec) {
+        int rc = capture(c, [&] { return issue_step(c); }, &c->graph, &c->gexec);
+        if (rc) { drop_graph(c); return rc; }
+    }
+    if (use_graph && c->p.filter_every > 0 && !c->fgexec) {
+        int rc = capture(c, [&] { return issue_filter(c); }, &c->fgraph, &c->fgexec);
+        if (rc) { drop_graph(c); return rc; }
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        if (use_graph) {
+            EMIX_CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+        } else {
             int rc = issue_step(c);
             if (rc) return rc;
         }
-        return EMIX_OK;
-    }
-    if (!c->gexec) {
-        EMIX_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = issue_step(c);
-        cudaGraph_t gr = nullptr;
-        cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
-        if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
-        if (e != cudaSuccess) { set_last_error(e, "cudaStreamEndCapture", __FILE__, __LINE__); return EMIX_ERR_CUDA; }
-        c->graph = gr;
-        e = cudaGraphInstantiate(&c->gexec, gr, 0);
-        if (e != cudaSuccess) {
-            drop_graph(c);
-            set_last_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
-            return EMIX_ERR_CUDA;
+        // filtrado after the step's last substep (rungek_ico.f90:269-278)
+        if (filter_due(c)) {
+            if (use_graph) {
+                EMIX_CUDA_TRY(cudaGraphLaunch(c->fgexec, c->stream));
+            } else {
+                int rc = issue_filter(c);
+                if (rc) return rc;
+            }
         }
+        ++c->step_index;
     }
-    for (int s = 0; s < nsteps; ++s) EMIX_CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+    return EMIX_OK;
+}
+
+int emix_ctx_get_step_index(emix_ctx *c, long *index) {
+    if (!c || !index) return EMIX_ERR_ARG;
+    *index = c->step_index;
+    return EMIX_OK;
+}
+
+int emix_ctx_set_step_index(emix_ctx *c, long index) {
+    if (!c || index < 0) return EMIX_ERR_ARG;
+    c->step_index = index;
     return EMIX_OK;
 }
 
@@ -516,8 +568,13 @@ int emix_ctx_profile(emix_ctx *c, int nsteps, double *ms, int *launches) {
         c->prof = true;
         c->prof_n = 0;
         int rc = issue_step(c);
+        if (!rc && filter_due(c)) {
+            ProfScope ps(c, CLS_FILTER);
+            rc = issue_filter(c);
+        }
         c->prof = false;
         if (rc) return rc;
+        ++c->step_index;
         EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
         for (int q = 0; q < c->prof_n; ++q) {
             float t = 0.f;

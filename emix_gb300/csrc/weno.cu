@@ -16,7 +16,7 @@ __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict
         const double c[3] = {jbn[q] * sx, jbn[4 * n + q] * sy, jbn[8 * n + q] * sz};
         for (int d = 0; d < 3; ++d) {
             wc[d * n + q] = c[d];
-            we[d * n + q] = 12.0e-6 / (c[d] * c[d]);
+            we[d * n + q] = kWenoEps4 / (c[d] * c[d]);
         }
     }
 }

@@ -61,7 +61,7 @@ __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict
 
 int launch_weno_stage(const WenoArgs &a, cudaStream_t st);
 
-// C_d = jbn_d / h_d and E_d = 12e-6 / C_d^2 for the precomputed-scale path
+// C_d = jbn_d / h_d and E_d = kWenoEps4 / C_d^2 for the precomputed-scale path
 __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
                               double *__restrict__ we, double sx, double sy, double sz, long n);
 
@@ -90,33 +90,37 @@ EMIX_DEV double rcp_newton(double d) {
 
 // Jiang-Peng WENO5 reconstruction from five differences (Phi_x_WENO,
 // src/LevelSet/lsTools.cu:9-50).  Same weights 0.1/0.6/0.3 and
-// epsilon = 1e-6 on (beta + eps)^2; rearranged to one reciprocal:
-//   12*beta_k = 13 d_k^2 + 3 e_k^2,  alpha_k ~ c_k / (12 beta_k + 12 eps)^2,
-//   result = sum(w_k q_k) / (6 sum w_k),  w_1 = 0.1 t_2 t_3, ...
-// eps12 is 12*epsilon for differences already scaled by the metric, or
-// 12*epsilon/C^2 for unscaled differences (WENO(C v; eps) = C WENO(v; eps/C^2)).
-EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5, double eps12) {
+// epsilon = 1e-6 on (beta + eps)^2, rearranged to cut FP64 operations:
+//   with d_k, e_k the second and first differences of candidate stencil k,
+//   4 beta_k = (13/3) d_k^2 + e_k^2, so alpha_k ~ c_k / (4 beta_k + 4 eps)^2;
+//   the three candidate values are v3 + r_k / 12 with r_1 = d_1 + 3 e_1,
+//   r_2 = d_2 - 3 e_2, r_3 = d_3 - 3 e_3, so the result is
+//   v3 + sum(w_k r_k) / (12 sum w_k), with w_1 = t_2 t_3, w_2 = 6 t_1 t_3,
+//   w_3 = 3 t_1 t_2 (the weights times t_1 t_2 t_3 / 0.1); one reciprocal.
+// eps4 is 4*epsilon for differences already scaled by the metric, or
+// 4*epsilon/C^2 for unscaled differences (WENO(C v; eps) = C WENO(v; eps/C^2)).
+constexpr double kWenoEps4 = 4.0e-6;
+
+EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5, double eps4) {
+    constexpr double c13 = 13.0 / 3.0;
     const double d1 = fma(-2.0, v2, v1 + v3);
     const double e1 = fma(-4.0, v2, fma(3.0, v3, v1));
     const double d2 = fma(-2.0, v3, v2 + v4);
     const double e2 = v2 - v4;
     const double d3 = fma(-2.0, v4, v3 + v5);
     const double e3 = fma(-4.0, v4, fma(3.0, v3, v5));
-    const double s1 = fma(13.0 * d1, d1, (3.0 * e1) * e1);
-    const double s2 = fma(13.0 * d2, d2, (3.0 * e2) * e2);
-    const double s3 = fma(13.0 * d3, d3, (3.0 * e3) * e3);
-    double t1 = s1 + eps12; t1 *= t1;
-    double t2 = s2 + eps12; t2 *= t2;
-    double t3 = s3 + eps12; t3 *= t3;
-    const double w1 = (0.1 * t2) * t3;
-    const double w2 = (0.6 * t1) * t3;
-    const double w3 = (0.3 * t1) * t2;
-    const double q1 = fma(11.0, v3, fma(-7.0, v2, 2.0 * v1));
-    const double q2 = fma(2.0, v4, fma(5.0, v3, -v2));
-    const double q3 = fma(5.0, v4, fma(2.0, v3, -v5));
-    const double num = fma(w1, q1, fma(w2, q2, w3 * q3));
-    const double den = 6.0 * (w1 + w2 + w3);
-    return num * rcp_newton(den);
+    double t1 = fma(c13 * d1, d1, e1 * e1) + eps4; t1 *= t1;
+    double t2 = fma(c13 * d2, d2, e2 * e2) + eps4; t2 *= t2;
+    double t3 = fma(c13 * d3, d3, e3 * e3) + eps4; t3 *= t3;
+    const double w1 = t2 * t3;
+    const double w2 = (6.0 * t1) * t3;
+    const double w3 = (3.0 * t1) * t2;
+    const double r1 = fma(3.0, e1, d1);
+    const double r2 = fma(-3.0, e2, d2);
+    const double r3 = fma(-3.0, e3, d3);
+    const double num = fma(w1, r1, fma(w2, r2, w3 * r3));
+    const double den = 12.0 * (w1 + w2 + w3);
+    return fma(num, rcp_newton(den), v3);
 }
 
 // Positions (0..n-1) of the five differences for the left-biased (u >= 0)
@@ -243,7 +247,7 @@ EMIX_DEV void weno_stage_body(const WenoArgs &a, uint3 bid, uint3 tid3) {
     } else {
         cx = a.jbn[iv] * a.sx; cy = a.jbn[4 * nv + iv] * a.sy; cz = a.jbn[8 * nv + iv] * a.sz;
         mx = 1.0; my = 1.0; mz = 1.0;
-        ex = 12.0e-6; ey = 12.0e-6; ez = 12.0e-6;
+        ex = kWenoEps4; ey = kWenoEps4; ez = kWenoEps4;
     }
 
     int p[5];

@@ -223,6 +223,24 @@ def weno5_advect_dev(phi, vel, jbn, h, dt, ref_bugs=0):
     return phi
 
 
+def filtrado_dev(um, jbn, cfilt):
+    """filtrado (x, y, z compact filter of the 5 fields) in place on device tensors."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(um)
+    check(lib.emix_filtrado_dev(_ptr(um), _ptr(jbn), cfilt, nx, ny, nz, _stream()), "emix_filtrado_dev")
+    return um
+
+
+def filter_dev(f, jbn, cfilt, axis, zrows=0):
+    """One filter pass along `axis` over the fields of f (3-D or stacked 4-D), in place."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(f)
+    nf = 1 if f.dim() == 3 else f.shape[0]
+    check(lib.emix_filter_dev(_ptr(f), nf, _ptr(jbn), cfilt, axis, zrows, nx, ny, nz, _stream()),
+          "emix_filter_dev")
+    return f
+
+
 def advect_extrapolate_dev(press, jbn, sobject, delta, deltamin):
     """advect_CUDA on device tensors, in place on press."""
     lib = _lib.load()
@@ -328,26 +346,10 @@ class Context:
     """One grid resident in device memory; wraps ``emix_ctx``."""
 
     def __init__(self, workload=None, *, params: EmixParams | None = None, level_set=True,
-                 ref_bugs=0, ls_ghost=5, bc_walls=0):
+                 ref_bugs=0, ls_ghost=5, bc_walls=0, filter_every=0, cfilt=0.0):
         lib = _lib.load()
         if params is None:
-            w = workload
-            g = w.grid
-            params = EmixParams()
-            params.nx, params.ny, params.nz = g.nx, g.ny, g.nz
-            for a in range(3):
-                params.scheme[a] = w.schemes[a]
-                params.h[a] = g.h(a)
-            params.sgs_model = w.sgs_model
-            params.cs = w.cs
-            params.amu0 = w.amu0
-            params.c4 = 1.0 / w.reynolds
-            params.mach = w.mach
-            params.dt = w.dt
-            params.level_set = 1 if level_set else 0
-            params.ls_ghost = ls_ghost
-            params.ref_bugs = ref_bugs
-            params.bc_walls = bc_walls
+            params = _params_of(workload, level_set, ref_bugs, ls_ghost, bc_walls, filter_every, cfilt)
         self.params = params
         self._h = C.c_void_p()
         check(lib.emix_ctx_create(C.byref(params), C.byref(self._h)), "emix_ctx_create")
@@ -390,6 +392,16 @@ class Context:
     def step(self, nsteps=1, use_graph=False):
         check(self.lib.emix_step(self._h, nsteps, 1 if use_graph else 0), "emix_step")
 
+    @property
+    def step_index(self) -> int:
+        v = C.c_long()
+        check(self.lib.emix_ctx_get_step_index(self._h, C.byref(v)), "emix_ctx_get_step_index")
+        return v.value
+
+    @step_index.setter
+    def step_index(self, index: int):
+        check(self.lib.emix_ctx_set_step_index(self._h, int(index)), "emix_ctx_set_step_index")
+
     def step_host(self, um, phi, nsteps=1):
         check(self.lib.emix_step_host(self._h, _ptr(um), _ptr(phi), nsteps), "emix_step_host")
 
@@ -420,7 +432,8 @@ class Context:
             pass
 
 
-def _params_of(w, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0) -> EmixParams:
+def _params_of(w, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0, filter_every=0,
+               cfilt=0.0) -> EmixParams:
     g = w.grid
     p = EmixParams()
     p.nx, p.ny, p.nz = g.nx, g.ny, g.nz
@@ -437,6 +450,8 @@ def _params_of(w, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0) -> EmixPar
     p.ls_ghost = ls_ghost
     p.ref_bugs = ref_bugs
     p.bc_walls = bc_walls
+    p.filter_every = filter_every
+    p.cfilt = cfilt
     return p
 
 

@@ -17,13 +17,14 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--no-level-set", action="store_true")
+    ap.add_argument("--walls", action="store_true", help="frontera wall conditions every substep")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
     from . import fields as F
     from . import ops
     w = F.stirred_tank(n=a.n) if a.workload == "tank" else F.taylor_green(n=a.n)
-    ctx = ops.Context(w, level_set=not a.no_level_set)
+    ctx = ops.Context(w, level_set=not a.no_level_set, bc_walls=int(a.walls))
     t0 = time.perf_counter()
     ctx.step(a.steps, use_graph=a.graph)
     torch.cuda.synchronize()

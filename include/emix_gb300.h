@@ -218,6 +218,24 @@ int emix_extrapolate_dev(double *ext, const double *phiS, const double *jbn,
                          void *stream);
 
 /* ========================================================================
+ * Compact filter
+ * ======================================================================== */
+
+/* filtrado as RUNGEK calls it (itf = 1: x, then y, then z;
+ * src/MSVSingle/herramientas_incomp2.f90:227-410), with filtronper
+ * (src/MSVSingle/filtro_incomp.f90:307-362) on every pencil: each pencil of
+ * um[0..4] is scaled by jbn(10), filtered, scaled by jbn(11).  z uses the
+ * periodic row arrays, as filtrado passes them.  In place, device pointers,
+ * every dimension >= 11. */
+int emix_filtrado_dev(double *um, const double *jbn, double cfilt,
+                      int nx, int ny, int nz, void *stream);
+
+/* One filter pass along `axis` over nf fields in place; zrows = 1 selects the
+ * periodic rows (a = c = cfilt on every row), 0 the non-periodic ones. */
+int emix_filter_dev(double *f, int nf, const double *jbn, double cfilt, int axis, int zrows,
+                    int nx, int ny, int nz, void *stream);
+
+/* ========================================================================
  * Boundary conditions, time step and metrics
  * ======================================================================== */
 
@@ -262,6 +280,10 @@ typedef struct emix_params {
     int ls_ghost;       /* ghost layers of the level-set grid (5 in the reference) */
     int ref_bugs;       /* 1: keep the reference's z-top WENO neighbour index      */
     int bc_walls;       /* 1: apply frontera_z/y/x_val after each RK combination   */
+    int filter_every;   /* > 0: compact filter (filtrado) after every filter_every-th
+                           step, counting from the first (9 in the reference,
+                           solver/rungek_ico.f90:269-276); 0: off               */
+    double cfilt;       /* filter parameter alpha (cfilt of data.in)              */
 } emix_params;
 
 typedef struct emix_ctx emix_ctx;
@@ -287,8 +309,14 @@ int emix_ctx_download(emix_ctx *ctx, double *um, double *phi);
 int emix_ctx_state(emix_ctx *ctx, double **um, double **phi);
 
 /* Advance nsteps RK3 steps on the device, asynchronously on the context
- * stream.  use_graph = 1 replays a captured CUDA graph of one step. */
+ * stream.  use_graph = 1 replays a captured CUDA graph of one step (and one
+ * of the filter, when it is on). */
 int emix_step(emix_ctx *ctx, int nsteps, int use_graph);
+
+/* Steps taken by the context so far (starts at 0; the filter runs after the
+ * steps whose index is a multiple of filter_every).  Settable for restarts. */
+int emix_ctx_get_step_index(emix_ctx *ctx, long *index);
+int emix_ctx_set_step_index(emix_ctx *ctx, long index);
 
 /* End-to-end form: copy um/phi from host, advance nsteps, copy back;
  * synchronous. */

@@ -832,6 +832,88 @@ int orc_advect_extrapolate(double *press, const double *jbn, const double *sobje
     return 0;
 }
 
+/* inifiltro (src/MSVSingle/filtro_incomp.f90:1-162): the tridiagonal rows of
+ * the compact filter for a pencil of n points.  b = 1; with zrows = 0 the
+ * non-periodic rows (a = c = cfilt for 1-based rows 6..n-5, 0 elsewhere:
+ * cfilt2..cfilt5 are 0 in both branches of :17-31), with zrows = 1 the
+ * periodic rows (a = c = cfilt everywhere), which filtrado passes for z. */
+static void filter_rows(int n, double cfilt, int zrows, double *a, double *b, double *c) {
+    for (int l = 0; l < n; ++l) {
+        b[l] = 1.0;
+        const bool in = zrows || (l >= 5 && l <= n - 6);
+        a[l] = in ? cfilt : 0.0;
+        c[l] = in ? cfilt : 0.0;
+    }
+}
+
+int orc_filtronper(int n, double *u, double cfilt, int zrows) {
+    /* filtronper (src/MSVSingle/filtro_incomp.f90:307-362) with the
+     * right-hand-side constants of inifiltro (:140-145) */
+    if (n < 11) return 1;
+    const double arsf = (193. + 126. * cfilt) / 256., brsf = (105. + 302. * cfilt) / 256.,
+                 crsf = (-15. + 30. * cfilt) / 64., drsf = (45. - 90. * cfilt) / 512.,
+                 ersf = (-5. + 10. * cfilt) / 256., frsf = (1. - 2 * cfilt) / 512.;
+    std::vector<double> a(n), b(n), c(n), r(n), gam(n);
+    filter_rows(n, cfilt, zrows, a.data(), b.data(), c.data());
+    for (int l = 5; l <= n - 6; ++l)
+        r[l] = 0.5 * (arsf * (u[l] + u[l]) + brsf * (u[l + 1] + u[l - 1]) + crsf * (u[l + 2] + u[l - 2]) +
+                      drsf * (u[l + 3] + u[l - 3]) + ersf * (u[l + 4] + u[l - 4]) +
+                      frsf * (u[l + 5] + u[l - 5]));
+    for (int l = 0; l < 5; ++l) {   /* SIN FILTRO rows (:336-345) */
+        r[l] = u[l];
+        r[n - 1 - l] = u[n - 1 - l];
+    }
+    double bet = b[0];
+    u[0] = r[0] / bet;
+    for (int l = 1; l < n; ++l) {
+        gam[l] = c[l - 1] / bet;
+        bet = b[l] - a[l] * gam[l];
+        u[l] = (r[l] - a[l] * u[l - 1]) / bet;
+    }
+    for (int l = n - 2; l >= 0; --l) u[l] = u[l] - gam[l + 1] * u[l + 1];
+    return 0;
+}
+
+int orc_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, int nz) {
+    /* filtrado with itf = 1, the only value it is called with
+     * (solver/rungek_ico.f90:269-276; src/MSVSingle/herramientas_incomp2.f90:
+     * 227-410): for each of the 5 equations, x then y then z, each pencil
+     * scaled by jbn(10) before and by jbn(11) after; z with the periodic rows
+     * azpf/bzpf/czpf (:281-289, 361-371). */
+    if (nx < 11 || ny < 11 || nz < 11) return 1;
+    const size_t n = (size_t)nx * ny * nz;
+    const double *J10 = jbn + 9 * n, *J11 = jbn + 10 * n;
+    for (int m = 0; m < 5; ++m) {
+        double *f = um + (size_t)m * n;
+#pragma omp parallel
+        {
+            std::vector<double> du(nx), dv(ny), dw(nz);
+#pragma omp for schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j) {
+                    for (int i = 0; i < nx; ++i) du[i] = f[lin(i, j, k, nx, ny)] * J10[lin(i, j, k, nx, ny)];
+                    orc_filtronper(nx, du.data(), cfilt, 0);
+                    for (int i = 0; i < nx; ++i) f[lin(i, j, k, nx, ny)] = du[i] * J11[lin(i, j, k, nx, ny)];
+                }
+#pragma omp for schedule(static)
+            for (int k = 0; k < nz; ++k)
+                for (int i = 0; i < nx; ++i) {
+                    for (int j = 0; j < ny; ++j) dv[j] = f[lin(i, j, k, nx, ny)] * J10[lin(i, j, k, nx, ny)];
+                    orc_filtronper(ny, dv.data(), cfilt, 0);
+                    for (int j = 0; j < ny; ++j) f[lin(i, j, k, nx, ny)] = dv[j] * J11[lin(i, j, k, nx, ny)];
+                }
+#pragma omp for schedule(static)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    for (int k = 0; k < nz; ++k) dw[k] = f[lin(i, j, k, nx, ny)] * J10[lin(i, j, k, nx, ny)];
+                    orc_filtronper(nz, dw.data(), cfilt, 1);
+                    for (int k = 0; k < nz; ++k) f[lin(i, j, k, nx, ny)] = dw[k] * J11[lin(i, j, k, nx, ny)];
+                }
+        }
+    }
+    return 0;
+}
+
 int orc_bc_walls(double *um, int nx, int ny, int nz) {
     const size_t n = (size_t)nx * ny * nz;
     double *U[5] = {um, um + n, um + 2 * n, um + 3 * n, um + 4 * n};
@@ -1047,6 +1129,10 @@ int orc_step(const orc_step_params *p, double *um0, double *phi,
         }
         std::memcpy(um.data(), um1.data(), 5 * n * sizeof(double));
     }
+    /* the compact filter every filter_every-th step, counting from the first
+     * (itf = 1, 10, 19, ...: rungek_ico.f90:269-276) */
+    if (p->filter_every > 0 && p->step_index % p->filter_every == 0)
+        if (orc_filtrado(um1.data(), jbn, p->cfilt, nx, ny, nz)) return 1;
     std::memcpy(um0, um1.data(), 5 * n * sizeof(double));   /* rungek_ico.f90:278 */
     return 0;
 }

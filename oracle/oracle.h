@@ -116,6 +116,9 @@ typedef struct {
     int ls_ghost;         /* ghost layers for the level set (5 in the reference) */
     int ref_bugs;         /* 1: reproduce the reference's z-top WENO index */
     int bc_walls;         /* 1: frontera_z/y/x_val after each RK combination */
+    int filter_every;     /* > 0: filtrado at the end of steps with step_index % filter_every == 0 (9 in the reference) */
+    double cfilt;         /* filter parameter alpha (cfilt of data.in) */
+    long step_index;      /* steps taken before this one */
 } orc_step_params;
 
 /* One RK3 step.  State in/out: um (5 fields) and phi (1 field, may be NULL
@@ -152,6 +155,15 @@ int orc_extrapolation(double *ext, const double *phiS, const double *j0, const d
 int orc_advect_extrapolate(double *press, const double *jbn, const double *sobject,
                            double deltaX, double deltaY, double deltaZ, int nx, int ny, int nz,
                            double deltamin);
+
+/* filtronper (src/MSVSingle/filtro_incomp.f90:307-362) on one pencil, in
+ * place, with the rows of inifiltro for cfilt (zrows = 1: the periodic rows
+ * that filtrado passes for z). */
+int orc_filtronper(int n, double *u, double cfilt, int zrows);
+
+/* filtrado as RUNGEK calls it (itf = 1; herramientas_incomp2.f90:227-410) on
+ * um[5] in place. */
+int orc_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, int nz);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

@@ -27,7 +27,8 @@ class StepParams(C.Structure):
         ("sgs_model", C.c_int), ("cs", C.c_double), ("amu0", C.c_double), ("c4", C.c_double),
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
-        ("bc_walls", C.c_int),
+        ("bc_walls", C.c_int), ("filter_every", C.c_int), ("cfilt", C.c_double),
+        ("step_index", C.c_long),
     ]
 
 
@@ -73,6 +74,8 @@ def load():
                               C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int],
         "orc_advect_extrapolate": [vp, vp, vp, C.c_double, C.c_double, C.c_double,
                                    C.c_int, C.c_int, C.c_int, C.c_double],
+        "orc_filtronper": [C.c_int, vp, C.c_double, C.c_int],
+        "orc_filtrado": [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int],
         "orc_set_threads": [C.c_int],
         "orc_get_threads": [],
     }
@@ -264,7 +267,21 @@ def jacobeano(xyz, scheme, h):
     return jbn
 
 
-def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0):
+def filtronper(u, cfilt, zrows=0):
+    u = np.array(u, dtype=np.float64, copy=True)
+    _ok(load().orc_filtronper(len(u), _p(u), cfilt, zrows), "orc_filtronper")
+    return u
+
+
+def filtrado(um, jbn, cfilt):
+    um = np.array(um, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(um)
+    _ok(load().orc_filtrado(_p(um), _p(np.ascontiguousarray(jbn)), cfilt, nx, ny, nz), "orc_filtrado")
+    return um
+
+
+def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0, filter_every=0,
+                cfilt=0.0):
     w = workload
     p = StepParams()
     p.nx, p.ny, p.nz = w.grid.nx, w.grid.ny, w.grid.nz
@@ -281,6 +298,9 @@ def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0):
     p.ls_ghost = ls_ghost
     p.ref_bugs = ref_bugs
     p.bc_walls = bc_walls
+    p.filter_every = filter_every
+    p.cfilt = cfilt
+    p.step_index = 0
     return p
 
 
@@ -288,7 +308,8 @@ def step(params: StepParams, um, phi, jbn, mask, dxyz, ratios=None, nsteps=1):
     um = np.array(um, dtype=np.float64, copy=True)
     phi = None if phi is None else np.array(phi, dtype=np.float64, copy=True)
     lib = load()
-    for _ in range(nsteps):
+    for it in range(nsteps):
+        params.step_index = it
         _ok(lib.orc_step(C.byref(params), _p(um), _p(phi), _p(np.ascontiguousarray(jbn)),
                          _p(np.ascontiguousarray(mask)), _p(np.ascontiguousarray(dxyz)),
                          _p(None if ratios is None else np.ascontiguousarray(ratios))),
