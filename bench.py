@@ -32,7 +32,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 N_GRID = 256
-SAMPLE_N = 96            # CPU sample grid (same generator, fewer cells)
+SAMPLE_N = 128            # CPU sample grid (same generator, fewer cells)
 G = 5                    # level-set ghost layers
 
 
@@ -87,17 +87,23 @@ def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1, dims=None, g: in
     return 0.0
 
 
-# FP64 lane operations per cell of each kernel class (per launch), counted
-# from the kernel source (adds, multiplies and FMAs; a divide or square root
-# counted as the 8 operations of its refinement sequence).
 # wall boundary conditions of the tank (frontera_z/y/x_val) in every substep
 WALLS = 1
+# the impeller as a rotating volumetric forcing (rushton(sub_step)) in every substep
+IMPELLER = True
 
+# FP64 operations (dfma + dadd + dmul thread instructions) per cell a launch
+# covers, measured with ncu on the 192^3 tank (profiles/step_kernels_full_
+# stirred_tank_192.txt, profiles/weno_stage_stirred_tank_192.txt).
 FP64_OPS_PER_CELL = {
-    "weno_stage": 3 * 62 + 8, "grad_x": 3 * 6, "grad_y": 3 * 6, "grad_z": 3 * 6,
-    "div_x": 5 * 6, "div_y": 5 * 7, "div_z": 5 * 7, "flux": 55, "sgs": 32,
-    "rk_post": 45, "prim": 12, "ghost_pad": 0,
+    "weno_stage": 150.2, "grad_x": 18.0, "grad_y": 18.0, "grad_z": 18.0,
+    "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 45.0, "sgs": 31.0,
+    "rk_post": 31.9,
 }
+
+# DRAM bytes (read + write) per cell a launch covers, from the same ncu
+# captures; the bench scales them to the 256^3 launch by its cells.
+DRAM_BYTES_PER_CELL = {"weno_stage": 87.5}
 
 
 class ClockSampler:
@@ -166,7 +172,7 @@ def cpu_sample(steps: int, warmup: int):
     tank, all host threads.  Returns (Mcell-steps/s, seconds, threads)."""
     from emix_gb300 import fields as F
     from oracle import oracle_py as O
-    w = F.stirred_tank(n=SAMPLE_N)
+    w = F.stirred_tank(n=SAMPLE_N, impeller=IMPELLER)
     p = O.step_params(w, bc_walls=WALLS)
     d, r = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
     um, phi = w.um, w.phi
@@ -248,6 +254,39 @@ def ensemble_leg(steps: int, warmup: int, stream=None):
     }
 
 
+def large_leg(steps: int, warmup: int, stream=None):
+    """The 512 x 512 x 384 tank (same generator and settings as the headline
+    workload): device-resident graph-replayed steps and the context's device
+    footprint.  Returns a dict for the JSON line."""
+    import torch
+    from emix_gb300 import fields as F
+    from emix_gb300 import ops
+    w = F.stirred_tank(n=512, nz=384, impeller=IMPELLER)
+    ctx = ops.Context(w, level_set=True, ls_ghost=G, bc_walls=WALLS)
+    s = stream or torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    ctx.step(warmup, use_graph=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    ctx.step(steps, use_graph=True)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    n = w.grid.nx * w.grid.ny * w.grid.nz
+    um, phi = ctx.download()
+    ok = bool(np.isfinite(um).all() and np.isfinite(phi).all())
+    dev_bytes = ctx.device_bytes()
+    ctx.close()
+    return {
+        "workload": "stirred tank 512x512x384 walls, RK3 step with WENO5 level set",
+        "cells": n, "steps": steps, "value": round(n / (ms * 1e-3) / 1e6, 3),
+        "unit": "Mcell-RK3-steps/s", "ms_per_step": round(ms, 3),
+        "device_gib": round(dev_bytes / 2**30, 2), "finite": ok,
+    }
+
+
 def config_dict(w):
     return {
         "workload": f"stirred tank {N_GRID}^3 walls, RK3 step with WENO5 level set",
@@ -255,6 +294,8 @@ def config_dict(w):
         "scheme": "Lele-6 compact, 3rd/4th-order closures (derivada_incomp.f90)",
         "sgs": "Smagorinsky Cs=0.1", "level_set": "WENO5 TVD stage per substep",
         "walls": "frontera_z/y/x_val after every RK combination" if WALLS else "none",
+        "impeller": ("6-blade rotating forcing at z=H/3, blade radius 0.33R, height 0.05H, "
+                     "omega=1" if IMPELLER else "static mask"),
         "cfl": 0.3, "dt": None if w is None else w.dt, "precision": "fp64",
         "l2": "inputs larger than L2 (9 GB resident, 128 MiB per field)",
         "parallelism": "replicas (one independent grid per GPU)",
@@ -269,6 +310,7 @@ def main():
     ap.add_argument("--impl", default="emix", choices=["emix", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 512x512x384 leg")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -295,7 +337,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    w = F.stirred_tank(n=N_GRID)
+    w = F.stirred_tank(n=N_GRID, impeller=IMPELLER)
     n = w.grid.ncell
     ng = (N_GRID + 2 * G) ** 3
     ctx = ops.Context(w, level_set=True, ls_ghost=G, bc_walls=WALLS)
@@ -356,10 +398,9 @@ def main():
     cells_top = cells_per_launch(top, (N_GRID,) * 3, G)
     fp64_ach = FP64_OPS_PER_CELL.get(top, 0) * cells_top / (top_ms * 1e-3)
     achieved = ab / (top_ms * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get(top)
+    traffic = DRAM_BYTES_PER_CELL.get(top)
+    if traffic is not None:
+        traffic = round(traffic * cells_top)
     roofline = {
         "kernel": top, "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak,
         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
@@ -385,13 +426,16 @@ def main():
         "kernels": kernels,
         "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
     }
-    if not args.no_ensemble:
+    # the side workloads run at N = 1 only (the scaling runs time the headline step)
+    if world == 1 and not args.no_ensemble:
         line["ensemble"] = ensemble_leg(min(args.steps, 10), 3, stream)
+    if world == 1 and not args.no_large:
+        line["large"] = large_leg(min(args.steps, 5), 3, stream)
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, sec, thr = cpu_sample(2, 1)
+        v, sec, thr = cpu_sample(16, 1)
         line["cpu_baseline"] = {
             "value": round(v, 4), "unit": "Mcell-RK3-steps/s", "cores": thr, "kind": "port",
-            "sample": f"2 RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator), CPU "
+            "sample": f"16 RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator), CPU "
                       f"restatement of the reference algorithm, {sec:.1f} s, {thr} threads"}
     if rank == 0:
         print(json.dumps(line), flush=True)

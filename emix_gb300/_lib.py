@@ -26,6 +26,16 @@ class EmixError(RuntimeError):
         self.rc = rc
 
 
+class EmixImpeller(C.Structure):
+    _fields_ = [
+        ("on", C.c_int), ("nblades", C.c_int), ("omega", C.c_double), ("theta0", C.c_double),
+        ("r1", C.c_double), ("r2", C.c_double), ("z1", C.c_double), ("z2", C.c_double),
+        ("half_thick", C.c_double), ("hub_r", C.c_double), ("hub_z1", C.c_double),
+        ("hub_z2", C.c_double), ("shaft_r", C.c_double), ("shaft_z0", C.c_double),
+        ("shaft_z1", C.c_double),
+    ]
+
+
 class EmixParams(C.Structure):
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
@@ -36,6 +46,7 @@ class EmixParams(C.Structure):
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
         ("bc_walls", C.c_int), ("filter_every", C.c_int), ("cfilt", C.c_double),
+        ("imp", EmixImpeller), ("t0", C.c_double),
     ]
 
 
@@ -61,6 +72,10 @@ PROTOTYPES = {
                                [C.c_int] * 3 + [vp]),
     "emix_weno5_advect_dev": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4 + [vp]),
     "emix_weno5_advect": (C.c_int, [vp, vp, vp] + [C.c_double] * 4 + [C.c_int] * 4),
+    "emix_impeller_force_dev": (C.c_int, [vp, vp, C.POINTER(EmixImpeller), C.c_double, C.c_int,
+                                          C.c_int, C.c_int, vp, vp]),
+    "emix_deriv_t_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int,
+                                   C.c_int, C.c_int, vp]),
     "emix_filtrado_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
     "emix_filter_dev": (C.c_int, [vp, C.c_int, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_int, vp]),
@@ -85,6 +100,8 @@ PROTOTYPES = {
     "emix_step": (C.c_int, [vp, C.c_int, C.c_int]),
     "emix_ctx_get_step_index": (C.c_int, [vp, C.POINTER(C.c_long)]),
     "emix_ctx_set_step_index": (C.c_int, [vp, C.c_long]),
+    "emix_ctx_set_time": (C.c_int, [vp, C.c_double]),
+    "emix_ctx_get_time": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "emix_step_host": (C.c_int, [vp, vp, vp, C.c_int]),
     "emix_ctx_launches_per_step": (C.c_int, [vp]),
     "emix_ctx_device_bytes": (C.c_longlong, [vp]),

@@ -1,0 +1,123 @@
+// adjoint_deriv.cu -- D^T, the transpose of the compact first derivative
+// D = (1/h) A^{-1} B of every scheme: D^T = (1/h) B^T A^{-T}.
+//
+// One thread per pencil (lanes along x for the y and z pencils; along y for
+// the x pencils, whose lines stay in L1 across the walk).  Forward sweep of
+// A^T into the scratch w, backward sweep with a 7-value register window of z
+// from which out_j = sum_k B^T[j][k] z_{j+k-3} is finished as soon as its last
+// z is known.  The cyclic scheme is anti-self-adjoint (D^T = -D) and uses the
+// forward kernels with a negated table.
+#include "adjoint.cuh"
+
+namespace emix {
+
+namespace {
+
+template <int ACC>
+__global__ void __launch_bounds__(128) k_deriv_t(DerivTTable T, PencilFields F, int axis, int nx,
+                                                 int ny, int nz) {
+    const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long base, s;
+    int L;
+    if (axis == 0) {
+        if (p >= (long)ny * nz) return;
+        base = p * nx; s = 1; L = nx;
+    } else if (axis == 1) {
+        if (p >= (long)nx * nz) return;
+        base = (p % nx) + (p / nx) * (long)nx * ny; s = nx; L = ny;
+    } else {
+        if (p >= (long)nx * ny) return;
+        base = p; s = (long)nx * ny; L = nz;
+    }
+    const int f = blockIdx.y;
+    const double *in = pick(F.in, f) + base;
+    double *w = pick(F.w, f) + base;
+    double *out = pick(F.out, f) + base;
+    const DerivTRow *R = T.rows;
+    const double *BT = T.bt;
+    // forward: y_i = r_i ib_i - m_i y_{i-1}
+    double y = 0.0;
+    for (int i = 0; i < L; ++i) {
+        const DerivTRow r = R[i];
+        y = fma(-r.m, y, in[i * s] * r.ib);
+        w[i * s] = y;
+    }
+    // backward: z_i = y_i - g_i z_{i+1}; zq[t] = z_{i+t}
+    double zq[7];
+#pragma unroll
+    for (int t = 0; t < 7; ++t) zq[t] = 0.0;
+    double z = 0.0;
+    for (int i = L - 1; i >= -3; --i) {
+#pragma unroll
+        for (int t = 6; t > 0; --t) zq[t] = zq[t - 1];
+        if (i >= 0) {
+            z = (i == L - 1) ? w[i * s] : fma(-R[i].g, z, w[i * s]);
+            zq[0] = z;
+        } else {
+            zq[0] = 0.0;
+        }
+        const int j = i + 3;
+        if (j < L) {
+            const double *b = BT + 7 * (long)j;
+            double o = b[0] * zq[0];
+#pragma unroll
+            for (int t = 1; t < 7; ++t) o = fma(b[t], zq[t], o);
+            if (ACC) out[j * s] += o;
+            else out[j * s] = o;
+        }
+    }
+}
+
+} // namespace
+
+int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double *const *in,
+                   double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st) {
+    if (nf < 1 || nf > kMaxFields || axis < 0 || axis > 2) return EMIX_ERR_ARG;
+    if (T.periodic) {
+        if (!acc) return launch_deriv(T.neg, axis, EPI_STORE, nf, in, w, out, nx, ny, nz, st);
+        return launch_deriv(T.neg, axis, EPI_ACCUM, nf, in, w, out, nx, ny, nz, st);
+    }
+    PencilFields F{};
+    for (int f = 0; f < nf; ++f) {
+        F.in[f] = in[f];
+        F.w[f] = w[f];
+        F.out[f] = out[f];
+    }
+    const long np = axis == 0 ? (long)ny * nz : (axis == 1 ? (long)nx * nz : (long)nx * ny);
+    dim3 grid((unsigned)((np + 127) / 128), nf);
+    if (acc) k_deriv_t<1><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
+    else k_deriv_t<0><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
+
+} // namespace emix
+
+using namespace emix;
+
+extern "C" {
+
+int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                     int nx, int ny, int nz, int accumulate, void *stream) {
+    const int dims[3] = {nx, ny, nz};
+    if (axis < 0 || axis > 2 || nf < 1 || nf > kMaxFields || !out || !in || !(h > 0) || nx < 1 ||
+        ny < 1 || nz < 1 || (accumulate != 0 && accumulate != 1))
+        return EMIX_ERR_ARG;
+    DerivTTable T;
+    int rc = get_deriv_t_table(scheme, dims[axis], h, &T);
+    if (rc) return rc;
+    const long n = (long)nx * ny * nz;
+    double *scr;
+    rc = device_scratch((size_t)nf * n * sizeof(double), &scr);
+    if (rc) return rc;
+    const double *ins[kMaxFields];
+    double *ws[kMaxFields], *outs[kMaxFields];
+    for (int f = 0; f < nf; ++f) {
+        ins[f] = in + f * n;
+        ws[f] = scr + f * n;
+        outs[f] = out + f * n;
+    }
+    return launch_deriv_t(T, axis, accumulate, nf, ins, ws, outs, nx, ny, nz, (cudaStream_t)stream);
+}
+
+} // extern "C"

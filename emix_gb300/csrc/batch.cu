@@ -50,6 +50,7 @@ struct VortOp { using A = VortArgs; static EMIX_DEV void cell(const A &a, long q
 struct SelOp { using A = SelArgs; static EMIX_DEV void cell(const A &a, long q) { select_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
 struct FluxOp { using A = FluxArgs; static EMIX_DEV void cell(const A &a, long q) { flux_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return a.n; } };
 struct BcOp { using A = BcArgs; static EMIX_DEV void cell(const A &a, long q) { bc_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return bc_count(a); } };
+struct ClockOp { using A = ImpClockArgs; static EMIX_DEV void cell(const A &a, long q) { if (q == 0) imp_clock_tick(a); } static EMIX_DEV long cnt(const A &) { return 1; } };
 struct RkOp { using A = RkArgs; static EMIX_DEV void cell(const A &a, long q) { rk_cell(a, q); } static EMIX_DEV long cnt(const A &a) { return rk_count(a); } };
 
 template <class Op>
@@ -168,6 +169,7 @@ size_t args_size(int kind) {
     case LK_FLUX: return sizeof(FluxArgs);
     case LK_RK: return sizeof(RkArgs);
     case LK_BC: return sizeof(BcArgs);
+    case LK_CLOCK: return sizeof(ImpClockArgs);
     default: return 0;
     }
 }
@@ -185,6 +187,7 @@ const void *args_ptr(const Launch &L) {
     case LK_FLUX: return &L.flux;
     case LK_RK: return &L.rk;
     case LK_BC: return &L.bc;
+    case LK_CLOCK: return &L.clock;
     default: return nullptr;
     }
 }
@@ -200,6 +203,7 @@ long point_count(const Launch &L) {
     case LK_FLUX: return L.flux.n;
     case LK_RK: return rk_count(L.rk);
     case LK_BC: return bc_count(L.bc);
+    case LK_CLOCK: return 1;
     default: return 0;
     }
 }
@@ -320,6 +324,7 @@ int issue(emix_batch *b) {
         case LK_FLUX: k_batch_cells<FluxOp><<<nb, 256, 0, st>>>((const FluxArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_RK: k_batch_cells<RkOp><<<nb, 256, 0, st>>>((const RkArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_BC: k_batch_cells<BcOp><<<nb, 256, 0, st>>>((const BcArgs *)P.args, P.start, G, b->tune.cpb); break;
+        case LK_CLOCK: k_batch_cells<ClockOp><<<nb, 256, 0, st>>>((const ImpClockArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_WENO:
             k_batch_weno<<<nb, dim3(kWX, kWY, kWZ), 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
             break;

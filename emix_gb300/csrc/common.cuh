@@ -74,4 +74,22 @@ int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow 
 // stream is being captured.
 int get_deriv_table(int scheme, int n, double h, DerivTable *out);
 
+// per-device grow-only scratch of the library (deriv_ops.cu); calls that use
+// it and overlap on one device race
+int device_scratch(size_t bytes, double **out);
+
+// Transposed operator D^T (the adjoint): y_i = r_i ib_i - m_i y_{i-1},
+// z_i = y_i - g_i z_{i+1} solves A^T z = r; then out_j = sum_k bt[7j+k] z_{j+k-3}.
+// For the cyclic scheme D^T = -D and `neg` is the forward table of -D.
+struct DerivTRow {
+    double ib, m, g;
+};
+struct DerivTTable {
+    int n, periodic;
+    const DerivTRow *rows;
+    const double *bt;
+    DerivTable neg;
+};
+int get_deriv_t_table(int scheme, int n, double h, DerivTTable *out);
+
 } // namespace emix

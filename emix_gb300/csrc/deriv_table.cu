@@ -89,13 +89,29 @@ int define_rows(int scheme, int n, std::vector<RowDef> &R) {
 
 } // namespace
 
+namespace {
+
+// the table of (sign/h) * A^{-1} B: sign = -1 gives -D, which is D^T for the
+// cyclic scheme (A symmetric circulant, B antisymmetric circulant)
+int build_table_signed(int scheme, int n, double h, double sign, DerivTable &t, DerivRow *rows,
+                       double *clo, double *chi, double *u0, double *zz);
+
+} // namespace
+
 int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow *rows,
                            double *clo, double *chi, double *u0, double *zz) {
     if (n < 6 || n > kTableMaxN || !(h > 0.0)) return EMIX_ERR_ARG;
+    return build_table_signed(scheme, n, h, 1.0, t, rows, clo, chi, u0, zz);
+}
+
+namespace {
+
+int build_table_signed(int scheme, int n, double h, double sign, DerivTable &t, DerivRow *rows,
+                       double *clo, double *chi, double *u0, double *zz) {
     std::vector<RowDef> R;
     if (define_rows(scheme, n, R)) return EMIX_ERR_ARG;
     const bool per = scheme == EMIX_SCHEME_BPER;
-    const double s = 1.0 / h;
+    const double s = sign / h;
 
     std::vector<double> bb(n), bet(n), gam(n, 0.0);
     for (int i = 0; i < n; ++i) bb[i] = R[i].b;
@@ -179,8 +195,6 @@ int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow 
     return EMIX_OK;
 }
 
-namespace {
-
 struct TableKey {
     int dev, scheme, n;
     double h;
@@ -194,10 +208,17 @@ std::map<TableKey, DerivTable> g_tables;   // device buffers live until process 
 
 } // namespace
 
+int get_table_signed(int scheme, int n, double h, double sign, DerivTable *out);
+
 int get_deriv_table(int scheme, int n, double h, DerivTable *out) {
+    if (!(h > 0.0)) return EMIX_ERR_ARG;
+    return get_table_signed(scheme, n, h, 1.0, out);
+}
+
+int get_table_signed(int scheme, int n, double h, double sign, DerivTable *out) {
     int dev = 0;
     EMIX_CUDA_TRY(cudaGetDevice(&dev));
-    TableKey key{dev, scheme, n, h};
+    TableKey key{dev, scheme, n, sign * h};
     std::lock_guard<std::mutex> lock(g_table_mu);
     auto it = g_tables.find(key);
     if (it != g_tables.end()) {
@@ -208,8 +229,8 @@ int get_deriv_table(int scheme, int n, double h, DerivTable *out) {
     std::vector<DerivRow> rows(n);
     std::vector<double> clo(kMaxClosure * 4), chi(kMaxClosure * 4), u0(n, 0.0), zz(n, 0.0);
     DerivTable t{};
-    int rc = build_deriv_table_host(scheme, n, h, t, rows.data(), clo.data(), chi.data(),
-                                    u0.data(), zz.data());
+    int rc = build_table_signed(scheme, n, h, sign, t, rows.data(), clo.data(), chi.data(),
+                                u0.data(), zz.data());
     if (rc) return rc;
     // one allocation: rows | clo | chi | u0 | zz
     const size_t nd = (size_t)4 * n + 8 * kMaxClosure + 2 * (size_t)n;
@@ -232,6 +253,111 @@ int get_deriv_table(int scheme, int n, double h, DerivTable *out) {
     t.u0 = t.chi + 4 * kMaxClosure;
     t.zz = t.u0 + n;
     g_tables[key] = t;
+    *out = t;
+    return EMIX_OK;
+}
+
+// ---- transposed operator D^T = B^T A^{-T} (the adjoint's pencil solves) ----
+
+namespace {
+
+struct TKey {
+    int dev, scheme, n;
+    double h;
+    bool operator<(const TKey &o) const {
+        return std::tie(dev, scheme, n, h) < std::tie(o.dev, o.scheme, o.n, o.h);
+    }
+};
+
+std::mutex g_t_mu;
+std::map<TKey, DerivTTable> g_t_tables;
+
+// A^T (sub-diagonal c_{i-1}, super-diagonal a_{i+1}) factored once; B^T as a
+// band of 7 (offsets -3..3, the closure rows reach 3 away), 1/h folded in
+int build_t_host(int scheme, int n, double h, std::vector<DerivTRow> &rows, std::vector<double> &bt) {
+    std::vector<RowDef> R;
+    if (define_rows(scheme, n, R)) return EMIX_ERR_ARG;
+    const double s = 1.0 / h;
+    rows.assign(n, DerivTRow{});
+    std::vector<double> bet(n), gam(n + 1, 0.0);
+    bet[0] = R[0].b;
+    for (int i = 1; i < n; ++i) {
+        gam[i] = R[i].a / bet[i - 1];                 // super-diagonal of A^T at row i-1
+        bet[i] = R[i].b - R[i - 1].c * gam[i];        // sub-diagonal of A^T at row i: c_{i-1}
+        if (bet[i] == 0.0 || !std::isfinite(bet[i])) return EMIX_ERR_ARG;
+    }
+    for (int i = 0; i < n; ++i) {
+        const double ib = 1.0 / bet[i];
+        rows[i].ib = ib;
+        rows[i].m = i == 0 ? 0.0 : R[i - 1].c * ib;
+        rows[i].g = i == n - 1 ? 0.0 : gam[i + 1];
+    }
+    // B as rows: B[i][j]; B^T[j][i - j + 3] = B[i][j]
+    bt.assign((size_t)7 * n, 0.0);
+    auto put = [&](int i, int j, double v) {
+        const int k = i - j + 3;
+        if (j < 0 || j >= n || k < 0 || k > 6) return false;
+        bt[(size_t)7 * j + k] += s * v;
+        return true;
+    };
+    for (int i = 0; i < n; ++i) {
+        const RowDef &r = R[i];
+        bool ok = true;
+        if (r.kind == 0) {
+            ok = ok && (r.ars == 0.0 || (put(i, i + 1, r.ars) && put(i, i - 1, -r.ars)));
+            ok = ok && (r.brs == 0.0 || (put(i, i + 2, r.brs) && put(i, i - 2, -r.brs)));
+        } else if (r.kind == 1) {
+            for (int q = 0; q < 4; ++q) if (r.cc[q] != 0.0) ok = ok && put(i, q, r.cc[q]);
+        } else {
+            for (int q = 0; q < 4; ++q) if (r.cc[q] != 0.0) ok = ok && put(i, n - 1 - q, r.cc[q]);
+        }
+        if (!ok) return EMIX_ERR_ARG;
+    }
+    return EMIX_OK;
+}
+
+} // namespace
+
+int get_deriv_t_table(int scheme, int n, double h, DerivTTable *out) {
+    if (!(h > 0.0) || n < 6 || n > kTableMaxN) return EMIX_ERR_ARG;
+    int dev = 0;
+    EMIX_CUDA_TRY(cudaGetDevice(&dev));
+    TKey key{dev, scheme, n, h};
+    {
+        std::lock_guard<std::mutex> lock(g_t_mu);
+        auto it = g_t_tables.find(key);
+        if (it != g_t_tables.end()) {
+            *out = it->second;
+            return EMIX_OK;
+        }
+    }
+    DerivTTable t{};
+    t.n = n;
+    if (scheme == EMIX_SCHEME_BPER) {
+        // cyclic scheme: D^T = -D, the forward kernels with -1/h
+        t.periodic = 1;
+        int rc = get_table_signed(scheme, n, h, -1.0, &t.neg);
+        if (rc) return rc;
+    } else {
+        std::vector<DerivTRow> rows;
+        std::vector<double> bt;
+        int rc = build_t_host(scheme, n, h, rows, bt);
+        if (rc) return rc;
+        const size_t nd = (size_t)3 * n + bt.size();
+        double *buf = nullptr;
+        if (cudaMalloc(&buf, nd * sizeof(double)) != cudaSuccess) {
+            set_last_message("cudaMalloc of a transposed derivative table failed");
+            return EMIX_ERR_ALLOC;
+        }
+        std::vector<double> host(nd);
+        std::memcpy(host.data(), rows.data(), (size_t)n * sizeof(DerivTRow));
+        std::memcpy(host.data() + 3 * (size_t)n, bt.data(), bt.size() * sizeof(double));
+        EMIX_CUDA_TRY(cudaMemcpy(buf, host.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
+        t.rows = reinterpret_cast<const DerivTRow *>(buf);
+        t.bt = buf + 3 * (size_t)n;
+    }
+    std::lock_guard<std::mutex> lock(g_t_mu);
+    g_t_tables[key] = t;
     *out = t;
     return EMIX_OK;
 }

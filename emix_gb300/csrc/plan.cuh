@@ -17,7 +17,7 @@ namespace emix {
 
 enum LaunchKind {
     LK_PRIM, LK_PAD, LK_WENO, LK_DERIV_X, LK_DERIV_YZ, LK_SMAG, LK_SF, LK_VORT, LK_SELECT,
-    LK_FLUX, LK_RK, LK_BC, LK_COUNT
+    LK_FLUX, LK_RK, LK_BC, LK_CLOCK, LK_COUNT
 };
 
 // profile classes (emix_ctx_profile)
@@ -47,6 +47,7 @@ struct Launch {
         FluxArgs flux;
         RkArgs rk;
         BcArgs bc;
+        ImpClockArgs clock;
     };
 };
 

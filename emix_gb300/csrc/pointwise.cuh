@@ -6,6 +6,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "impeller.cuh"
 
 namespace emix {
 
@@ -233,6 +234,10 @@ struct RkArgs {
     int faces;            // with walls: 0 = cells no wall rule touches, 1 = the wall cells
     int nx, ny, nz;
     long n;
+    ImpGeom imp;          // impeller forcing after the walls (imp.on = 0: none)
+    const double *xyz;    // coordinates (3 fields), read when imp.on
+    const double *clock;  // impeller clock (k_imp_clock), read when imp.on
+    const unsigned char *impflag;   // cells the impeller can reach (k_imp_flags)
 };
 
 // Wall cells: z = 0, nz-2, nz-1 (frontera_z), y = 0, ny-1 (frontera_y),
@@ -266,8 +271,14 @@ EMIX_DEV void rk_combine(const RkArgs &a, long q, double v[5]) {
 
 // varc_to_varnc + clip + mask + varc_to_varnc (:104-124), then the rebuild
 // after the level-set call site (:127-138), of the combined values v
-EMIX_DEV void rk_convert(const RkArgs &a, long q, const double v[5]) {
+EMIX_DEV void rk_convert(const RkArgs &a, long q, double v[5]) {
     const long n = a.n;
+    if (a.imp.on && a.impflag[q]) {
+        // rushton(stage) after the walls (rungek_ico.f90:102); cells the
+        // impeller cannot reach are left as they are
+        impeller_force_cell(a.imp, a.clock + 2 + 2 * (a.stage - 1) * kImpMaxBlades, a.xyz[q],
+                            a.xyz[n + q], a.xyz[2 * n + q], v, nullptr);
+    }
     const double r = v[0];
     const double rr = 1.0 / r;
     const double mk = a.mask[q];

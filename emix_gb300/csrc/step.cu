@@ -16,7 +16,7 @@
 // The level set is advanced as part of the same SSP-RK3 step (one TVD stage
 // per flow substep, each with the velocity the flow stage uses); with a
 // frozen velocity this is exactly one cuAdvectLsJB step.
-#include "plan.cuh"
+#include "ctx.cuh"
 
 #include <cstdio>
 #include <cstring>
@@ -71,6 +71,9 @@ int launch_single(const Launch &L, cudaStream_t st) {
     case LK_BC:
         k_bc<<<cells_grid(bc_count(L.bc)), 256, 0, st>>>(L.bc);
         break;
+    case LK_CLOCK:
+        k_imp_clock<<<1, 32, 0, st>>>(L.clock);
+        break;
     default:
         return EMIX_ERR_ARG;
     }
@@ -81,31 +84,7 @@ int launch_single(const Launch &L, cudaStream_t st) {
 
 using namespace emix;
 
-struct emix_ctx {
-    emix_params p{};
-    int dev = 0;
-    long n = 0, ng = 0;
-    cudaStream_t stream = nullptr;
-    cudaStream_t own = nullptr;
-    double *arena = nullptr;
-    size_t arena_bytes = 0;
-    double *um0, *um, *u, *pres, *dvel, *vis, *amut, *vort, *flux, *R, *W, *jbn, *jx, *jy, *jz,
-        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB, *wenoC, *wenoE;
-    DerivTable T[3];
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    cudaGraph_t fgraph = nullptr;          // the filter (filtrado), when on
-    cudaGraphExec_t fgexec = nullptr;
-    long step_index = 0;
-    bool static_set = false;
-    int launches = 0;
-    // optional per-launch timing (emix_ctx_profile): events around every launch
-    bool prof = false;
-    int prof_n = 0;
-    cudaEvent_t prof_ev[2 * 64] = {};
-    int prof_cls[64] = {};
-    std::vector<Launch> plan;   // one RK3 step
-};
+
 
 static const char *kClassNames[] = {
     "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
@@ -163,6 +142,15 @@ void build_plan(emix_ctx *c) {
     const double inv_m2 = 1.0 / (p.mach * p.mach);
     std::vector<Launch> &P = c->plan;
     P.clear();
+    const ImpGeom ig{p.imp.on, p.imp.nblades, p.imp.omega, p.imp.theta0, p.imp.r1, p.imp.r2,
+                     p.imp.z1, p.imp.z2, p.imp.half_thick, p.imp.hub_r, p.imp.hub_z1, p.imp.hub_z2,
+                     p.imp.shaft_r, p.imp.shaft_z0, p.imp.shaft_z1};
+    if (ig.on) {
+        // blade angles of this step's substeps, then advance the clock
+        Launch L = make(LK_CLOCK, CLS_RK);
+        L.clock = ImpClockArgs{c->clock, p.dt, ig};
+        P.push_back(L);
+    }
     {
         Launch L = make(LK_PRIM, CLS_PRIM);
         L.prim = PrimArgs{c->um0, c->u, c->pres, inv_m2, n};
@@ -262,6 +250,10 @@ void build_plan(emix_ctx *c) {
             ra.nx = nx; ra.ny = ny; ra.nz = nz;
             ra.walls = p.bc_walls;
             ra.faces = 0;
+            ra.imp = ig;
+            ra.xyz = c->xyz;
+            ra.clock = c->clock;
+            ra.impflag = c->impflag;
             if (p.bc_walls) {
                 Launch F = L;
                 F.rk.faces = 1;
@@ -294,6 +286,9 @@ bool params_ok(const emix_params *p) {
     if (p->sgs_model < EMIX_SGS_NONE || p->sgs_model > EMIX_SGS_STRUCTURE) return false;
     if (p->bc_walls != 0 && p->bc_walls != 1) return false;
     if (p->filter_every < 0 || (p->filter_every > 0 && (p->nx < 11 || p->ny < 11 || p->nz < 11)))
+        return false;
+    if ((p->imp.on != 0 && p->imp.on != 1) ||
+        (p->imp.on && (p->imp.nblades < 0 || p->imp.nblades > kImpMaxBlades)))
         return false;
     if (!(p->mach > 0.0) || !(p->dt > 0.0)) return false;
     if (p->level_set && (p->ls_ghost < 3 || p->ls_ghost > p->nx || p->ls_ghost > p->ny ||
@@ -342,6 +337,14 @@ int capture(emix_ctx *c, F issue, cudaGraph_t *g, cudaGraphExec_t *ge) {
 
 } // namespace
 
+namespace emix {
+void ctx_rebuild_plan(emix_ctx *c) {
+    drop_graph(c);
+    build_plan(c);
+}
+int ctx_issue_step(emix_ctx *c) { return issue_step(c); }
+} // namespace emix
+
 extern "C" {
 
 int emix_ctx_create(const emix_params *p, emix_ctx **out) {
@@ -368,7 +371,9 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     const bool sf = p->sgs_model == EMIX_SGS_STRUCTURE;
     const long nfield = 5 + 5 + 3 + 1 + 9 + 1 + 15 + 5 + 5 + 11 + 3 + 1 + 1 + (p->level_set ? 7 : 0) +
                         (sf ? 1 + 3 + 6 : 0);
-    const size_t bytes = ((size_t)nfield * n + 3 * (size_t)ng) * sizeof(double);
+    const bool imp = p->imp.on != 0;
+    const size_t bytes = ((size_t)(nfield + (imp ? 3 : 0)) * n + 3 * (size_t)ng +
+                          (imp ? kImpClockLen + (n + 7) / 8 : 0)) * sizeof(double);
     if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
         cudaGetLastError();
         set_last_message("cudaMalloc of the context arena failed");
@@ -391,6 +396,9 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     c->phig0 = p->level_set ? take(ng) : nullptr;
     c->phigA = p->level_set ? take(ng) : nullptr;
     c->phigB = p->level_set ? take(ng) : nullptr;
+    c->xyz = imp ? take(3 * n) : nullptr;
+    c->clock = imp ? take(kImpClockLen) : nullptr;
+    c->impflag = imp ? reinterpret_cast<unsigned char *>(take((n + 7) / 8)) : nullptr;
     if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(c->arena);
@@ -407,6 +415,17 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
         delete c;
         set_last_message("clearing the context arena failed");
         return EMIX_ERR_CUDA;
+    }
+    if (imp) {
+        const double head[2] = {p->t0, 0.0};
+        if (cudaMemcpy(c->clock, head, sizeof head, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            cudaStreamDestroy(c->own);
+            cudaFree(c->arena);
+            delete c;
+            set_last_message("setting the impeller clock failed");
+            return EMIX_ERR_CUDA;
+        }
     }
     build_plan(c);
     *out = c;
@@ -441,6 +460,13 @@ int emix_ctx_set_static(emix_ctx *c, const double *jbn, const double *mask, cons
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->mask, mask, n * sizeof(double), cudaMemcpyHostToDevice, st));
     // coordinates go through the flux buffer (free at this point)
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->flux, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (c->xyz) {
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->xyz, c->flux, 3 * n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        const ImpGeom ig{p.imp.on, p.imp.nblades, p.imp.omega, p.imp.theta0, p.imp.r1, p.imp.r2,
+                         p.imp.z1, p.imp.z2, p.imp.half_thick, p.imp.hub_r, p.imp.hub_z1,
+                         p.imp.hub_z2, p.imp.shaft_r, p.imp.shaft_z0, p.imp.shaft_z1};
+        k_imp_flags<<<cells_grid(n), 256, 0, st>>>(c->xyz, ig, n, c->impflag);
+    }
     double *ratios = c->ratios ? c->ratios : c->flux + 3 * n;
     k_sgs_setup<<<cells_grid(n), 256, 0, st>>>(c->flux, c->dxyz, ratios, p.nx, p.ny, p.nz);
     k_metric_products<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->jx, c->jy, c->jz, n);
@@ -520,6 +546,23 @@ int emix_step(emix_ctx *c, int nsteps, int use_graph) {
 int emix_ctx_get_step_index(emix_ctx *c, long *index) {
     if (!c || !index) return EMIX_ERR_ARG;
     *index = c->step_index;
+    return EMIX_OK;
+}
+
+int emix_ctx_set_time(emix_ctx *c, double t0) {
+    if (!c || !c->clock) return EMIX_ERR_ARG;
+    const double head[2] = {t0, 0.0};
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->clock, head, sizeof head, cudaMemcpyHostToDevice, c->stream));
+    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return EMIX_OK;
+}
+
+int emix_ctx_get_time(emix_ctx *c, double *t) {
+    if (!c || !t || !c->clock) return EMIX_ERR_ARG;
+    double head[2];
+    EMIX_CUDA_TRY(cudaMemcpyAsync(head, c->clock, sizeof head, cudaMemcpyDeviceToHost, c->stream));
+    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    *t = head[0] + head[1] * c->p.dt;
     return EMIX_OK;
 }
 

@@ -103,6 +103,45 @@ class Grid:
 
 
 @dataclass
+class Impeller:
+    """A rotating impeller applied as a volumetric forcing each substep: blade
+    b at angle theta0 + omega*t + b*2*pi/nblades is the box r1 <= along <= r2,
+    |across| <= half_thick, z1 <= z <= z2; plus a hub disc and a shaft.  Inside
+    it the velocity is the rigid rotation (-omega*y, omega*x)."""
+    nblades: int = 6
+    omega: float = 1.0
+    theta0: float = -math.pi / 6.0
+    r1: float = 0.165
+    r2: float = 0.33
+    z1: float = 0.6167
+    z2: float = 0.7167
+    half_thick: float = 0.012
+    hub_r: float = 0.2475
+    hub_z1: float = 0.654
+    hub_z2: float = 0.679
+    shaft_r: float = 0.0264
+    shaft_z0: float = 0.6667
+    shaft_z1: float = 5.0
+
+
+def tank_impeller(grid: "Grid", radius=1.0, height=2.0, omega=1.0, nblades=6, z_frac=1.0 / 3.0,
+                  blade_r=0.33, blade_h=0.05) -> Impeller:
+    """Impeller of the tank workload in the proportions of the reference's
+    rushton(sub_step) (rush_ruth_me.f90:52-95: blades from R2/2 to R2, hub
+    disc of 0.75 R2, blade half-thickness 1.5 dmin, shaft of 0.08 R2 from the
+    disc upward, initial angle -pi/6), with blade radius blade_r*R and blade
+    height blade_h*H at z = z_frac*H."""
+    dmin = min(grid.length[a] * grid.h(a) for a in range(3))
+    r2 = blade_r * radius
+    zc = z_frac * height
+    th = 1.5 * dmin
+    return Impeller(nblades=nblades, omega=omega, theta0=-math.pi / 6.0, r1=0.5 * r2, r2=r2,
+                    z1=zc - 0.5 * blade_h * height, z2=zc + 0.5 * blade_h * height, half_thick=th,
+                    hub_r=0.75 * r2, hub_z1=zc - th, hub_z2=zc + th, shaft_r=0.08 * r2,
+                    shaft_z0=zc, shaft_z1=2.5 * height)
+
+
+@dataclass
 class Workload:
     grid: Grid
     schemes: tuple
@@ -118,6 +157,8 @@ class Workload:
     dt: float = 0.0
     name: str = ""
     extra: dict = field(default_factory=dict)
+    impeller: Impeller | None = None   # rotating impeller forcing (None: static mask only)
+    t0: float = 0.0                    # time at the start of the first step
 
 
 def cfl_dt(grid: Grid, u: np.ndarray, mach: float, cfl: float) -> float:
@@ -194,11 +235,14 @@ def rushton_mask(grid: Grid, radius=1.0, height=2.0, nblades=6, z_frac=1.0 / 3.0
 
 
 def stirred_tank(n=256, seed=2, nmodes=64, kmax=8, omega=1.0, radius=1.0, height=2.0,
-                 scheme=SCHEME_B, mach=0.1, cfl=0.3, reynolds=1000.0, nz=None) -> Workload:
+                 scheme=SCHEME_B, mach=0.1, cfl=0.3, reynolds=1000.0, nz=None,
+                 impeller=False, impeller_omega=None) -> Workload:
     """Wall-bounded tank [-R,R]^2 x [0,H]: solid-body rotation about z plus
     ``nmodes`` seeded Fourier modes with |k| <= kmax and Gaussian amplitudes
     rescaled to an RMS of 0.1*omega*R, a flat free surface at z = 0.8H and a
-    6-blade impeller mask at z = H/3."""
+    6-blade impeller at z = H/3: a static mask, or with ``impeller`` a
+    rotating impeller forcing (angular velocity ``impeller_omega``, default
+    ``omega``) and no static mask."""
     nz = n if nz is None else nz
     g = Grid(n, n, nz, (2 * radius, 2 * radius, height), (-radius, -radius, 0.0),
              (False, False, False))
@@ -238,9 +282,12 @@ def stirred_tank(n=256, seed=2, nmodes=64, kmax=8, omega=1.0, radius=1.0, height
     temp = np.ones(g.shape)
     um = _conserved(p, u, temp, mach)
     phi = Z - 0.8 * height
-    mask = rushton_mask(g, radius, height)
+    mask = np.ones(g.shape) if impeller else rushton_mask(g, radius, height)
     w = Workload(g, (scheme,) * 3, um, phi, g.jbn(), mask, mach=mach, reynolds=reynolds,
                  name=f"stirred_tank_{n}x{n}x{nz}")
+    if impeller:
+        w.impeller = tank_impeller(g, radius, height,
+                                   omega if impeller_omega is None else impeller_omega)
     w.dt = cfl_dt(g, u, mach, cfl)
     return w
 

@@ -223,6 +223,35 @@ def weno5_advect_dev(phi, vel, jbn, h, dt, ref_bugs=0):
     return phi
 
 
+def impeller_force_dev(um, xyz, imp, t):
+    """The impeller forcing at time t on device tensors (um in place); returns the mask."""
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(um)
+    c = _lib.EmixImpeller()
+    c.on = 1
+    for f, _ in _lib.EmixImpeller._fields_[1:]:
+        setattr(c, f, getattr(imp, f))
+    mask = torch.empty_like(um[0])
+    check(lib.emix_impeller_force_dev(_ptr(um), _ptr(xyz), C.byref(c), t, nx, ny, nz, _ptr(mask),
+                                      _stream()), "emix_impeller_force_dev")
+    return mask
+
+
+def deriv_t_dev(y, axis: int, h: float, scheme=SCHEME_C, out=None):
+    """D^T y along `axis` (the transpose of deriv_dev); out += D^T y when out is given."""
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(y)
+    nf = 1 if y.dim() == 3 else y.shape[0]
+    acc = out is not None
+    if out is None:
+        out = torch.empty_like(y)
+    check(lib.emix_deriv_t_dev(scheme, axis, nf, _ptr(out), _ptr(y), h, nx, ny, nz, int(acc),
+                               _stream()), "emix_deriv_t_dev")
+    return out
+
+
 def filtrado_dev(um, jbn, cfilt):
     """filtrado (x, y, z compact filter of the 5 fields) in place on device tensors."""
     lib = _lib.load()
@@ -393,6 +422,16 @@ class Context:
         check(self.lib.emix_step(self._h, nsteps, 1 if use_graph else 0), "emix_step")
 
     @property
+    def time(self) -> float:
+        v = C.c_double()
+        check(self.lib.emix_ctx_get_time(self._h, C.byref(v)), "emix_ctx_get_time")
+        return v.value
+
+    @time.setter
+    def time(self, t0: float):
+        check(self.lib.emix_ctx_set_time(self._h, float(t0)), "emix_ctx_set_time")
+
+    @property
     def step_index(self) -> int:
         v = C.c_long()
         check(self.lib.emix_ctx_get_step_index(self._h, C.byref(v)), "emix_ctx_get_step_index")
@@ -452,6 +491,12 @@ def _params_of(w, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0, filter_eve
     p.bc_walls = bc_walls
     p.filter_every = filter_every
     p.cfilt = cfilt
+    imp = getattr(w, "impeller", None)
+    if imp is not None:
+        p.imp.on = 1
+        for f, _ in _lib.EmixImpeller._fields_[1:]:
+            setattr(p.imp, f, getattr(imp, f))
+    p.t0 = getattr(w, "t0", 0.0)
     return p
 
 
@@ -483,10 +528,13 @@ class Batch:
         return sum(w.grid.ncell for w in self.workloads)
 
     def upload(self):
+        """Initial state of every grid, and the impeller clocks back to t0."""
         for h, w in zip(self.ctx, self.workloads):
             um = np.ascontiguousarray(w.um)
             phi = np.ascontiguousarray(w.phi) if self.level_set else None
             check(self.lib.emix_ctx_upload(h, _ptr(um), _ptr(phi)), "emix_ctx_upload")
+            if getattr(w, "impeller", None) is not None:
+                check(self.lib.emix_ctx_set_time(h, getattr(w, "t0", 0.0)), "emix_ctx_set_time")
 
     def download(self, g):
         w = self.workloads[g]

@@ -18,12 +18,13 @@ def main(argv=None):
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--no-level-set", action="store_true")
     ap.add_argument("--walls", action="store_true", help="frontera wall conditions every substep")
+    ap.add_argument("--impeller", action="store_true", help="rotating impeller forcing (tank)")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
     from . import fields as F
     from . import ops
-    w = F.stirred_tank(n=a.n) if a.workload == "tank" else F.taylor_green(n=a.n)
+    w = F.stirred_tank(n=a.n, impeller=a.impeller) if a.workload == "tank" else F.taylor_green(n=a.n)
     ctx = ops.Context(w, level_set=not a.no_level_set, bc_walls=int(a.walls))
     t0 = time.perf_counter()
     ctx.step(a.steps, use_graph=a.graph)

@@ -218,6 +218,17 @@ int emix_extrapolate_dev(double *ext, const double *phiS, const double *jbn,
                          void *stream);
 
 /* ========================================================================
+ * Adjoint building blocks
+ * ======================================================================== */
+
+/* out = D^T in (accumulate = 0) or out += D^T in (1): the transpose of the
+ * compact first derivative emix_deriv_dev computes (no counterpart in the
+ * reference; the adjoint of cudaDeriv / cuDivergence).  Device pointers;
+ * uses the library's per-device scratch. */
+int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                     int nx, int ny, int nz, int accumulate, void *stream);
+
+/* ========================================================================
  * Compact filter
  * ======================================================================== */
 
@@ -266,6 +277,24 @@ int emix_metrics_dev(const double *xyz, double *jbn, int scheme, double hx, doub
  * Device-resident RK3 step (solver/rungek_ico.f90:61-313)
  * ======================================================================== */
 
+/* A rotating impeller applied as a volumetric forcing after the walls in
+ * every substep: the linked rushton(sub_step) without its blade-edge
+ * interpolation (src/Geometry/rush_ruth_me.f90:2-108, makeAspa :519-593;
+ * addMaskCil, addAngularVel: src/Geometry/rotating.f90:110-205).  Blade b at
+ * angle theta0 + omega*t + b*2*pi/nblades is the box r1 <= along <= r2,
+ * |across| <= half_thick, z1 <= z <= z2; the hub disc has radius hub_r over
+ * [hub_z1, hub_z2], the shaft radius shaft_r over [shaft_z0, shaft_z1].
+ * Inside, the velocity is set to the rigid rotation (-omega*y, omega*x).
+ * The reference's impeller is omega = -2*pi, theta0 = -pi/6 (:58-61). */
+typedef struct emix_impeller {
+    int on;             /* 0: no impeller forcing                                  */
+    int nblades;        /* <= 16                                                   */
+    double omega, theta0;
+    double r1, r2, z1, z2, half_thick;
+    double hub_r, hub_z1, hub_z2;
+    double shaft_r, shaft_z0, shaft_z1;
+} emix_impeller;
+
 typedef struct emix_params {
     int nx, ny, nz;
     int scheme[3];      /* per axis, EMIX_SCHEME_*                                */
@@ -284,7 +313,14 @@ typedef struct emix_params {
                            step, counting from the first (9 in the reference,
                            solver/rungek_ico.f90:269-276); 0: off               */
     double cfilt;       /* filter parameter alpha (cfilt of data.in)              */
+    emix_impeller imp;  /* rotating impeller forcing (imp.on = 0: none)           */
+    double t0;          /* time at the start of the first step (the impeller's clock) */
 } emix_params;
+
+/* The impeller forcing at time t on um[5] (device pointers, in place);
+ * mask (may be NULL) receives the impeller mask.  Synchronous. */
+int emix_impeller_force_dev(double *um, const double *xyz, const emix_impeller *imp, double t,
+                            int nx, int ny, int nz, double *mask, void *stream);
 
 typedef struct emix_ctx emix_ctx;
 
@@ -317,6 +353,11 @@ int emix_step(emix_ctx *ctx, int nsteps, int use_graph);
  * steps whose index is a multiple of filter_every).  Settable for restarts. */
 int emix_ctx_get_step_index(emix_ctx *ctx, long *index);
 int emix_ctx_set_step_index(emix_ctx *ctx, long index);
+
+/* The impeller's clock: time of the next step = t0 + k*dt with k the steps
+ * taken since the clock was last set (emix_ctx_set_time sets t0 and k = 0). */
+int emix_ctx_set_time(emix_ctx *ctx, double t0);
+int emix_ctx_get_time(emix_ctx *ctx, double *t);
 
 /* End-to-end form: copy um/phi from host, advance nsteps, copy back;
  * synchronous. */

@@ -914,6 +914,65 @@ int orc_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, in
     return 0;
 }
 
+/* makeAspa (src/Geometry/rush_ruth_me.f90:519-593) for every blade, then
+ * addMaskCil for the hub and the shaft (src/Geometry/rotating.f90:110-140):
+ * the impeller mask of one cell at time t. */
+static double impeller_mask_cell(const orc_impeller *imp, double x, double y, double z, double t) {
+    double m = 1.0;
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    for (int b = 0; b < imp->nblades; ++b) {
+        const double th = imp->theta0 + imp->omega * t + b * (two_pi / imp->nblades);
+        const double c = std::cos(th), sn = std::sin(th);
+        /* planes of a blade rotated by th: A1..A4 = (0,1), (0,-1), (1,0), (-1,0) */
+        const double A1p = 0.0 * c - 1.0 * sn, B1p = 0.0 * sn + 1.0 * c;
+        const double A2p = 0.0 * c - (-1.0) * sn, B2p = 0.0 * sn + (-1.0) * c;
+        const double A3p = 1.0 * c - 0.0 * sn, B3p = 1.0 * sn + 0.0 * c;
+        const double A4p = -1.0 * c - 0.0 * sn, B4p = -1.0 * sn + 0.0 * c;
+        const double pl1 = A1p * x + B1p * y + (-imp->half_thick);
+        const double pl2 = A2p * x + B2p * y + (-imp->half_thick);
+        const double pl3 = A3p * x + B3p * y + (-imp->r2);
+        const double pl4 = A4p * x + B4p * y + imp->r1;
+        if (pl1 <= 0.0 && pl2 <= 0.0 && pl3 <= 0.0 && pl4 <= 0.0 && z >= imp->z1 && z <= imp->z2) m = 0.0;
+    }
+    const double radio = std::sqrt(x * x + y * y);
+    if (radio >= 0.0 && radio <= imp->hub_r && z >= imp->hub_z1 && z <= imp->hub_z2) m = 0.0;
+    if (radio >= 0.0 && radio <= imp->shaft_r && z >= imp->shaft_z0 && z <= imp->shaft_z1) m = 0.0;
+    return m;
+}
+
+/* the body velocity of addAngularVel (rotating.f90:163-186): the polar angle
+ * from atan(|y/x|) with the reference's constants for pi, then
+ * (-omega r sin, omega r cos) */
+static void impeller_velocity(double omega, double x, double y, double *ue, double *ve) {
+    const double radio = std::sqrt(x * x + y * y);
+    double th;
+    if (x != 0.0) th = std::atan(std::fabs(y / x));
+    else th = 3.1415926 / 2.;
+    if (x < 0.0 && y > 0.0) th = 3.141592 - th;
+    else if (x < 0.0 && y <= 0.0) th = th + 3.141592;
+    else if (x >= 0.0 && y < 0.0) th = 2.0 * 3.141592 - th;
+    *ue = -1.0 * omega * radio * std::sin(th);
+    *ve = omega * radio * std::cos(th);
+}
+
+int orc_impeller_force(double *um, const double *xyz, const orc_impeller *imp, double t,
+                       int nx, int ny, int nz, double *mask_out) {
+    const size_t n = (size_t)nx * ny * nz;
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < (long)n; ++q) {
+        const double x = xyz[q], y = xyz[n + q], z = xyz[2 * n + q];
+        const double m = impeller_mask_cell(imp, x, y, z, t);
+        double ue = 0.0, ve = 0.0;
+        if (m != 1.0) impeller_velocity(imp->omega, x, y, &ue, &ve);
+        const double r = um[q];
+        um[n + q] = ((1.0 - m) * ue + m * (um[n + q] / r)) * r;
+        um[2 * n + q] = ((1.0 - m) * ve + m * (um[2 * n + q] / r)) * r;
+        um[3 * n + q] = m * um[3 * n + q];
+        if (mask_out) mask_out[q] = m;
+    }
+    return 0;
+}
+
 int orc_bc_walls(double *um, int nx, int ny, int nz) {
     const size_t n = (size_t)nx * ny * nz;
     double *U[5] = {um, um + n, um + 2 * n, um + 3 * n, um + 4 * n};
@@ -1103,6 +1162,13 @@ int orc_step(const orc_step_params *p, double *um0, double *phi,
             }
         }
         if (p->bc_walls) orc_bc_walls(um1.data(), nx, ny, nz);   /* rungek_ico.f90:98-100 */
+        /* rushton(s) at dto, dto + dt/2, dto + dt (rungek_ico.f90:102;
+         * rush_ruth_me.f90:52-54) */
+        if (p->imp.on) {
+            if (!p->xyz) return 1;
+            const double ts = p->time + (s == 1 ? 0.0 : (s == 2 ? 0.5 * dt : dt));
+            orc_impeller_force(um1.data(), p->xyz, &p->imp, ts, nx, ny, nz, nullptr);
+        }
         /* varc_to_varnc, clip to [-6,6], mask, varc_to_varnc
          * (rungek_ico.f90:104-124, herramientas_incomp2.f90:16-27) */
         for (size_t q = 0; q < n; ++q) {

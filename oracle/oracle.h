@@ -101,6 +101,24 @@ int orc_weno_advect(double *phi, const double *vel, const double *jbn,
                     int nxg, int nyg, int nzg, int ref_bugs);
 double orc_phi_x_weno(double b1, double b2, double b3, double b4, double b5);
 
+/* A rotating Rushton-type impeller as a volumetric forcing, the linked
+ * rushton(sub_step) without its blade-edge interpolation
+ * (src/Geometry/rush_ruth_me.f90:2-108 with makeAspa :519-593, and
+ * addMaskCil / addAngularVel, src/Geometry/rotating.f90:110-205): a mask that
+ * is 0 inside nblades rectangular blades (blade b at angle
+ * theta0 + omega*t + b*2*pi/nblades, radial extent [r1, r2], half-thickness
+ * half_thick, z in [z1, z2]), a hub disc (radius hub_r, z in
+ * [hub_z1, hub_z2]) and a shaft (radius shaft_r, z in [shaft_z0, shaft_z1]),
+ * and 1 elsewhere; inside it the velocity is that of the rotating body. */
+typedef struct {
+    int on;
+    int nblades;
+    double omega, theta0;
+    double r1, r2, z1, z2, half_thick;
+    double hub_r, hub_z1, hub_z2;
+    double shaft_r, shaft_z0, shaft_z1;
+} orc_impeller;
+
 /* Parameters of one RK3 step (solver/rungek_ico.f90:61-313). */
 typedef struct {
     int nx, ny, nz;
@@ -119,6 +137,9 @@ typedef struct {
     int filter_every;     /* > 0: filtrado at the end of steps with step_index % filter_every == 0 (9 in the reference) */
     double cfilt;         /* filter parameter alpha (cfilt of data.in) */
     long step_index;      /* steps taken before this one */
+    orc_impeller imp;     /* rotating impeller forcing after the walls */
+    double time;          /* time at the start of this step (dto) */
+    const double *xyz;    /* grid coordinates (3 fields), read when imp.on */
 } orc_step_params;
 
 /* One RK3 step.  State in/out: um (5 fields) and phi (1 field, may be NULL
@@ -164,6 +185,11 @@ int orc_filtronper(int n, double *u, double cfilt, int zrows);
 /* filtrado as RUNGEK calls it (itf = 1; herramientas_incomp2.f90:227-410) on
  * um[5] in place. */
 int orc_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, int nz);
+
+/* The impeller forcing at time t on um[5] in place (rush_ruth_me.f90:52-95);
+ * mask_out (may be NULL) receives the impeller mask. */
+int orc_impeller_force(double *um, const double *xyz, const orc_impeller *imp, double t,
+                       int nx, int ny, int nz, double *mask_out);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

@@ -20,6 +20,16 @@ vp = C.c_void_p
 i3 = C.c_int * 3
 
 
+class Impeller(C.Structure):
+    _fields_ = [
+        ("on", C.c_int), ("nblades", C.c_int), ("omega", C.c_double), ("theta0", C.c_double),
+        ("r1", C.c_double), ("r2", C.c_double), ("z1", C.c_double), ("z2", C.c_double),
+        ("half_thick", C.c_double), ("hub_r", C.c_double), ("hub_z1", C.c_double),
+        ("hub_z2", C.c_double), ("shaft_r", C.c_double), ("shaft_z0", C.c_double),
+        ("shaft_z1", C.c_double),
+    ]
+
+
 class StepParams(C.Structure):
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
@@ -28,7 +38,7 @@ class StepParams(C.Structure):
         ("mach", C.c_double), ("dt", C.c_double),
         ("level_set", C.c_int), ("ls_ghost", C.c_int), ("ref_bugs", C.c_int),
         ("bc_walls", C.c_int), ("filter_every", C.c_int), ("cfilt", C.c_double),
-        ("step_index", C.c_long),
+        ("step_index", C.c_long), ("imp", Impeller), ("time", C.c_double), ("xyz", vp),
     ]
 
 
@@ -75,6 +85,7 @@ def load():
         "orc_advect_extrapolate": [vp, vp, vp, C.c_double, C.c_double, C.c_double,
                                    C.c_int, C.c_int, C.c_int, C.c_double],
         "orc_filtronper": [C.c_int, vp, C.c_double, C.c_int],
+        "orc_impeller_force": [vp, vp, C.POINTER(Impeller), C.c_double, C.c_int, C.c_int, C.c_int, vp],
         "orc_filtrado": [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int],
         "orc_set_threads": [C.c_int],
         "orc_get_threads": [],
@@ -267,6 +278,20 @@ def jacobeano(xyz, scheme, h):
     return jbn
 
 
+def impeller_force(um, xyz, imp, t):
+    """The impeller forcing at time t; returns (um, mask)."""
+    um = np.array(um, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(um)
+    mask = np.empty(um.shape[1:])
+    c = Impeller()
+    c.on = 1
+    for f, _ in Impeller._fields_[1:]:
+        setattr(c, f, getattr(imp, f))
+    _ok(load().orc_impeller_force(_p(um), _p(np.ascontiguousarray(xyz)), C.byref(c), t, nx, ny, nz,
+                                  _p(mask)), "orc_impeller_force")
+    return um, mask
+
+
 def filtronper(u, cfilt, zrows=0):
     u = np.array(u, dtype=np.float64, copy=True)
     _ok(load().orc_filtronper(len(u), _p(u), cfilt, zrows), "orc_filtronper")
@@ -301,6 +326,14 @@ def step_params(workload, level_set=True, ref_bugs=0, ls_ghost=5, bc_walls=0, fi
     p.filter_every = filter_every
     p.cfilt = cfilt
     p.step_index = 0
+    imp = getattr(w, "impeller", None)
+    if imp is not None:
+        p.imp.on = 1
+        for f, _ in Impeller._fields_[1:]:
+            setattr(p.imp, f, getattr(imp, f))
+        p._xyz = np.ascontiguousarray(w.grid.coords())   # kept alive with the params
+        p.xyz = p._xyz.ctypes.data
+    p.time = getattr(w, "t0", 0.0)
     return p
 
 
@@ -308,8 +341,10 @@ def step(params: StepParams, um, phi, jbn, mask, dxyz, ratios=None, nsteps=1):
     um = np.array(um, dtype=np.float64, copy=True)
     phi = None if phi is None else np.array(phi, dtype=np.float64, copy=True)
     lib = load()
+    t0 = params.time
     for it in range(nsteps):
         params.step_index = it
+        params.time = t0 + it * params.dt
         _ok(lib.orc_step(C.byref(params), _p(um), _p(phi), _p(np.ascontiguousarray(jbn)),
                          _p(np.ascontiguousarray(mask)), _p(np.ascontiguousarray(dxyz)),
                          _p(None if ratios is None else np.ascontiguousarray(ratios))),
