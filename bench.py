@@ -287,6 +287,60 @@ def large_leg(steps: int, warmup: int, stream=None):
     }
 
 
+def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=None, fd=True):
+    """dJ/d(omega, Cs) of the tank objective after nsteps steps on the n^3 tank
+    by the hand-written adjoint, its cost against the forward steps, and the
+    central finite differences (h = 1e-6) it is checked against."""
+    import torch
+    from emix_gb300 import fields as F
+    from emix_gb300 import ops
+    w = F.stirred_tank(n=n, nz=nz, impeller=True)
+    X, Y, Z = w.grid.coords()
+    # free surface with a ripple, inside the box
+    w.phi = np.ascontiguousarray(Z - 0.8 * 2.0 + 0.02 * np.sin(3 * X) * np.cos(2 * Y))
+    r = ops.TankGradient(w, nsteps, every, bc_walls=WALLS)
+    s = stream or torch.cuda.Stream()
+    r.ctx.set_stream(s.cuda_stream)
+    om, cs = w.impeller.omega, w.cs
+    r.run(om, cs)                     # warm-up (graph capture, tables)
+    r.adj.backward()
+    t0 = time.perf_counter()
+    J = r.run(om, cs)
+    t1 = time.perf_counter()
+    g = r.adj.backward()
+    t2 = time.perf_counter()
+    fd = []
+    for k, p0 in enumerate((om, cs) if fd else ()):
+        h = 1e-6 * max(abs(p0), 1.0)
+        a = [om, cs]; a[k] = p0 + h
+        b = [om, cs]; b[k] = p0 - h
+        fd.append((r.run(*a) - r.run(*b)) / (2 * h))
+    # plain steps without checkpoints, for the cost ratio
+    r.ctx.upload(w.um, w.phi)
+    r.ctx.step(1, use_graph=True)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    r.ctx.step(nsteps, use_graph=True)
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    gib = r.adj.device_bytes() / 2**30
+    r.close()
+    cells = w.grid.ncell
+    plain = t4 - t3
+    return {
+        "workload": f"stirred tank {n}x{n}x{nz or n} walls + rotating impeller, {nsteps} RK3 steps, "
+                    "J = annulus kinetic energy + interface area",
+        "J": J, "dJ_domega": g[0], "dJ_dCs": g[1],
+        "fd_domega": fd[0] if fd else None, "fd_dCs": fd[1] if fd else None,
+        "rel_err": [abs(g[0] - fd[0]) / abs(fd[0]), abs(g[1] - fd[1]) / abs(fd[1])] if fd else None,
+        "forward_s": round(t1 - t0, 4), "backward_s": round(t2 - t1, 4), "plain_steps_s": round(plain, 4),
+        "adjoint_over_forward": round((t2 - t1) / plain, 3),
+        "forward_value": round(cells * nsteps / plain / 1e6, 3),
+        "adjoint_value": round(cells * nsteps / (t2 - t1) / 1e6, 3),
+        "unit": "Mcell-RK3-steps/s", "checkpoint_every": every, "adjoint_gib": round(gib, 2),
+    }
+
+
 def config_dict(w):
     return {
         "workload": f"stirred tank {N_GRID}^3 walls, RK3 step with WENO5 level set",
@@ -311,6 +365,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--no-large", action="store_true", help="skip the 512x512x384 leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (gradient) leg")
+    ap.add_argument("--large-adjoint", action="store_true",
+                    help="also run forward + adjoint on 512x512x384 (20 steps, checkpoints every 5)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -431,6 +488,10 @@ def main():
         line["ensemble"] = ensemble_leg(min(args.steps, 10), 3, stream)
     if world == 1 and not args.no_large:
         line["large"] = large_leg(min(args.steps, 5), 3, stream)
+    if world == 1 and not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(stream=stream)
+    if world == 1 and args.large_adjoint:
+        line["large_adjoint"] = adjoint_leg(512, 20, 5, stream, nz=384, fd=False)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sec, thr = cpu_sample(16, 1)
         line["cpu_baseline"] = {

@@ -36,6 +36,11 @@ class EmixImpeller(C.Structure):
     ]
 
 
+class EmixObjective(C.Structure):
+    _fields_ = [("r_in", C.c_double), ("r_out", C.c_double), ("eps", C.c_double),
+                ("w_ke", C.c_double), ("w_if", C.c_double)]
+
+
 class EmixParams(C.Structure):
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
@@ -76,6 +81,13 @@ PROTOTYPES = {
                                           C.c_int, C.c_int, vp, vp]),
     "emix_deriv_t_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int,
                                    C.c_int, C.c_int, vp]),
+    "emix_adj_create": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(EmixObjective), C.POINTER(vp)]),
+    "emix_adj_destroy": (C.c_int, [vp]),
+    "emix_adj_device_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+    "emix_adj_forward": (C.c_int, [vp, C.POINTER(C.c_double)]),
+    "emix_adj_backward": (C.c_int, [vp, C.POINTER(C.c_double)]),
+    "emix_adj_state_gradient": (C.c_int, [vp, vp, vp]),
+    "emix_ctx_set_forcing": (C.c_int, [vp, C.c_double, C.c_double]),
     "emix_filtrado_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
     "emix_filter_dev": (C.c_int, [vp, C.c_int, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_int, vp]),

@@ -388,6 +388,11 @@ class Context:
             self.upload(workload.um, workload.phi if level_set else None)
 
     @property
+    def shape(self):
+        p = self.params
+        return (p.nz, p.ny, p.nx)
+
+    @property
     def handle(self):
         return self._h
 
@@ -581,3 +586,100 @@ class Batch:
         except Exception:
             pass
 
+
+
+# --------------------------------------------------------------------------
+# gradient of the tank objective (hand-written adjoint of the RK3 step)
+# --------------------------------------------------------------------------
+def tank_objective(workload, r_in=0.2, r_out=0.5, radius=1.0, w_ke=1.0, w_if=1.0):
+    """Kinetic energy in the annulus r_in R <= r <= r_out R plus the smoothed
+    interface area of the level set (delta half-width 1.5 x the largest
+    spacing)."""
+    g = workload.grid
+    dmax = max(g.length[a] * g.h(a) for a in range(3))
+    o = _lib.EmixObjective()
+    o.r_in, o.r_out, o.eps = r_in * radius, r_out * radius, 1.5 * dmax
+    o.w_ke, o.w_if = w_ke, w_if
+    return o
+
+
+class Adjoint:
+    """Forward steps with checkpoints and the reverse sweep (``emix_adj``)."""
+
+    def __init__(self, ctx: "Context", nsteps: int, every: int = 1, objective=None):
+        self.lib = _lib.load()
+        self.ctx = ctx
+        self.objective = objective
+        self._h = C.c_void_p()
+        check(self.lib.emix_adj_create(ctx.handle, nsteps, every, C.byref(objective),
+                                       C.byref(self._h)), "emix_adj_create")
+
+    def forward(self) -> float:
+        J = C.c_double()
+        check(self.lib.emix_adj_forward(self._h, C.byref(J)), "emix_adj_forward")
+        return J.value
+
+    def backward(self):
+        dJ = (C.c_double * 2)()
+        check(self.lib.emix_adj_backward(self._h, dJ), "emix_adj_backward")
+        return dJ[0], dJ[1]
+
+    def state_gradient(self):
+        import torch
+        nz, ny, nx = self.ctx.shape
+        lum = torch.empty((5, nz, ny, nx), dtype=torch.float64, device="cuda")
+        lphi = torch.empty((nz, ny, nx), dtype=torch.float64, device="cuda")
+        check(self.lib.emix_adj_state_gradient(self._h, _ptr(lum), _ptr(lphi)),
+              "emix_adj_state_gradient")
+        return lum, lphi
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        check(self.lib.emix_adj_device_bytes(self._h, C.byref(b)), "emix_adj_device_bytes")
+        return b.value
+
+    def close(self):
+        if self._h:
+            self.lib.emix_adj_destroy(self._h)
+            self._h = C.c_void_p()
+
+
+class TankGradient:
+    """J(omega, Cs) of a tank run as a torch.autograd.Function: the forward
+    runs nsteps RK3 steps from the workload's initial state with the given
+    impeller angular velocity and Smagorinsky constant; the backward is the
+    hand-written adjoint."""
+
+    def __init__(self, workload, nsteps, every=1, objective=None, **ctx_kw):
+        self.workload = workload
+        self.ctx = Context(workload, **ctx_kw)
+        self.adj = Adjoint(self.ctx, nsteps, every, objective or tank_objective(workload))
+
+    def run(self, omega: float, cs: float) -> float:
+        w = self.workload
+        check(self.ctx.lib.emix_ctx_set_forcing(self.ctx.handle, float(omega), float(cs)),
+              "emix_ctx_set_forcing")
+        self.ctx.upload(w.um, w.phi)
+        self.ctx.time = getattr(w, "t0", 0.0)
+        return self.adj.forward()
+
+    def function(self):
+        import torch
+        runner = self
+
+        class _J(torch.autograd.Function):
+            @staticmethod
+            def forward(fctx, theta):
+                J = runner.run(float(theta[0]), float(theta[1]))
+                return torch.tensor(J, dtype=torch.float64)
+
+            @staticmethod
+            def backward(fctx, grad):
+                d = runner.adj.backward()
+                return grad * torch.tensor(d, dtype=torch.float64)
+
+        return _J.apply
+
+    def close(self):
+        self.adj.close()
+        self.ctx.close()

@@ -419,6 +419,45 @@ int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms);
  * device in lane operations per second (a short dependent-chain kernel). */
 int emix_fp64_peak(double *lane_ops_per_s);
 
+/* ========================================================================
+ * Gradient of a tank objective through the RK3 step (hand-written adjoint;
+ * no counterpart in the reference)
+ * ======================================================================== */
+
+/* J = w_ke * sum_{r_in <= r <= r_out} dV |u|^2 / 2
+ *   + w_if * sum dV delta_eps(phi) |grad phi|
+ * over the state after the forward steps; r = sqrt(x^2 + y^2), dV =
+ * jbn(10) hx hy hz, delta_eps the cosine-smoothed delta of half-width eps,
+ * grad phi by central differences (one-sided at the walls) times the diagonal
+ * metric. */
+typedef struct emix_objective {
+    double r_in, r_out, eps, w_ke, w_if;
+} emix_objective;
+
+typedef struct emix_adj emix_adj;
+
+/* An adjoint of `nsteps` steps of ctx with a checkpoint every `every` steps
+ * (1 = every step; larger values trade recomputation for memory).  Covers the
+ * tank step: level set on, Smagorinsky (or no SGS), impeller on, no filter. */
+int emix_adj_create(emix_ctx *ctx, int nsteps, int every, const emix_objective *obj,
+                    emix_adj **adj);
+int emix_adj_destroy(emix_adj *adj);
+int emix_adj_device_bytes(emix_adj *adj, size_t *bytes);
+
+/* Run nsteps from the context's current state, keeping checkpoints; J out. */
+int emix_adj_forward(emix_adj *adj, double *J);
+
+/* Reverse sweep after emix_adj_forward: dJ[0] = dJ/d(impeller omega),
+ * dJ[1] = dJ/dCs.  Leaves the context at the forward pass's final state. */
+int emix_adj_backward(emix_adj *adj, double *dJ);
+
+/* dJ/d(initial um[5]) and dJ/d(initial phi), device pointers (after backward). */
+int emix_adj_state_gradient(emix_adj *adj, double *lum, double *lphi);
+
+/* Change the impeller angular velocity and the Smagorinsky constant of a
+ * context (the plan is rebuilt; captured graphs are dropped). */
+int emix_ctx_set_forcing(emix_ctx *ctx, double omega, double cs);
+
 #ifdef __cplusplus
 }
 #endif

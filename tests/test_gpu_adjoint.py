@@ -51,3 +51,74 @@ def test_deriv_transpose_dot_product(emix, oracle, scheme, axis):
     emix.deriv_t_dev(_dev(y), axis, h, scheme, out=acc)
     assert_close(acc.cpu().numpy(), x + dty, tol=1e-14, what="accumulate")
     torch.cuda.synchronize()
+
+
+def _tank_case(n=20, steps=2):
+    w = F.stirred_tank(n=n, impeller=True, impeller_omega=1.3, height=2.0)
+    # the free surface inside the box so the interface term is active
+    X, Y, Z = w.grid.coords()
+    w.phi = np.ascontiguousarray(Z - 1.0 + 0.05 * np.sin(3 * X) * np.cos(2 * Y))
+    return w
+
+
+def _runner(emix, w, steps, every=1):
+    return emix.TankGradient(w, steps, every, bc_walls=1)
+
+
+@pytest.mark.parametrize("every", [1, 2])
+def test_parameter_gradient_matches_finite_differences(emix, every):
+    w = _tank_case()
+    r = _runner(emix, w, 3, every)
+    om, cs = 1.3, 0.1
+    J = r.run(om, cs)
+    g_om, g_cs = r.adj.backward()
+    assert np.isfinite(J) and J > 0
+    for k, (p0, g) in enumerate(((om, g_om), (cs, g_cs))):
+        h = 1e-6 * max(abs(p0), 1.0)
+        args_p = [om, cs]; args_p[k] = p0 + h
+        args_m = [om, cs]; args_m[k] = p0 - h
+        fd = (r.run(*args_p) - r.run(*args_m)) / (2 * h)
+        assert abs(g - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(J)), (k, g, fd)
+    r.close()
+
+
+def test_state_gradient_matches_directional_derivative(emix):
+    import torch
+    w = _tank_case(18)
+    r = _runner(emix, w, 2)
+    J = r.run(1.3, 0.1)
+    r.adj.backward()
+    lum, lphi = r.adj.state_gradient()
+    lum, lphi = lum.cpu().numpy(), lphi.cpu().numpy()
+    um0, phi0 = w.um.copy(), w.phi.copy()
+    sh = phi0.shape
+    dum = np.stack([1e-2 * F.uniform(93, m, sh) for m in range(5)]) * np.abs(um0).max(axis=(1, 2, 3))[:, None, None, None]
+    dphi = 1e-2 * F.uniform(94, 0, sh)
+    for du, dp in ((dum, 0 * dphi), (0 * dum, dphi)):
+        pred = float((lum * du).sum() + (lphi * dp).sum())
+        eps = 1e-5
+        vals = []
+        for sgn in (1, -1):
+            w.um = np.ascontiguousarray(um0 + sgn * eps * du)
+            w.phi = np.ascontiguousarray(phi0 + sgn * eps * dp)
+            vals.append(r.run(1.3, 0.1))
+        fd = (vals[0] - vals[1]) / (2 * eps)
+        assert abs(pred - fd) <= 1e-6 * max(abs(fd), 1e-6 * abs(J)), (pred, fd)
+    w.um, w.phi = um0, phi0
+    r.close()
+
+
+def test_autograd_function(emix):
+    import torch
+    w = _tank_case(16)
+    r = _runner(emix, w, 2)
+    f = r.function()
+    theta = torch.tensor([1.3, 0.1], dtype=torch.float64, requires_grad=True)
+    J = f(theta)
+    J.backward()
+    g = theta.grad.numpy()
+    J2 = r.run(1.3, 0.1)
+    assert float(J) == J2
+    g2 = r.adj.backward()
+    assert np.allclose(g, g2, rtol=1e-12, atol=0)
+    r.close()
