@@ -32,7 +32,7 @@ class EmixImpeller(C.Structure):
         ("r1", C.c_double), ("r2", C.c_double), ("z1", C.c_double), ("z2", C.c_double),
         ("half_thick", C.c_double), ("hub_r", C.c_double), ("hub_z1", C.c_double),
         ("hub_z2", C.c_double), ("shaft_r", C.c_double), ("shaft_z0", C.c_double),
-        ("shaft_z1", C.c_double),
+        ("shaft_z1", C.c_double), ("interp", C.c_int),
     ]
 
 
@@ -88,6 +88,15 @@ PROTOTYPES = {
     "emix_adj_backward": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "emix_adj_state_gradient": (C.c_int, [vp, vp, vp]),
     "emix_ctx_set_forcing": (C.c_int, [vp, C.c_double, C.c_double]),
+    "emix_reinit_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                  C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, vp]),
+    "emix_write_field": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp]),
+    "emix_read_field": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp]),
+    "emix_write_time": (C.c_int, [C.c_char_p, C.c_double, C.c_int]),
+    "emix_read_time": (C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "emix_write_array": (C.c_int, [C.c_char_p, vp, C.c_long]),
+    "emix_read_array": (C.c_int, [C.c_char_p, vp, C.c_long]),
+    "emix_read_sobject": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, vp]),
     "emix_filtrado_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, vp]),
     "emix_filter_dev": (C.c_int, [vp, C.c_int, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_int, vp]),

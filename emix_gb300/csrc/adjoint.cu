@@ -298,9 +298,10 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     *out = nullptr;
     const emix_params &p = c->p;
     if (!c->static_set || !p.level_set || p.sgs_model == EMIX_SGS_STRUCTURE || !p.imp.on ||
-        p.filter_every != 0 || p.ref_bugs != 0) {
+        p.imp.interp || p.filter_every != 0 || p.ref_bugs != 0) {
         set_last_message("emix_adj_create: the adjoint covers the tank step (level set on, "
-                         "Smagorinsky or no SGS, impeller on, no filter, ref_bugs 0)");
+                         "Smagorinsky or no SGS, impeller on without the blade-edge "
+                         "interpolation, no filter, ref_bugs 0)");
         return EMIX_ERR_ARG;
     }
     emix_adj *a = new (std::nothrow) emix_adj();

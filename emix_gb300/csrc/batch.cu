@@ -396,6 +396,11 @@ int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
     if (!out || !params || ngrid < 1) return EMIX_ERR_ARG;
     *out = nullptr;
     for (int g = 0; g < ngrid; ++g)
+        if (params[g].imp.on && params[g].imp.interp) {
+            set_last_message("emix_batch_create: the impeller's blade-edge interpolation is not batched");
+            return EMIX_ERR_ARG;
+        }
+    for (int g = 0; g < ngrid; ++g)
         if (params[g].filter_every != 0) {
             set_last_message("emix_batch_create: the compact filter is not batched (filter_every must be 0)");
             return EMIX_ERR_ARG;

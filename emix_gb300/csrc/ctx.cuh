@@ -17,6 +17,12 @@ struct emix_ctx {
     double *um0, *um, *u, *pres, *dvel, *vis, *amut, *vort, *flux, *R, *W, *jbn, *jx, *jy, *jz,
         *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB, *wenoC, *wenoE, *xyz, *clock;
     unsigned char *impflag = nullptr;
+    // blade-edge interpolation of the impeller (imp.interp)
+    double *ip_geo = nullptr;
+    unsigned char *ip_status = nullptr;
+    signed char *ip_face = nullptr;
+    int *ip_nb = nullptr, *ip_list = nullptr, *ip_count = nullptr;
+    double rango = 0.0;
     emix::DerivTable T[3];
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;

@@ -121,6 +121,25 @@ EMIX_DEV void imp_clock_tick(const ImpClockArgs &a) {
 
 __global__ void k_imp_clock(ImpClockArgs a);
 
+// the blade-edge interpolation (impeller_interp.cu)
+struct ImpInterpArgs {
+    ImpGeom g;
+    const double *xyz, *clock, *mask;
+    double *out, *u;        // the substep's um output and u output, updated in place
+    int nx, ny, nz;
+    long n;
+    double rango;           // grid diagonal (getInterpolData :357-361)
+    int stage, phase;       // phase 0: geometry, 1: lists, 2: apply
+    unsigned char *status;  // per blade and plane cell
+    signed char *face;
+    double *geo;            // 11 per blade and plane cell: matrix, surface point
+    int *nb;                // 2 per blade and plane cell: neighbour cells
+    int *list, *count;
+};
+__global__ void k_interp_geom(ImpInterpArgs a);
+__global__ void k_interp_list(ImpInterpArgs a);
+__global__ void k_interp_apply(ImpInterpArgs a);
+
 // 1 where some blade angle could put the cell inside the impeller (blade
 // band within reach of a blade corner, hub disc, shaft), 0 elsewhere: the RK
 // kernel tests only flagged cells.  The margin 1e-9 is far above rounding.

@@ -17,7 +17,7 @@ namespace emix {
 
 enum LaunchKind {
     LK_PRIM, LK_PAD, LK_WENO, LK_DERIV_X, LK_DERIV_YZ, LK_SMAG, LK_SF, LK_VORT, LK_SELECT,
-    LK_FLUX, LK_RK, LK_BC, LK_CLOCK, LK_COUNT
+    LK_FLUX, LK_RK, LK_BC, LK_CLOCK, LK_INTERP, LK_COUNT
 };
 
 // profile classes (emix_ctx_profile)
@@ -48,6 +48,7 @@ struct Launch {
         RkArgs rk;
         BcArgs bc;
         ImpClockArgs clock;
+        ImpInterpArgs interp;
     };
 };
 

@@ -1,0 +1,149 @@
+// reinit.cu -- Sussman reinitialisation of the level set, the device form of
+// cuReinitLsJB (src/LevelSet/lsTransportEc.cu:420-676) with the right-hand
+// side reini_RS_WENOJB (src/LevelSet/lsTools.cu:824-902):
+//
+//   per iteration: mirror the ghost layers of phi, phi0 = phi, then three
+//   TVD-RK3 stages of  d(phi)/dtau = -S(phi0) (|grad phi| - 1),
+//   S = phi0 / sqrt(phi0^2 + dmin^2),  dtau = deltamin / 2,
+//   |grad phi| by the Godunov upwinding of the left- and right-biased WENO5
+//   derivatives (PhiDevPlus/MinusParameterJB, lsTools.cu:587-770).
+//
+// One fused kernel per stage: both WENO5 reconstructions of each direction,
+// the Godunov combination, the speed and the stage update; stages ping-pong
+// between two scratch fields so that stencil reads never meet a write.
+#include "weno.cuh"
+
+namespace emix {
+
+namespace {
+
+struct ReinitArgs {
+    const double *src;    // field the derivatives are taken of
+    const double *phi;    // iteration start (the TVD combination's phi_n)
+    const double *phi0;   // sign field
+    const double *jbn;    // padded, 11 components (1, 5, 9 read)
+    const double *dmins;  // padded smoothing widths
+    double *out;
+    int nxg, nyg, nzg;
+    double sx, sy, sz, dt;
+    int stage, ref_bugs;
+};
+
+EMIX_DEV double bd(const double *f, long base, long s, int p) {
+    return p == 0 ? f[base + s] - f[base] : f[base + p * s] - f[base + (p - 1) * s];
+}
+
+__global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
+    const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
+    const long sxy = (long)nxg * nyg, ng = sxy * nzg;
+    for (long id = blockIdx.x * (long)blockDim.x + threadIdx.x; id < ng; id += (long)gridDim.x * blockDim.x) {
+        const int c3[3] = {(int)(id % nxg), (int)((id / nxg) % nyg), (int)(id / sxy)};
+        const int L3[3] = {nxg, nyg, nzg};
+        const long s3[3] = {1, nxg, sxy};
+        const double sc[3] = {a.sx, a.sy, a.sz};
+        const double p0 = a.phi0[id];
+        const double ta = (double)(p0 > 0.0) - (double)(p0 < 0.0);
+        double r = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double C = sc[d] * a.jbn[4 * d * ng + id];
+            const double eps = kWenoEps4 / (C * C);
+            const long base = id - c3[d] * s3[d];
+            int p[5];
+            // left-biased (phi^-)
+            stencil_left(c3[d], L3[d], p);
+            double v5 = bd(a.src, base, s3[d], p[4]);
+            if (d == 2 && a.ref_bugs && c3[2] == nzg - 1) {
+                // lsTools.cu:636: id_kp2 = id_jm1 at the top layer
+                const long ib = c3[1] == 0 ? id : id - nxg;
+                v5 = a.src[ib] - a.src[ib - sxy];
+            }
+            const double am = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
+                                        bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]), v5, eps);
+            // right-biased (phi^+)
+            stencil_right(c3[d], L3[d], p);
+            const double bp = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
+                                        bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]),
+                                        bd(a.src, base, s3[d], p[4]), eps);
+            double pmax = fmax(am, 0.0) * fmax(am, 0.0), pmin = fmin(bp, 0.0) * fmin(bp, 0.0);
+            double rd = 0.5 * (ta + 1.0) * fmax(pmax, pmin);
+            pmax = fmax(bp, 0.0) * fmax(bp, 0.0);
+            pmin = fmin(am, 0.0) * fmin(am, 0.0);
+            rd += 0.5 * fabs(ta - 1.0) * fmax(pmax, pmin);
+            r += rd;
+        }
+        const double dm = a.dmins[id];
+        const double rs = (p0 / sqrt(p0 * p0 + dm * dm)) * (sqrt(r) - 1.0);
+        const double t = a.src[id] - a.dt * rs;
+        double o;
+        if (a.stage == 1) o = t;
+        else if (a.stage == 2) o = 0.75 * a.phi[id] + 0.25 * t;
+        else o = (a.phi[id] + 2.0 * t) / 3.0;
+        a.out[id] = o;
+    }
+}
+
+// ghost layers of a padded field from its own interior (mirror images)
+__global__ void k_mirror_inplace(double *f, int g, int nx, int ny, int nz) {
+    const int nxg = nx + 2 * g, nyg = ny + 2 * g, nzg = nz + 2 * g;
+    const long ng = (long)nxg * nyg * nzg;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < ng; q += (long)gridDim.x * blockDim.x) {
+        const int X = (int)(q % nxg), Y = (int)((q / nxg) % nyg), Z = (int)(q / ((long)nxg * nyg));
+        if (X >= g && X < nx + g && Y >= g && Y < ny + g && Z >= g && Z < nz + g) continue;
+        const long src = (mirror(X, g, nx) + g) + (long)nxg * ((mirror(Y, g, ny) + g) + (long)nyg * (mirror(Z, g, nz) + g));
+        f[q] = f[src];
+    }
+}
+
+int grid_r(long n) {
+    long b = (n + 255) / 256;
+    if (b > 152L * 8) b = 152L * 8;
+    return (int)(b < 1 ? 1 : b);
+}
+
+} // namespace
+
+int reinit_impl(double *phi, const double *jbn, const double *dmins, double dX, double dY, double dZ,
+                int nxg, int nyg, int nzg, int g, double deltamin, int iters, int ref_bugs,
+                cudaStream_t st) {
+    const long ng = (long)nxg * nyg * nzg;
+    double *scr;
+    int rc = device_scratch((size_t)3 * ng * sizeof(double), &scr);
+    if (rc) return rc;
+    double *phi0 = scr, *A = scr + ng, *B = scr + 2 * ng;
+    const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
+    ReinitArgs a{};
+    a.phi = phi; a.phi0 = phi0; a.jbn = jbn; a.dmins = dmins;
+    a.nxg = nxg; a.nyg = nyg; a.nzg = nzg;
+    a.sx = 1.0 / dX; a.sy = 1.0 / dY; a.sz = 1.0 / dZ; a.dt = 0.5 * deltamin; a.ref_bugs = ref_bugs;
+    for (int it = 0; it < iters; ++it) {
+        if (g > 0) k_mirror_inplace<<<grid_r(ng), 256, 0, st>>>(phi, g, nx, ny, nz);
+        EMIX_CUDA_TRY(cudaMemcpyAsync(phi0, phi, ng * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        a.src = phi; a.out = A; a.stage = 1;
+        k_reinit_stage<<<grid_r(ng), 256, 0, st>>>(a);
+        a.src = A; a.out = B; a.stage = 2;
+        k_reinit_stage<<<grid_r(ng), 256, 0, st>>>(a);
+        a.src = B; a.out = phi; a.stage = 3;
+        k_reinit_stage<<<grid_r(ng), 256, 0, st>>>(a);
+    }
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
+
+} // namespace emix
+
+using namespace emix;
+
+extern "C" {
+
+int emix_reinit_dev(double *phi, const double *jbn, const double *dmins, double deltaX, double deltaY,
+                    double deltaZ, int nxg, int nyg, int nzg, int gcells, double deltamin, int iters,
+                    int ref_bugs, void *stream) {
+    if (!phi || !jbn || !dmins || gcells < 0 || nxg - 2 * gcells < 1 || nyg - 2 * gcells < 1 ||
+        nzg - 2 * gcells < 1 || nxg < 4 || nyg < 4 || nzg < 4 || iters < 0 || !(deltaX > 0) ||
+        !(deltaY > 0) || !(deltaZ > 0) || (ref_bugs != 0 && ref_bugs != 1))
+        return EMIX_ERR_ARG;
+    return reinit_impl(phi, jbn, dmins, deltaX, deltaY, deltaZ, nxg, nyg, nzg, gcells, deltamin, iters,
+                       ref_bugs, (cudaStream_t)stream);
+}
+
+} // extern "C"

@@ -74,6 +74,14 @@ int launch_single(const Launch &L, cudaStream_t st) {
     case LK_CLOCK:
         k_imp_clock<<<1, 32, 0, st>>>(L.clock);
         break;
+    case LK_INTERP:
+        if (L.interp.phase == 0)
+            k_interp_geom<<<cells_grid((long)L.interp.g.nblades * L.interp.nx * L.interp.ny), 256, 0, st>>>(L.interp);
+        else if (L.interp.phase == 1)
+            k_interp_list<<<L.interp.g.nblades, 1024, 0, st>>>(L.interp);
+        else
+            k_interp_apply<<<(L.interp.nz + 63) / 64, 64, 0, st>>>(L.interp);
+        break;
     default:
         return EMIX_ERR_ARG;
     }
@@ -260,6 +268,20 @@ void build_plan(emix_ctx *c) {
                 P.push_back(F);
             }
             P.push_back(L);
+            if (ig.on && p.imp.interp) {
+                // the blade-edge interpolation of rushton(s) on the substep's output
+                Launch I = make(LK_INTERP, CLS_RK);
+                ImpInterpArgs &ia = I.interp;
+                ia.g = ig; ia.xyz = c->xyz; ia.clock = c->clock; ia.mask = c->mask;
+                ia.out = ra.out; ia.u = c->u; ia.nx = nx; ia.ny = ny; ia.nz = nz; ia.n = n;
+                ia.rango = c->rango; ia.stage = s;
+                ia.status = c->ip_status; ia.face = c->ip_face; ia.geo = c->ip_geo; ia.nb = c->ip_nb;
+                ia.list = c->ip_list; ia.count = c->ip_count;
+                for (int ph = 0; ph < 3; ++ph) {
+                    ia.phase = ph;
+                    P.push_back(I);
+                }
+            }
         }
     }
 }
@@ -287,6 +309,7 @@ bool params_ok(const emix_params *p) {
     if (p->bc_walls != 0 && p->bc_walls != 1) return false;
     if (p->filter_every < 0 || (p->filter_every > 0 && (p->nx < 11 || p->ny < 11 || p->nz < 11)))
         return false;
+    if (p->imp.on && p->imp.interp != 0 && p->imp.interp != 1) return false;
     if ((p->imp.on != 0 && p->imp.on != 1) ||
         (p->imp.on && (p->imp.nblades < 0 || p->imp.nblades > kImpMaxBlades)))
         return false;
@@ -372,8 +395,10 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     const long nfield = 5 + 5 + 3 + 1 + 9 + 1 + 15 + 5 + 5 + 11 + 3 + 1 + 1 + (p->level_set ? 7 : 0) +
                         (sf ? 1 + 3 + 6 : 0);
     const bool imp = p->imp.on != 0;
+    const long nb2 = imp && p->imp.interp ? (long)p->imp.nblades * p->nx * p->ny : 0;
+    const size_t ip_words = nb2 ? 11 * nb2 + 2 * ((nb2 + 7) / 8) + nb2 + (nb2 + 1) / 2 + kImpMaxBlades : 0;
     const size_t bytes = ((size_t)(nfield + (imp ? 3 : 0)) * n + 3 * (size_t)ng +
-                          (imp ? kImpClockLen + (n + 7) / 8 : 0)) * sizeof(double);
+                          (imp ? kImpClockLen + (n + 7) / 8 : 0) + ip_words) * sizeof(double);
     if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
         cudaGetLastError();
         set_last_message("cudaMalloc of the context arena failed");
@@ -399,6 +424,15 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     c->xyz = imp ? take(3 * n) : nullptr;
     c->clock = imp ? take(kImpClockLen) : nullptr;
     c->impflag = imp ? reinterpret_cast<unsigned char *>(take((n + 7) / 8)) : nullptr;
+    if (imp && p->imp.interp) {
+        const long nb2 = (long)p->imp.nblades * p->nx * p->ny;
+        c->ip_geo = take(11 * nb2);
+        c->ip_status = reinterpret_cast<unsigned char *>(take((nb2 + 7) / 8));
+        c->ip_face = reinterpret_cast<signed char *>(take((nb2 + 7) / 8));
+        c->ip_nb = reinterpret_cast<int *>(take(nb2));
+        c->ip_list = reinterpret_cast<int *>(take((nb2 + 1) / 2));
+        c->ip_count = reinterpret_cast<int *>(take(kImpMaxBlades));
+    }
     if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(c->arena);
@@ -460,6 +494,16 @@ int emix_ctx_set_static(emix_ctx *c, const double *jbn, const double *mask, cons
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->mask, mask, n * sizeof(double), cudaMemcpyHostToDevice, st));
     // coordinates go through the flux buffer (free at this point)
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->flux, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (c->xyz && p.imp.interp) {
+        // grid diagonal of getInterpolData (rush_ruth_me.f90:357-361)
+        const int nx = p.nx, ny = p.ny, nz = p.nz;
+        const long nxy = (long)nx * ny;
+        const double dx = (xyz[nx - 1] - xyz[0]) / (double)(nx - 1);
+        const double dy = (xyz[n + (long)nx * (ny - 1)] - xyz[n]) / (double)(ny - 1);
+        const double dz = (xyz[2 * n + nxy * (nz - 1)] - xyz[2 * n]) / (double)(nz - 1);
+        c->rango = sqrt(dx * dx + dy * dy + dz * dz);
+        ctx_rebuild_plan(c);
+    }
     if (c->xyz) {
         EMIX_CUDA_TRY(cudaMemcpyAsync(c->xyz, c->flux, 3 * n * sizeof(double), cudaMemcpyDeviceToDevice, st));
         const ImpGeom ig{p.imp.on, p.imp.nblades, p.imp.omega, p.imp.theta0, p.imp.r1, p.imp.r2,

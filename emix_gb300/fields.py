@@ -122,6 +122,7 @@ class Impeller:
     shaft_r: float = 0.0264
     shaft_z0: float = 0.6667
     shaft_z1: float = 5.0
+    interp: int = 0          # 1: the blade-edge interpolation of the velocity as well
 
 
 def tank_impeller(grid: "Grid", radius=1.0, height=2.0, omega=1.0, nblades=6, z_frac=1.0 / 3.0,

@@ -252,6 +252,15 @@ def deriv_t_dev(y, axis: int, h: float, scheme=SCHEME_C, out=None):
     return out
 
 
+def reinit_dev(phi, jbn, dmins, delta, g, deltamin, iters=10, ref_bugs=0):
+    """Sussman reinitialisation (cuReinitLsJB) of a padded level set, in place."""
+    lib = _lib.load()
+    nx, ny, nz = _dims(phi)
+    check(lib.emix_reinit_dev(_ptr(phi), _ptr(jbn), _ptr(dmins), delta[0], delta[1], delta[2],
+                              nx, ny, nz, g, deltamin, iters, ref_bugs, _stream()), "emix_reinit_dev")
+    return phi
+
+
 def filtrado_dev(um, jbn, cfilt):
     """filtrado (x, y, z compact filter of the 5 fields) in place on device tensors."""
     lib = _lib.load()
@@ -683,3 +692,54 @@ class TankGradient:
     def close(self):
         self.adj.close()
         self.ctx.close()
+
+
+# --------------------------------------------------------------------------
+# the reference's checkpoint files (GRAVA / leer_campos)
+# --------------------------------------------------------------------------
+def _primitive(um, mach):
+    r = um[0]
+    u = np.ascontiguousarray(um[1:4] / r)
+    return u, np.ascontiguousarray(um[4]), np.ascontiguousarray(r / (mach * mach))
+
+
+def write_checkpoint(directory, serie, sample, um, mach, dto, it, impellermask=None, nd=5):
+    """GRAVA's files for the state um (5 conserved fields): field_SS.NNN with
+    u, v, w, temp, pres (varc_to_varnc), time_SS.NNN and, when given,
+    impellermask_SS.NNN.  Returns the field file's path."""
+    import os
+    lib = _lib.load()
+    nz, ny, nx = um.shape[-3:]
+    u, temp, pres = _primitive(np.asarray(um, dtype=np.float64), mach)
+    tag = f"{serie:02d}.{sample:03d}"
+    fpath = os.path.join(directory, f"field_{tag}")
+    check(lib.emix_write_field(fpath.encode(), nd, nx, ny, nz, _ptr(u), _ptr(temp), _ptr(pres)),
+          "emix_write_field")
+    check(lib.emix_write_time(os.path.join(directory, f"time_{tag}").encode(), float(dto), int(it)),
+          "emix_write_time")
+    if impellermask is not None:
+        m = np.ascontiguousarray(impellermask, dtype=np.float64)
+        check(lib.emix_write_array(os.path.join(directory, f"impellermask_{tag}").encode(), _ptr(m),
+                                   m.size), "emix_write_array")
+    return fpath
+
+
+def read_field(path, shape, mach, nd=5):
+    """leer_campos: the field file at `path` for a grid of shape (nz, ny, nx),
+    converted back to the conserved state (varnc_to_varc)."""
+    lib = _lib.load()
+    nz, ny, nx = shape
+    u = np.empty((3, nz, ny, nx))
+    temp = np.empty((nz, ny, nx))
+    pres = np.empty((nz, ny, nx))
+    check(lib.emix_read_field(str(path).encode(), nd, nx, ny, nz, _ptr(u), _ptr(temp), _ptr(pres)),
+          "emix_read_field")
+    r = pres * mach * mach
+    return np.stack([r, u[0] * r, u[1] * r, u[2] * r, temp])
+
+
+def read_time(path):
+    lib = _lib.load()
+    d, i = C.c_double(), C.c_int()
+    check(lib.emix_read_time(str(path).encode(), C.byref(d), C.byref(i)), "emix_read_time")
+    return d.value, i.value

@@ -19,11 +19,24 @@ def main(argv=None):
     ap.add_argument("--no-level-set", action="store_true")
     ap.add_argument("--walls", action="store_true", help="frontera wall conditions every substep")
     ap.add_argument("--impeller", action="store_true", help="rotating impeller forcing (tank)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="forward + reverse sweep of the tank objective (implies --impeller --walls)")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
     from . import fields as F
     from . import ops
+    if a.adjoint:
+        w = F.stirred_tank(n=a.n, impeller=True)
+        r = ops.TankGradient(w, a.steps, 1, bc_walls=1)
+        t0 = time.perf_counter()
+        J = r.run(w.impeller.omega, w.cs)
+        g = r.adj.backward()
+        torch.cuda.synchronize()
+        print(f"{w.name}: J={J:.12g} dJ/domega={g[0]:.6g} dJ/dCs={g[1]:.6g} "
+              f"in {time.perf_counter() - t0:.3f} s")
+        r.close()
+        return 0
     w = F.stirred_tank(n=a.n, impeller=a.impeller) if a.workload == "tank" else F.taylor_green(n=a.n)
     ctx = ops.Context(w, level_set=not a.no_level_set, bc_walls=int(a.walls))
     t0 = time.perf_counter()

@@ -228,6 +228,18 @@ int emix_extrapolate_dev(double *ext, const double *phiS, const double *jbn,
 int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
                      int nx, int ny, int nz, int accumulate, void *stream);
 
+/* Sussman reinitialisation of a padded level set: the device form of
+ * cuReinitLsJB (src/LevelSet/lsTransportEc.cu:420-676, with
+ * reini_RS_WENOJB, src/LevelSet/lsTools.cu:824-902).  phi (in/out), jbn
+ * (11 components) and dmins are arrays of the padded grid nxg x nyg x nzg with
+ * gcells ghost layers, mirrored at the start of every iteration; iters
+ * iterations (10 in the reference) of three TVD-RK3 stages of deltamin/2; the
+ * kernels use 1/deltaX.  ref_bugs keeps the z-top index of
+ * PhiDevPlusParameterJB.  Uses the library's per-device scratch. */
+int emix_reinit_dev(double *phi, const double *jbn, const double *dmins, double deltaX, double deltaY,
+                    double deltaZ, int nxg, int nyg, int nzg, int gcells, double deltamin, int iters,
+                    int ref_bugs, void *stream);
+
 /* ========================================================================
  * Compact filter
  * ======================================================================== */
@@ -293,6 +305,8 @@ typedef struct emix_impeller {
     double r1, r2, z1, z2, half_thick;
     double hub_r, hub_z1, hub_z2;
     double shaft_r, shaft_z0, shaft_z1;
+    int interp;         /* 1: also the blade-edge interpolation of the velocity
+                           (rush_ruth_me.f90:97-185 with getInterpolData)       */
 } emix_impeller;
 
 typedef struct emix_params {
@@ -457,6 +471,28 @@ int emix_adj_state_gradient(emix_adj *adj, double *lum, double *lphi);
 /* Change the impeller angular velocity and the Smagorinsky constant of a
  * context (the plan is rebuilt; captured graphs are dropped). */
 int emix_ctx_set_forcing(emix_ctx *ctx, double omega, double cs);
+
+/* ========================================================================
+ * Checkpoint files of the reference (Fortran unformatted sequential records:
+ * 4-byte length markers around each record, 4-byte integers, 8-byte reals;
+ * records of 2^31 bytes or more as signed subrecords).  Host buffers.
+ * ======================================================================== */
+
+/* field_SS.NNN of GRAVA (solver/gravar_incomp.f90:19-34): nd | nx ny nz |
+ * u | v | w | temp | pres; u holds the three velocity fields. */
+int emix_write_field(const char *path, int nd, int nx, int ny, int nz, const double *u,
+                     const double *temp, const double *pres);
+/* leer_campos (solver/leer_incomp.f90:65-95): fails on a different nd or size. */
+int emix_read_field(const char *path, int nd, int nx, int ny, int nz, double *u, double *temp,
+                    double *pres);
+/* time_SS.NNN: dto, it (gravar_incomp.f90:36-40). */
+int emix_write_time(const char *path, double dto, int it);
+int emix_read_time(const char *path, double *dto, int *it);
+/* One record of n reals (impellermask_SS.NNN, gravar_incomp.f90:42-46). */
+int emix_write_array(const char *path, const double *a, long n);
+int emix_read_array(const char *path, double *a, long n);
+/* sobject.field: nx ny nz | sobject (leer_incomp.f90:99-106). */
+int emix_read_sobject(const char *path, int nx, int ny, int nz, double *sobject);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,7 @@
  */
 #include "oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -955,6 +956,112 @@ static void impeller_velocity(double omega, double x, double y, double *ue, doub
     *ve = omega * radio * std::cos(th);
 }
 
+/* The blade-edge interpolation of rushton (rush_ruth_me.f90:97-185) with
+ * getInterpolData (:302-517) and getMatrix (:243-299), blade by blade: the
+ * cells next to a blade in the (x, y) plane of the first z layer take, in
+ * the blade band, the velocity of the plane through the blade-surface point
+ * (rigid rotation there) and two neighbour cells on the outer side; cells are
+ * visited in the reference's k, j, i order, so a cell may read a neighbour
+ * updated before it.  The interpolated mask of :116-128 only feeds the
+ * impellermask output and is left out. */
+static void impeller_interp(double *um, const double *xyz, const orc_impeller *imp, double t,
+                            int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+    const double *X = xyz, *Y = xyz + n, *Z = xyz + 2 * n;
+    const double dx = (X[lin(nx - 1, 0, 0, nx, ny)] - X[lin(0, 0, 0, nx, ny)]) / (double)(nx - 1);
+    const double dy = (Y[lin(0, ny - 1, 0, nx, ny)] - Y[lin(0, 0, 0, nx, ny)]) / (double)(ny - 1);
+    const double dz = (Z[lin(0, 0, nz - 1, nx, ny)] - Z[lin(0, 0, 0, nx, ny)]) / (double)(nz - 1);
+    const double rango = std::sqrt(dx * dx + dy * dy + dz * dz);
+    const double two_pi = 2.0 * 3.14159265358979323846, pi = 2.0 * std::acos(0.0);
+    const size_t n2 = (size_t)nx * ny;
+    std::vector<double> m2(n2), M(9 * n2), P1(2 * n2);
+    std::vector<int> flag(n2), i1(n2), j1(n2), i2(n2), j2(n2);
+    for (int b = 0; b < imp->nblades; ++b) {
+        const double th = imp->theta0 + imp->omega * t + b * (two_pi / imp->nblades);
+        const double c = std::cos(th), sn = std::sin(th);
+        const double A[4] = {0.0 * c - 1.0 * sn, 0.0 * c - (-1.0) * sn, 1.0 * c - 0.0 * sn, -1.0 * c - 0.0 * sn};
+        const double B[4] = {0.0 * sn + 1.0 * c, 0.0 * sn + (-1.0) * c, 1.0 * sn + 0.0 * c, -1.0 * sn + 0.0 * c};
+        const double D[4] = {-imp->half_thick, -imp->half_thick, -imp->r2, imp->r1};
+        auto plane = [&](int q, double x, double y) { return A[q] * x + B[q] * y + D[q]; };
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t id = lin(i, j, 0, nx, ny);
+                bool in = true;
+                for (int q = 0; q < 4; ++q) in = in && plane(q, X[id], Y[id]) <= 0.0;
+                m2[j * nx + i] = in ? 0.0 : 1.0;
+                flag[j * nx + i] = 1;
+            }
+        for (int j = 1; j < ny - 1; ++j)
+            for (int i = 1; i < nx - 1; ++i) {
+                const size_t q = (size_t)j * nx + i;
+                if (m2[q] == 1.0 && (m2[q + 1] == 0.0 || m2[q - 1] == 0.0 || m2[q + nx] == 0.0 ||
+                                     m2[q - nx] == 0.0))
+                    flag[q] = -1;
+            }
+        double Ag = 0.0, Bg = 0.0, Dg = 0.0;
+        bool have = false;
+        for (int j = 1; j < ny - 1; ++j)
+            for (int i = 1; i < nx - 1; ++i) {
+                const size_t q = (size_t)j * nx + i;
+                if (flag[q] != -1) continue;
+                const size_t id = lin(i, j, 0, nx, ny);
+                const double x = X[id], y = Y[id];
+                for (int pq = 0; pq < 4; ++pq) {
+                    const double v = plane(pq, x, y);
+                    if (v >= 0.0 && v <= rango) { Ag = A[pq]; Bg = B[pq]; Dg = D[pq]; have = true; break; }
+                }
+                if (!have) { flag[q] = 1; continue; }   /* no plane yet: left alone */
+                const double tt = -(Dg + x * Ag + y * Bg) / (Ag * Ag + Bg * Bg);
+                const double angle = std::acos(Ag) / std::sqrt(Ag * Ag + Bg * Bg);
+                const int sA = Ag >= 0.0 ? 1 : -1, sB = Bg >= 0.0 ? 1 : -1;
+                int a1i, a1j, a2i, a2j;
+                if ((angle >= pi / 6.0 && angle <= pi / 3.0) || (angle >= 2.0 * pi / 3.0 && angle <= 5.0 * pi / 6.0)) {
+                    a1i = i + sA; a1j = j; a2i = i; a2j = j + sB;
+                } else if (angle <= pi / 6.0 || angle >= 5.0 * pi / 6.0) {
+                    a1i = i + sA; a1j = j; a2i = i + sA; a2j = j + sB;
+                } else {
+                    a1i = i; a1j = j + sB; a2i = i + sA; a2j = j + sB;
+                }
+                i1[q] = a1i; j1[q] = a1j; i2[q] = a2i; j2[q] = a2j;
+                const double p1x = x + tt * Ag, p1y = y + tt * Bg;
+                const size_t e1 = lin(a1i, a1j, 0, nx, ny), e2 = lin(a2i, a2j, 0, nx, ny);
+                const double p2x = X[e1], p2y = Y[e1], p3x = X[e2], p3y = Y[e2];
+                P1[2 * q] = p1x; P1[2 * q + 1] = p1y;
+                /* getMatrix (:262-296) */
+                const double det = p2x * p3y - p3x * p2y + p1x * p2y - p1x * p3y + p3x * p1y - p2x * p1y;
+                double *m = &M[9 * q];
+                m[0] = (p2x * p3y - p3x * p2y) / det;
+                m[1] = (p3x * p1y - p1x * p3y) / det;
+                m[2] = (p1x * p2y - p2x * p1y) / det;
+                m[3] = (p2y - p3y) / det;
+                m[4] = (p3y - p1y) / det;
+                m[5] = (p1y - p2y) / det;
+                m[6] = (p3x - p2x) / det;
+                m[7] = (p1x - p3x) / det;
+                m[8] = (p2x - p1x) / det;
+            }
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const size_t q = (size_t)j * nx + i;
+                    const size_t id = lin(i, j, k, nx, ny);
+                    if (flag[q] != -1 || !(Z[id] >= imp->z1 && Z[id] <= imp->z2)) continue;
+                    double ux, vy;
+                    impeller_velocity(imp->omega, P1[2 * q], P1[2 * q + 1], &ux, &vy);
+                    const size_t e1 = lin(i1[q], j1[q], k, nx, ny), e2 = lin(i2[q], j2[q], k, nx, ny);
+                    const double *m = &M[9 * q];
+                    for (int d = 1; d <= 2; ++d) {
+                        const double ub = d == 1 ? ux : vy;
+                        const double ua = um[d * n + e1] / um[e1], uc = um[d * n + e2] / um[e2];
+                        const double cb1 = m[0] * ub + m[1] * ua + m[2] * uc;
+                        const double cb2 = m[3] * ub + m[4] * ua + m[5] * uc;
+                        const double cb3 = m[6] * ub + m[7] * ua + m[8] * uc;
+                        um[d * n + id] = (cb1 + X[id] * cb2 + Y[id] * cb3) * um[id];
+                    }
+                }
+    }
+}
+
 int orc_impeller_force(double *um, const double *xyz, const orc_impeller *imp, double t,
                        int nx, int ny, int nz, double *mask_out) {
     const size_t n = (size_t)nx * ny * nz;
@@ -969,6 +1076,63 @@ int orc_impeller_force(double *um, const double *xyz, const orc_impeller *imp, d
         um[2 * n + q] = ((1.0 - m) * ve + m * (um[2 * n + q] / r)) * r;
         um[3 * n + q] = m * um[3 * n + q];
         if (mask_out) mask_out[q] = m;
+    }
+    if (imp->interp) impeller_interp(um, xyz, imp, t, nx, ny, nz);
+    return 0;
+}
+
+/* reini_RS_WENOJB (src/LevelSet/lsTools.cu:824-902): the Godunov
+ * approximation of |grad phi| from the left-biased (pp) and right-biased (pm)
+ * WENO5 derivatives, upwinded by the sign of phi0, and
+ * rs = S(phi0) (|grad phi| - 1) with S = phi0 / sqrt(phi0^2 + dmin^2). */
+static void reini_rs(double *rs, const double *pp, const double *pm, const double *phi0,
+                     const double *dmins, size_t n) {
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < (long)n; ++q) {
+        const size_t id = (size_t)q;
+        const double ta = (double)(phi0[id] > 0.0) - (double)(phi0[id] < 0.0);
+        double r[3];
+        for (int d = 0; d < 3; ++d) {
+            const double a = pp[id + d * n], b = pm[id + d * n];
+            double pmax = std::max(a, 0.0) * std::max(a, 0.0);
+            double pmin = std::min(b, 0.0) * std::min(b, 0.0);
+            r[d] = 0.5 * (ta + 1.0) * std::max(pmax, pmin);
+            pmax = std::max(b, 0.0) * std::max(b, 0.0);
+            pmin = std::min(a, 0.0) * std::min(a, 0.0);
+            r[d] += 0.5 * std::fabs(ta - 1.0) * std::max(pmax, pmin);
+        }
+        const double grad = std::sqrt(r[0] + r[1] + r[2]);
+        const double so = phi0[id] / std::sqrt(phi0[id] * phi0[id] + dmins[id] * dmins[id]);
+        rs[id] = 1.0 * so * (grad - 1.0);
+    }
+}
+
+int orc_reinit(double *phi, const double *jbn, const double *dmins, double dX, double dY, double dZ,
+               int nxg, int nyg, int nzg, int g, double deltamin, int iters, int ref_bugs) {
+    /* cuReinitLsJB (src/LevelSet/lsTransportEc.cu:420-676): on the padded
+     * grid, per iteration: mirror the ghost layers, phi0 = phi, then three
+     * TVD-RK3 stages of d(phi)/dtau = -S(phi0)(|grad phi| - 1) with
+     * dtau = deltamin/2; the kernels get 1/deltaX as their scale. */
+    const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
+    if (nx < 1 || ny < 1 || nz < 1 || nxg < 4 || nyg < 4 || nzg < 4 || iters < 0) return 1;
+    const size_t n = (size_t)nxg * nyg * nzg;
+    const double dt = 0.5 * deltamin;
+    std::vector<double> d(3 * n), pp(3 * n), pm(3 * n), rs(n), phi0(n), tmp(n);
+    auto rhs = [&](const double *f) {
+        dev1_downwind(d.data(), f, 1.0 / dX, 1.0 / dY, 1.0 / dZ, nxg, nyg, nzg);
+        weno_plus(pp.data(), d.data(), jbn, nxg, nyg, nzg, ref_bugs);
+        weno_minus(pm.data(), d.data(), jbn, nxg, nyg, nzg);
+        reini_rs(rs.data(), pp.data(), pm.data(), phi0.data(), dmins, n);
+    };
+    for (int it = 0; it < iters; ++it) {
+        orc_mirror_ghost(phi, g, nx, ny, nz, 1.0);
+        std::memcpy(phi0.data(), phi, n * sizeof(double));
+        rhs(phi);
+        for (size_t q = 0; q < n; ++q) tmp[q] = phi[q] - dt * rs[q];
+        rhs(tmp.data());
+        for (size_t q = 0; q < n; ++q) tmp[q] = 0.75 * phi[q] + 0.25 * (tmp[q] - dt * rs[q]);
+        rhs(tmp.data());
+        for (size_t q = 0; q < n; ++q) phi[q] = (phi[q] + 2.0 * (tmp[q] - dt * rs[q])) / 3.0;
     }
     return 0;
 }

@@ -117,6 +117,7 @@ typedef struct {
     double r1, r2, z1, z2, half_thick;
     double hub_r, hub_z1, hub_z2;
     double shaft_r, shaft_z0, shaft_z1;
+    int interp;           /* 1: also the blade-edge interpolation (:97-185, getInterpolData) */
 } orc_impeller;
 
 /* Parameters of one RK3 step (solver/rungek_ico.f90:61-313). */
@@ -190,6 +191,14 @@ int orc_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, in
  * mask_out (may be NULL) receives the impeller mask. */
 int orc_impeller_force(double *um, const double *xyz, const orc_impeller *imp, double t,
                        int nx, int ny, int nz, double *mask_out);
+
+/* cuReinitLsJB (src/LevelSet/lsTransportEc.cu:420-676): `iters` Sussman
+ * reinitialisation iterations of the padded level set phi (in/out) with the
+ * padded metric jbn (11 components), per-cell smoothing widths dmins, ghost
+ * width g, pseudo time step deltamin/2; ref_bugs keeps the z-top index of
+ * PhiDevPlusParameterJB. */
+int orc_reinit(double *phi, const double *jbn, const double *dmins, double dX, double dY, double dZ,
+               int nxg, int nyg, int nzg, int g, double deltamin, int iters, int ref_bugs);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

@@ -26,7 +26,7 @@ class Impeller(C.Structure):
         ("r1", C.c_double), ("r2", C.c_double), ("z1", C.c_double), ("z2", C.c_double),
         ("half_thick", C.c_double), ("hub_r", C.c_double), ("hub_z1", C.c_double),
         ("hub_z2", C.c_double), ("shaft_r", C.c_double), ("shaft_z0", C.c_double),
-        ("shaft_z1", C.c_double),
+        ("shaft_z1", C.c_double), ("interp", C.c_int),
     ]
 
 
@@ -87,6 +87,8 @@ def load():
         "orc_filtronper": [C.c_int, vp, C.c_double, C.c_int],
         "orc_impeller_force": [vp, vp, C.POINTER(Impeller), C.c_double, C.c_int, C.c_int, C.c_int, vp],
         "orc_filtrado": [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int],
+        "orc_reinit": [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                       C.c_int, C.c_double, C.c_int, C.c_int],
         "orc_set_threads": [C.c_int],
         "orc_get_threads": [],
     }
@@ -256,6 +258,16 @@ def advect_extrapolate(press, jbn, sobject, delta, deltamin):
     _ok(load().orc_advect_extrapolate(_p(press), _p(c(jbn)), _p(c(sobject)), delta[0], delta[1],
                                       delta[2], nx, ny, nz, deltamin), "orc_advect_extrapolate")
     return press
+
+
+def reinit(phi, jbn, dmins, delta, g, deltamin, iters=10, ref_bugs=0):
+    """cuReinitLsJB on padded arrays; returns the reinitialised phi."""
+    phi = np.array(phi, dtype=np.float64, copy=True)
+    nx, ny, nz = _dims(phi)
+    c = np.ascontiguousarray
+    _ok(load().orc_reinit(_p(phi), _p(c(jbn)), _p(c(dmins)), delta[0], delta[1], delta[2], nx, ny, nz,
+                          g, deltamin, iters, ref_bugs), "orc_reinit")
+    return phi
 
 
 def bc_walls(um):

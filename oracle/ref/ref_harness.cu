@@ -9,6 +9,7 @@
 //   pad    : cuSwapToGhost + mirrors      src/LevelSet/lsTransportEc.cu:91-127
 //   extrap : advect_CUDA as linked        src/LevelSet/lsTransportEc.cu:24-197
 //            with cuExtrapolation         src/LevelSet/interface.cu:341-436
+//   reinit : cuReinitLsJB                 src/LevelSet/lsTransportEc.cu:420-676
 // with two deliberate differences: the z grid of the level-set kernels is
 // NzG/5 (the reference writes NxG/5, :232), and grids are only used where they
 // tile the arrays exactly (the level-set kernels have no bounds checks).
@@ -19,6 +20,7 @@
 //   ref_harness weno <nxg> <nyg> <nzg> <hx> <hy> <hz> <dt> phi vel jbn out
 //   ref_harness pad <nx> <ny> <nz> <g> val out
 //   ref_harness extrap <nx> <ny> <nz> <dX> <dY> <dZ> <deltamin> press jbn sobject out
+//   ref_harness reinit <nxg> <nyg> <nzg> <g> <dX> <dY> <dZ> <deltamin> <iters> phi jbn dmins out
 #include <cuda.h>
 #include <cxxabi.h>
 
@@ -369,6 +371,61 @@ int main(int argc, char **argv) {
         void *af[] = {&pW, &pG, &g, &nx, &ny, &nz};
         launch(kF, nx / 10, ny / 10, nz / 5, 10, 10, 5, 0, af);
         write_bin(argv[12], download(pW, n));
+    } else if (mode == "reinit" && argc == 15) {
+        unsigned nxg = atoi(argv[2]), nyg = atoi(argv[3]), nzg = atoi(argv[4]);
+        int g = atoi(argv[5]);
+        double dX = atof(argv[6]), dY = atof(argv[7]), dZ = atof(argv[8]), dmin = atof(argv[9]);
+        int iters = atoi(argv[10]);
+        if (nxg % 10 || nyg % 10 || nzg % 5 || nxg != nyg || nyg != nzg || (int)nxg <= 2 * g) {
+            fprintf(stderr, "reinit: sizes must tile the reference grids exactly (cubic padded grid)\n");
+            return 5;
+        }
+        size_t ng = (size_t)nxg * nyg * nzg;
+        CUdeviceptr phi = upload(read_bin(argv[11], ng)), jbn = upload(read_bin(argv[12], 11 * ng)),
+                    dmins = upload(read_bin(argv[13], ng));
+        CUdeviceptr dPhi = dalloc(3 * ng), pP = dalloc(3 * ng), pM = dalloc(3 * ng), rs = dalloc(ng),
+                    phi0 = dalloc(ng), tmp = dalloc(ng);
+        CUfunction kD = find_kernel("Dev1thO_Downwind"), kP = find_kernel("PhiDevPlusParameterJB"),
+                   kM = find_kernel("PhiDevMinusParameterJB"), kR = find_kernel("reini_RS_WENOJB"),
+                   k1 = find_kernel("RunGK_FirstS"), k2 = find_kernel("RunGK_SecondS"),
+                   k3 = find_kernel("RunGK_ThirdS"), kZ = find_kernel("cuGhostCellsMirror3dZ"),
+                   kY = find_kernel("cuGhostCellsMirror3dY"), kX = find_kernel("cuGhostCellsMirror3dX");
+        const int gx = nxg / 10, gy = nyg / 10, gz = nzg / 5;
+        double sx = 1.0 / dX, sy = 1.0 / dY, sz = 1.0 / dZ, dt = 0.5 * dmin, dir = 1.0;
+        int ix = nxg, iy = nyg, iz = nzg, nxi = nxg - 2 * g, nyi = nyg - 2 * g, nzi = nzg - 2 * g;
+        auto rhs = [&](CUdeviceptr f, bool plus_first) {
+            void *ad[] = {&dPhi, &f, &sx, &sy, &sz, &nxg, &nyg, &nzg};
+            launch(kD, gx, gy, gz, 10, 10, 5, 0, ad);
+            void *ap[] = {&pP, &dPhi, &jbn, &nxg, &nyg, &nzg};
+            void *am[] = {&pM, &dPhi, &jbn, &nxg, &nyg, &nzg};
+            if (plus_first) {
+                launch(kP, gx, gy, gz, 10, 10, 5, 0, ap);
+                launch(kM, gx, gy, gz, 10, 10, 5, 0, am);
+            } else {
+                launch(kM, gx, gy, gz, 10, 10, 5, 0, am);
+                launch(kP, gx, gy, gz, 10, 10, 5, 0, ap);
+            }
+            void *ar[] = {&rs, &f, &dmins, &pP, &pM, &phi0, &nxg, &nyg, &nzg};
+            launch(kR, gx, gy, gz, 10, 10, 5, 0, ar);
+        };
+        for (int it = 0; it < iters; ++it) {
+            // lsTransportEc.cu:476-489: mirror Z, Y, X, then phi0 = phi
+            void *am[] = {&phi, &g, &nxi, &nyi, &nzi, &dir};
+            launch(kZ, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, am);
+            launch(kY, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, am);
+            launch(kX, nxg / 10, nyg / 10, 1, 10, 10, 1, 0, am);
+            CK(cuMemcpyDtoD(phi0, phi, ng * sizeof(double)));
+            rhs(phi, true);
+            void *a1[] = {&tmp, &phi, &dt, &rs, &ix, &iy, &iz};
+            launch(k1, gx, gy, gz, 10, 10, 5, 0, a1);
+            rhs(tmp, false);
+            void *a2[] = {&tmp, &phi, &tmp, &dt, &rs, &ix, &iy, &iz};
+            launch(k2, gx, gy, gz, 10, 10, 5, 0, a2);
+            rhs(tmp, false);
+            void *a3[] = {&phi, &phi, &tmp, &dt, &rs, &ix, &iy, &iz};
+            launch(k3, gx, gy, gz, 10, 10, 5, 0, a3);
+        }
+        write_bin(argv[14], download(phi, ng));
     } else {
         fprintf(stderr, "bad arguments for mode %s\n", mode.c_str());
         return 1;

@@ -14,9 +14,9 @@ GPU machine:
 Cases: the variant-C compact derivative along each axis (cu::cs::dFdX/Y/Z),
 cuDivergence, one cuAdvectLsJB WENO5 TVD-RK3 step, the ghost padding of
 advect_CUDA, and advect_CUDA itself (the pressure extrapolation into the
-solid).  Only the reference's outputs are stored; the inputs are regenerated
-from seeds by deriv_cases(), div_case(), weno_case(), pad_case() and
-extrap_case() below.
+solid) and cuReinitLsJB (level-set reinitialisation).  Only the reference's
+outputs are stored; the inputs are regenerated from seeds by deriv_cases(),
+div_case(), weno_case(), pad_case(), extrap_case() and reinit_case() below.
 """
 from __future__ import annotations
 
@@ -104,6 +104,24 @@ def extrap_case():
             (0.05, 0.055, 0.06), 0.04)
 
 
+def reinit_case():
+    """Padded 30^3 level set (a distorted sphere distance), padded metric,
+    smoothing widths, spacings, deltamin, iterations."""
+    n = 30
+    z, y, x = np.meshgrid(*(np.arange(n) / (n - 1),) * 3, indexing="ij")
+    d = np.sqrt((x - 0.5) ** 2 + (y - 0.45) ** 2 + (z - 0.55) ** 2) - 0.25
+    phi = 2.5 * d * (1.0 + 0.3 * np.sin(5 * x)) + 1e-3 * F.uniform(67, 0, d.shape)
+    jbn = np.zeros((11,) + d.shape)
+    for c in range(11):
+        jbn[c] = F.uniform(67, 1 + c, d.shape)
+    for c in (0, 4, 8):
+        jbn[c] = 1.0 + 0.05 * F.uniform(67, 20 + c, d.shape)
+    h = (1.0 / 29, 1.0 / 29, 1.0 / 29)
+    dm = np.full(d.shape, 0.8 / 29)
+    return (np.ascontiguousarray(phi), np.ascontiguousarray(jbn), np.ascontiguousarray(dm), h,
+            0.8 / 29, 10)
+
+
 def main(out_path=None):
     out_path = Path(out_path) if out_path else Path(__file__).resolve().parent / "reference_cuda.npz"
     build_harness()
@@ -146,6 +164,10 @@ def main(out_path=None):
         run("extrap", 20, 20, 20, *map(repr, delta), repr(dmin), wr("press", press), wr("jbn", jbn),
             wr("sobj", sobj), td / "extrap.bin")
         res.update(extrap_out=np.fromfile(td / "extrap.bin").reshape(press.shape))
+        phi, jbn, dm, h, dmin, iters = reinit_case()
+        run("reinit", 30, 30, 30, 5, *map(repr, h), repr(dmin), iters, wr("rphi", phi),
+            wr("rjbn", jbn), wr("rdm", dm), td / "reinit.bin")
+        res.update(reinit_out=np.fromfile(td / "reinit.bin").reshape(phi.shape))
     np.savez_compressed(out_path, **res)
     print(f"wrote {out_path} ({out_path.stat().st_size} bytes, {len(res)} arrays)")
 

@@ -99,3 +99,46 @@ def test_batched_impeller_equals_per_grid(emix):
     for g in range(len(ws)):
         assert_close(b.download(g)[0], ref[g], tol=1e-13, what=f"grid {g}")
     b.close()
+
+
+def test_oracle_interpolation_keeps_a_rigid_rotation(oracle):
+    """The interpolation fits a plane through the blade-surface point (moving
+    rigidly) and two outer neighbours: on a flow that is the same rigid
+    rotation everywhere it changes nothing (up to the reference's 7-digit pi)."""
+    w = _tank(32, omega=1.4)
+    X, Y, Z = w.grid.coords()
+    om = w.impeller.omega
+    um = w.um.copy()
+    um[1] = -om * Y * um[0]
+    um[2] = om * X * um[0]
+    a, _ = oracle.impeller_force(um, w.grid.coords(), w.impeller, 0.05)
+    w.impeller.interp = 1
+    b, _ = oracle.impeller_force(um, w.grid.coords(), w.impeller, 0.05)
+    changed = np.abs(b - a).max(axis=0) > 0
+    assert changed.sum() > 10
+    assert_close(b[1] / b[0], -om * Y, tol=3e-6, what="u")
+    assert_close(b[2] / b[0], om * X, tol=3e-6, what="v")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_step_with_impeller_interpolation_matches_oracle(emix, oracle, use_graph):
+    w = _tank(28, omega=1.6)
+    w.impeller.interp = 1
+    w.t0 = 0.1
+    p = oracle.step_params(w, level_set=True, bc_walls=1)
+    d, r = oracle.inisgdm(np.ascontiguousarray(w.grid.coords()))
+    rum, rphi = oracle.step(p, w.um, w.phi, w.jbn, w.mask, d, r, nsteps=2)
+    # the interpolation changes the result
+    w0 = _tank(28, omega=1.6)
+    w0.t0 = 0.1
+    p0 = oracle.step_params(w0, level_set=True, bc_walls=1)
+    rum0, _ = oracle.step(p0, w0.um, w0.phi, w0.jbn, w0.mask, d, r, nsteps=2)
+    assert np.abs(rum - rum0).max() > 1e-6
+    ctx = emix.Context(w, bc_walls=1)
+    ctx.step(2, use_graph=use_graph)
+    um, phi = ctx.download()
+    for m in range(5):
+        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
+    assert_close(phi, rphi, tol=1e-11, what="phi")
+    ctx.close()

@@ -40,6 +40,8 @@ def gold():
     g["pad_in"] = mg.pad_case()
     g["extrap_press"], g["extrap_jbn"], g["extrap_sobj"], g["extrap_delta"], g["extrap_dmin"] = \
         mg.extrap_case()
+    (g["reinit_phi"], g["reinit_jbn"], g["reinit_dm"], g["reinit_h"], g["reinit_dmin"],
+     g["reinit_iters"]) = mg.reinit_case()
     return g
 
 
@@ -78,6 +80,26 @@ def test_oracle_extrapolation_matches_reference_kernels(oracle, gold):
     assert_close(out, gold["extrap_out"], tol=TOL, what="press")
     assert_close(out - gold["extrap_press"], gold["extrap_out"] - gold["extrap_press"], tol=1e-11,
                  what="change of press")
+
+
+def test_oracle_reinit_matches_reference_kernels(oracle, gold):
+    if "reinit_out" not in gold:
+        pytest.skip("no cuReinitLsJB vectors in this golden file")
+    out = oracle.reinit(gold["reinit_phi"], gold["reinit_jbn"], gold["reinit_dm"], gold["reinit_h"], 5,
+                        gold["reinit_dmin"], iters=gold["reinit_iters"], ref_bugs=1)
+    assert_close(out, gold["reinit_out"], tol=TOL, what="phi")
+
+
+@pytest.mark.gpu
+def test_cuda_reinit_matches_reference_kernels(emix, gold):
+    import torch
+    if "reinit_out" not in gold:
+        pytest.skip("no cuReinitLsJB vectors in this golden file")
+    t = torch.from_numpy(gold["reinit_phi"].copy()).cuda()
+    emix.reinit_dev(t, torch.from_numpy(gold["reinit_jbn"]).cuda(), torch.from_numpy(gold["reinit_dm"]).cuda(),
+                    gold["reinit_h"], 5, gold["reinit_dmin"], iters=gold["reinit_iters"], ref_bugs=1)
+    torch.cuda.synchronize()
+    assert_close(t.cpu().numpy(), gold["reinit_out"], tol=TOL, what="phi")
 
 
 @pytest.mark.gpu
