@@ -246,14 +246,15 @@ int objective(emix_adj *a, bool adjoint, double *J) {
     for (int d = 0; d < 3; ++d) O.h[d] = p.h[d];
     O.r_in = a->obj.r_in; O.r_out = a->obj.r_out; O.eps = a->obj.eps;
     O.w_ke = a->obj.w_ke; O.w_if = a->obj.w_if;
-    O.nx = p.nx; O.ny = p.ny; O.nz = p.nz; O.red = a->red;
+    O.nx = p.nx; O.ny = p.ny; O.nz = p.nz; O.red = a->red + 8;
     if (adjoint) {
         O.lum = a->LA;
         O.lphi = a->Lphi;
         if ((rc = zero(a->Lphi, n, st))) return rc;
     }
-    if ((rc = zero(a->red + 2, 1, st))) return rc;
-    k_objective<<<grid_n(n), 256, 0, st>>>(O);
+    const int nb = grid_n(n);
+    k_objective<<<nb, 256, 0, st>>>(O);
+    k_sum_partials<<<1, 1024, 0, st>>>(a->red + 8, nb, a->red + 2);
     EMIX_CUDA_TRY(cudaGetLastError());
     EMIX_CUDA_TRY(cudaMemcpyAsync(J, a->red + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
     EMIX_CUDA_TRY(cudaStreamSynchronize(st));
@@ -320,7 +321,7 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     const long cnt = (long)ncp * 6 * n + (long)every * 6 * n + 6 * n        // checkpoints, segment, final
                      + 5 * n + 3 * (3 + 1 + 9 + 1 + 5) * n + 2 * 5 * n    // tape
                      + 5 * n * 3 + 3 * n * 2 + n * 2 + 5 * n + 15 * n + 9 * n + n + 5 * n + 6 * n
-                     + 2 * n + 3 * ng + 3 * ng + 8;
+                     + 2 * n + 3 * ng + 3 * ng + 8 + 2048;
     a->bytes = (size_t)cnt * sizeof(double);
     if (cudaMalloc(&a->arena, a->bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -349,7 +350,7 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     a->Lphi = take(q, n); a->Lphi_prev = take(q, n);
     a->Lphig0 = take(q, ng); a->LphiA = take(q, ng); a->LphiB = take(q, ng);
     a->LD = take(q, 3 * ng);
-    a->red = take(q, 8);
+    a->red = take(q, 8 + 2048);   // [0] dJ/domega, [1] dJ/dCs, [2] J, then J's block partials
     a->cp_clock.assign(2 * (size_t)ncp, 0.0);
     a->seg_clock.assign(2 * (size_t)every, 0.0);
     *out = a;

@@ -22,6 +22,36 @@ EMIX_DEV void block_sum_add(double v, double *out) {
     __syncthreads();
 }
 
+// sum of v over the block into out[blockIdx.x] (no atomics: the partial sums
+// are added in a fixed order by k_sum_partials, so the total is reproducible)
+EMIX_DEV void block_sum_store(double v, double *out) {
+    __shared__ double part[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) part[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? part[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) out[blockIdx.x] = v;
+    }
+}
+
+// out[0] = sum of the np partial sums, in a fixed order (one block of 1024)
+__global__ void k_sum_partials(const double *part, int np, double *out) {
+    __shared__ double s[1024];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) v += part[i];
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = s[0];
+}
+
 // ---- RK update: (convert + impeller)^T at every cell into T5 --------------
 struct RkAdjArgs {
     RkArgs a;              // the forward substep's arguments (tape pointers)

@@ -136,7 +136,7 @@ struct ObjArgs {
     double h[3];
     double r_in, r_out, eps, w_ke, w_if;
     int nx, ny, nz;
-    double *red;           // [2]: J
+    double *red;           // per-block partial sums of J (gridDim.x of them)
     double *lum, *lphi;    // adjoints (lum stored, lphi accumulated atomically); may be null
 };
 
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_objective(ObjArgs A) {
             }
         }
     }
-    block_sum_add(jsum, A.red + 2);
+    block_sum_store(jsum, A.red);
 }
 
 } // namespace emix

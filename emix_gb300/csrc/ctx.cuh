@@ -37,6 +37,14 @@ struct emix_ctx {
     cudaEvent_t prof_ev[2 * 64] = {};
     int prof_cls[64] = {};
     std::vector<emix::Launch> plan;   // one RK3 step
+    // optionally (emix_ctx_set_overlap) the level-set stages run on a second
+    // stream, concurrently with the flow's kernels of the same substep (fork
+    // before the stage, join before the RK update that overwrites the velocity
+    // the stage reads).  Off by default: both sides are FP64-bound and fill
+    // the GPU, and the overlap measured no gain.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
+    bool overlap = false;
 };
 
 namespace emix {

@@ -287,11 +287,29 @@ void build_plan(emix_ctx *c) {
 }
 
 int issue_step(emix_ctx *c) {
+    const bool fork = c->overlap && c->side && !c->prof;
+    int s = 0;
+    bool joined = true;
     for (const Launch &L : c->plan) {
+        if (fork && L.kind == LK_WENO) {
+            EMIX_CUDA_TRY(cudaEventRecord(c->fork_ev[s], c->stream));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->fork_ev[s], 0));
+            int rc = launch_single(L, c->side);
+            if (rc) return rc;
+            EMIX_CUDA_TRY(cudaEventRecord(c->join_ev[s], c->side));
+            joined = false;
+            ++s;
+            continue;
+        }
+        if (fork && !joined && L.kind == LK_RK) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
+            joined = true;
+        }
         ProfScope ps(c, L.cls);
         int rc = launch_single(L, c->stream);
         if (rc) return rc;
     }
+    if (fork && !joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
     c->launches = (int)c->plan.size();
     return EMIX_OK;
 }
@@ -441,6 +459,19 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
         return EMIX_ERR_CUDA;
     }
     c->stream = c->own;
+    if (p->level_set) {
+        if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            c->side = nullptr;
+        }
+        for (int k = 0; k < 3 && c->side; ++k)
+            if (cudaEventCreateWithFlags(&c->fork_ev[k], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                if (c->side) cudaStreamDestroy(c->side);
+                c->side = nullptr;
+            }
+    }
     if (cudaMemsetAsync(c->arena, 0, bytes, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -473,8 +504,20 @@ int emix_ctx_destroy(emix_ctx *c) {
     for (cudaEvent_t &e : c->prof_ev)
         if (e) cudaEventDestroy(e);
     if (c->own) cudaStreamDestroy(c->own);
+    for (int k = 0; k < 3; ++k) {
+        if (c->fork_ev[k]) cudaEventDestroy(c->fork_ev[k]);
+        if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+    }
+    if (c->side) cudaStreamDestroy(c->side);
     cudaFree(c->arena);
     delete c;
+    return EMIX_OK;
+}
+
+int emix_ctx_set_overlap(emix_ctx *c, int on) {
+    if (!c || (on != 0 && on != 1)) return EMIX_ERR_ARG;
+    c->overlap = on == 1;
+    drop_graph(c);
     return EMIX_OK;
 }
 

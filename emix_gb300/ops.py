@@ -435,6 +435,9 @@ class Context:
     def step(self, nsteps=1, use_graph=False):
         check(self.lib.emix_step(self._h, nsteps, 1 if use_graph else 0), "emix_step")
 
+    def set_overlap(self, on: bool):
+        check(self.lib.emix_ctx_set_overlap(self._h, 1 if on else 0), "emix_ctx_set_overlap")
+
     @property
     def time(self) -> float:
         v = C.c_double()

@@ -345,6 +345,12 @@ int emix_ctx_destroy(emix_ctx *ctx);
 /* Stream the context launches on (NULL = the legacy default stream). */
 int emix_ctx_set_stream(emix_ctx *ctx, void *stream);
 
+/* 1: each level-set stage runs on a second stream of the context,
+ * concurrently with the flow's kernels of its substep (joined before the RK
+ * update); 0 (default): one stream.  Results are the same either way; on a
+ * GB300 both sides are FP64-bound and the overlap gains nothing measurable. */
+int emix_ctx_set_overlap(emix_ctx *ctx, int on);
+
 /* Static inputs from host memory: jbn[11], mask, grid coordinates xyz[3]
  * (used to build the SGS filter width, as INISGDM). */
 int emix_ctx_set_static(emix_ctx *ctx, const double *jbn, const double *mask,

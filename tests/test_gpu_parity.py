@@ -267,3 +267,23 @@ def test_step(emix, oracle, kind, level_set):
     if level_set:
         assert np.array_equal(phi2, phi)
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_overlapped_level_set_stream_gives_the_same_bits(emix):
+    """The level-set stages on a second stream and on the context's one
+    stream (the default) give identical results."""
+    w = F.stirred_tank(n=24, impeller=True)
+    a = emix.Context(w, bc_walls=1)
+    b = emix.Context(w, bc_walls=1)
+    a.set_overlap(True)
+    for use_graph in (False, True):
+        a.upload(w.um, w.phi); a.time = 0.0
+        b.upload(w.um, w.phi); b.time = 0.0
+        a.step(3, use_graph=use_graph)
+        b.step(3, use_graph=use_graph)
+        ua, pa = a.download()
+        ub, pb = b.download()
+        assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+    a.close()
+    b.close()
