@@ -45,12 +45,7 @@ int launch_weno_stage(const WenoArgs &a_in, cudaStream_t st) {
         if (a.rn[d] <= 0) { a.r0[d] = 0; a.rn[d] = dims[d]; }   // default: whole padded grid
         if (a.r0[d] < 0 || a.r0[d] + a.rn[d] > dims[d]) return EMIX_ERR_ARG;
     }
-    dim3 block(kWX, kWY, kWZ);
-    dim3 grid((a.rn[0] + kWX - 1) / kWX, (a.rn[1] + kWY - 1) / kWY, (a.rn[2] + kWZ - 1) / kWZ);
-    if (grid.y > 65535 || grid.z > 65535) return EMIX_ERR_ARG;
-    k_weno_stage<<<grid, block, 0, st>>>(a);
-    EMIX_CUDA_TRY(cudaGetLastError());
-    return EMIX_OK;
+    return launch_weno_march(a, st);
 }
 
 namespace {

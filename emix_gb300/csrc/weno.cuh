@@ -60,6 +60,8 @@ __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict
                               int nx, int ny, int nz);
 
 int launch_weno_stage(const WenoArgs &a, cudaStream_t st);
+// the z-marching form of the stage (weno_march.cu); a's region normalised
+int launch_weno_march(const WenoArgs &a, cudaStream_t st);
 
 // C_d = jbn_d / h_d and E_d = kWenoEps4 / C_d^2 for the precomputed-scale path
 __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
@@ -72,7 +74,7 @@ __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict
 // Arithmetic, 2nd ed., section 4.7, on Newton-Raphson-like iterations).  The
 // seed's relative error is below 2^-22, so the step's error e^3 is below
 // 2^-66: a correctly rounded result up to the last operation's rounding.
-// Three FMAs.  For positive normal d well inside the double range.
+// Three FMAs.  For normal d of either sign well inside the double range.
 EMIX_DEV double rcp_newton(double d) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(d);
     const int ebits = (int)(b >> 52) & 0x7ff;                       // biased exponent
@@ -83,7 +85,8 @@ EMIX_DEV double rcp_newton(double d) {
     const int fexp = (int)(rf >> 23) & 0xff;
     const unsigned long long rm = ((unsigned long long)(fexp - 127 + 1023 - (ebits - 1023)) << 52) |
                                   ((unsigned long long)(rf & 0x7fffff) << 29);
-    const double x = __longlong_as_double((long long)rm);
+    // d's sign on the seed: the step below then converges for negative d too
+    const double x = __longlong_as_double((long long)(rm | (b & 0x8000000000000000ull)));
     const double e = fma(-d, x, 1.0);
     return fma(x, fma(e, e, e), x);
 }
@@ -109,9 +112,9 @@ EMIX_DEV double weno5(double v1, double v2, double v3, double v4, double v5, dou
     const double e2 = v2 - v4;
     const double d3 = fma(-2.0, v4, v3 + v5);
     const double e3 = fma(-4.0, v4, fma(3.0, v3, v5));
-    double t1 = fma(c13 * d1, d1, e1 * e1) + eps4; t1 *= t1;
-    double t2 = fma(c13 * d2, d2, e2 * e2) + eps4; t2 *= t2;
-    double t3 = fma(c13 * d3, d3, e3 * e3) + eps4; t3 *= t3;
+    double t1 = fma(c13 * d1, d1, fma(e1, e1, eps4)); t1 *= t1;
+    double t2 = fma(c13 * d2, d2, fma(e2, e2, eps4)); t2 *= t2;
+    double t3 = fma(c13 * d3, d3, fma(e3, e3, eps4)); t3 *= t3;
     const double w1 = t2 * t3;
     const double w2 = (6.0 * t1) * t3;
     const double w3 = (3.0 * t1) * t2;
