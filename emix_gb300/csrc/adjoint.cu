@@ -215,7 +215,7 @@ int step_adjoint(emix_adj *a) {
         G.lout = s == 3 ? a->Lphi : (s == 2 ? a->LphiB : a->LphiA);
         G.lphi0 = a->Lphig0;
         G.lphiin = s == 1 ? a->Lphig0 : (s == 2 ? a->LphiA : a->LphiB);
-        G.lD = a->LD; G.lu = LuIn; G.vel = a->t_u[s - 1]; G.wc = wa.wc; G.we = wa.we;
+        G.lD = a->LD; G.lu = LuIn; G.vel = a->t_u[s - 1]; G.wce = wa.wce;
         G.nxg = wa.nxg; G.nyg = wa.nyg; G.nzg = wa.nzg; G.g = wa.g;
         for (int d = 0; d < 3; ++d) { G.r0[d] = wa.r0[d]; G.rn[d] = wa.rn[d]; }
         G.dt = wa.dt; G.stage = s;

@@ -13,7 +13,7 @@ struct WenoAdjArgs {
     double *lphiin;          // adjoint of the input (padded), accumulated
     double *lD;              // 3 padded fields: adjoint of the backward differences (atomic)
     double *lu;              // 3 interior fields: adjoint of the velocity (atomic)
-    const double *vel, *wc, *we;
+    const double *vel, *wce;      // wce: (C, E) pairs as in WenoArgs
     int nxg, nyg, nzg, g;
     int r0[3], rn[3];
     double dt;
@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) k_adj_weno(WenoAdjArgs A) {
         const long s3[3] = {1, nxg, (long)nxg * nyg};
         for (int d = 0; d < 3; ++d) {
             const double ud = A.vel[d * nv + iv];
-            const double mx = A.wc[d * nv + iv], ex = A.we[d * nv + iv];
+            const double2 ce = weno_scale(A.wce, d, nv, iv);
+            const double mx = ce.x, ex = ce.y;
             int p[5];
             if (__double_as_longlong(ud) >= 0) stencil_left(c3[d], L3[d], p);
             else stencil_right(c3[d], L3[d], p);

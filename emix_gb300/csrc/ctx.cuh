@@ -15,7 +15,7 @@ struct emix_ctx {
     double *arena = nullptr;
     size_t arena_bytes = 0;
     double *um0, *um, *u, *pres, *dvel, *vis, *amut, *vort, *flux, *R, *W, *jbn, *jx, *jy, *jz,
-        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB, *wenoC, *wenoE, *xyz, *clock;
+        *mask, *dxyz, *ratios, *phi, *phig0, *phigA, *phigB, *wenoCE, *xyz, *clock;
     unsigned char *impflag = nullptr;
     // blade-edge interpolation of the impeller (imp.interp)
     double *ip_geo = nullptr;

@@ -91,7 +91,9 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
     const int n = T.n;
     const DerivRow *__restrict__ rows = T.rows;
 
-    // forward sweep; the input two rows ahead is loaded one iteration early
+    // forward sweep; the input two rows ahead comes from a queue of four rows
+    // loaded four iterations early (the loads' latency is longer than an
+    // iteration of every resident warp)
     double wp = 0.0, y0 = 0.0;
     int i = 0;
     if (!T.periodic) {
@@ -103,10 +105,15 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
         const int iend = n - T.nhi;
         if (i < iend) {
             double fm2 = in[(i - 2) * s], fm1 = in[(i - 1) * s], f0 = in[i * s], fp1 = in[(i + 1) * s];
-            double nxt = in[(i + 2) * s];
+            // q0..q3 = f(i+2) .. f(i+5) (rows past the end read as 0, unused)
+            double q0 = in[(i + 2) * s];
+            double q1 = i + 3 < n ? in[(i + 3) * s] : 0.0;
+            double q2 = i + 4 < n ? in[(i + 4) * s] : 0.0;
+            double q3 = i + 5 < n ? in[(i + 5) * s] : 0.0;
             for (; i < iend; ++i) {
-                const double fp2 = nxt;
-                if (i + 3 < n) nxt = in[(i + 3) * s];
+                const double fp2 = q0;
+                q0 = q1; q1 = q2; q2 = q3;
+                if (i + 6 < n) q3 = in[(i + 6) * s];
                 const DerivRow r = rows[i];
                 const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
                 w[i * s] = v;
@@ -136,19 +143,36 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
         }
     }
 
-    // backward sweep; w one row ahead
+    // backward sweep; w (and the accumulated output) from queues of four rows
+    // loaded four iterations early
     double fact = 0.0;
     if (T.periodic) fact = (y0 + T.sm1 * wp) * T.sm2;
     double yn = 0.0;
-    double wn = w[(n - 1) * s];
+    // w0..w3 = w(i) .. w(i-3), o0..o3 the same rows of out
+    double w0 = w[(n - 1) * s];
+    double w1 = n - 2 >= 0 ? w[(n - 2) * s] : 0.0;
+    double w2 = n - 3 >= 0 ? w[(n - 3) * s] : 0.0;
+    double w3 = n - 4 >= 0 ? w[(n - 4) * s] : 0.0;
+    double o0 = 0.0, o1 = 0.0, o2 = 0.0, o3 = 0.0;
+    if (EPI == EPI_ACCUM) {
+        o0 = out[(n - 1) * s];
+        o1 = n - 2 >= 0 ? out[(n - 2) * s] : 0.0;
+        o2 = n - 3 >= 0 ? out[(n - 3) * s] : 0.0;
+        o3 = n - 4 >= 0 ? out[(n - 4) * s] : 0.0;
+    }
     for (i = n - 1; i >= 0; --i) {
-        const double wi = wn;
-        if (i > 0) wn = w[(i - 1) * s];
+        const double wi = w0, oi = o0;
+        w0 = w1; w1 = w2; w2 = w3;
+        if (i - 4 >= 0) w3 = w[(i - 4) * s];
+        if (EPI == EPI_ACCUM) {
+            o0 = o1; o1 = o2; o2 = o3;
+            if (i - 4 >= 0) o3 = out[(i - 4) * s];
+        }
         const double y = wi - rows[i].g * yn;
         yn = y;
         double xv = y;
         if (T.periodic && (i < T.zlo || i >= T.zhi)) xv = y - fact * T.zz[i];
-        if (EPI == EPI_ACCUM) xv += out[i * s];
+        if (EPI == EPI_ACCUM) xv += oi;
         out[i * s] = xv;
     }
 }

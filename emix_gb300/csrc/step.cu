@@ -185,7 +185,7 @@ void build_plan(emix_ctx *c) {
             a.nxg = nx + 2 * g; a.nyg = ny + 2 * g; a.nzg = nz + 2 * g; a.g = g;
             a.sx = 1.0 / p.h[0]; a.sy = 1.0 / p.h[1]; a.sz = 1.0 / p.h[2];
             a.dt = p.dt; a.stage = s; a.ref_bugs = p.ref_bugs;
-            a.wc = c->wenoC; a.we = c->wenoE;
+            a.wce = c->wenoCE;
             // stage 3 writes only the interior, so stage 2 is needed only within
             // the 3-cell reach of the WENO5 stencil around it, and stage 3 only on
             // the interior (stage 1 covers the whole padded grid)
@@ -416,7 +416,7 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     const long nb2 = imp && p->imp.interp ? (long)p->imp.nblades * p->nx * p->ny : 0;
     const size_t ip_words = nb2 ? 11 * nb2 + 2 * ((nb2 + 7) / 8) + nb2 + (nb2 + 1) / 2 + kImpMaxBlades : 0;
     const size_t bytes = ((size_t)(nfield + (imp ? 3 : 0)) * n + 3 * (size_t)ng +
-                          (imp ? kImpClockLen + (n + 7) / 8 : 0) + ip_words) * sizeof(double);
+                          (imp ? kImpClockLen + (n + 7) / 8 : 0) + ip_words + 1) * sizeof(double);
     if (cudaMalloc(&c->arena, bytes) != cudaSuccess) {
         cudaGetLastError();
         set_last_message("cudaMalloc of the context arena failed");
@@ -431,8 +431,8 @@ int emix_ctx_create(const emix_params *p, emix_ctx **out) {
     c->W = take(5 * n); c->jbn = take(11 * n); c->jx = take(n); c->jy = take(n); c->jz = take(n);
     c->mask = take(n); c->dxyz = take(n);
     c->phi = p->level_set ? take(n) : nullptr;
-    c->wenoC = p->level_set ? take(3 * n) : nullptr;
-    c->wenoE = p->level_set ? take(3 * n) : nullptr;
+    if ((q - c->arena) & 1) ++q;   // 16-byte pairs
+    c->wenoCE = p->level_set ? take(6 * n) : nullptr;
     c->amut = sf ? take(n) : nullptr;
     c->vort = sf ? take(3 * n) : nullptr;
     c->ratios = sf ? take(6 * n) : nullptr;
@@ -558,8 +558,8 @@ int emix_ctx_set_static(emix_ctx *c, const double *jbn, const double *mask, cons
     k_sgs_setup<<<cells_grid(n), 256, 0, st>>>(c->flux, c->dxyz, ratios, p.nx, p.ny, p.nz);
     k_metric_products<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->jx, c->jy, c->jz, n);
     if (p.level_set)
-        k_weno_scales<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->wenoC, c->wenoE, 1.0 / p.h[0],
-                                                     1.0 / p.h[1], 1.0 / p.h[2], n);
+        k_weno_scales<<<cells_grid(n), 256, 0, st>>>(c->jbn, c->wenoCE, 1.0 / p.h[0], 1.0 / p.h[1],
+                                                     1.0 / p.h[2], n);
     EMIX_CUDA_TRY(cudaGetLastError());
     EMIX_CUDA_TRY(cudaStreamSynchronize(st));
     c->static_set = true;

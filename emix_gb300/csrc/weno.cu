@@ -10,14 +10,12 @@ __global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
     weno_stage_body(a, blockIdx, threadIdx);
 }
 
-__global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
-                              double *__restrict__ we, double sx, double sy, double sz, long n) {
+__global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wce, double sx,
+                              double sy, double sz, long n) {
+    double2 *ce = reinterpret_cast<double2 *>(wce);
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         const double c[3] = {jbn[q] * sx, jbn[4 * n + q] * sy, jbn[8 * n + q] * sz};
-        for (int d = 0; d < 3; ++d) {
-            wc[d * n + q] = c[d];
-            we[d * n + q] = kWenoEps4 / (c[d] * c[d]);
-        }
+        for (int d = 0; d < 3; ++d) ce[d * n + q] = make_double2(c[d], kWenoEps4 / (c[d] * c[d]));
     }
 }
 

@@ -22,9 +22,9 @@ namespace emix {
 struct WenoArgs {
     const double *phi;   // padded field read with the stencil
     // precomputed per-cell scale factors (reflect mode only; may be null):
-    // C_d = jbn_d/h_d and E_d = 12*1e-6/C_d^2, 3 components each, unpadded
-    const double *wc;
-    const double *we;
+    // pairs (C_d, E_d) with C_d = jbn_d/h_d and E_d = kWenoEps4/C_d^2, for
+    // d = 0, 1, 2 in turn, each over the unpadded grid (16-byte aligned)
+    const double *wce;
     // region of the padded grid to compute: [r0, r0 + rn) per axis
     int r0[3], rn[3];
     const double *phi0;  // padded field read at the cell (stages 2 and 3)
@@ -63,9 +63,14 @@ int launch_weno_stage(const WenoArgs &a, cudaStream_t st);
 // the z-marching form of the stage (weno_march.cu); a's region normalised
 int launch_weno_march(const WenoArgs &a, cudaStream_t st);
 
-// C_d = jbn_d / h_d and E_d = kWenoEps4 / C_d^2 for the precomputed-scale path
-__global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wc,
-                              double *__restrict__ we, double sx, double sy, double sz, long n);
+// the pairs (C_d, E_d) = (jbn_d / h_d, kWenoEps4 / C_d^2) of the precomputed-scale path
+__global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wce, double sx,
+                              double sy, double sz, long n);
+
+// (C_d, E_d) of unpadded cell iv (nv cells)
+EMIX_DEV double2 weno_scale(const double *wce, int d, long nv, long iv) {
+    return reinterpret_cast<const double2 *>(wce)[d * nv + iv];
+}
 
 // Reciprocal seeded from the single-precision reciprocal of d's mantissa
 // (d's exponent applied by integer arithmetic), then one third-order step of
@@ -241,12 +246,14 @@ EMIX_DEV void weno_stage_body(const WenoArgs &a, uint3 bid, uint3 tid3) {
     // scale of the differences: either multiply the five differences by
     // C = jbn/h (as the reference does) or use the precomputed per-cell
     // factors and rescale epsilon instead (one multiply per direction)
-    const bool pre = a.wc != nullptr;
+    const bool pre = a.wce != nullptr;
     double cx, cy, cz, ex, ey, ez, mx, my, mz;
     if (pre) {
         cx = 1.0; cy = 1.0; cz = 1.0;
-        mx = a.wc[iv]; my = a.wc[nv + iv]; mz = a.wc[2 * nv + iv];
-        ex = a.we[iv]; ey = a.we[nv + iv]; ez = a.we[2 * nv + iv];
+        const double2 sx2 = weno_scale(a.wce, 0, nv, iv), sy2 = weno_scale(a.wce, 1, nv, iv),
+                      sz2 = weno_scale(a.wce, 2, nv, iv);
+        mx = sx2.x; my = sy2.x; mz = sz2.x;
+        ex = sx2.y; ey = sy2.y; ez = sz2.y;
     } else {
         cx = a.jbn[iv] * a.sx; cy = a.jbn[4 * nv + iv] * a.sy; cz = a.jbn[8 * nv + iv] * a.sz;
         mx = 1.0; my = 1.0; mz = 1.0;

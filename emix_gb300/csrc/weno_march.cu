@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kNT, 4) k_weno_march(WenoArgs a) {
     const int g = a.g;
     const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
     const long nv = a.reflect ? (long)nx * ny * nz : sxy * nzg;
-    const bool pre = a.wc != nullptr;
+    const bool pre = a.wce != nullptr;
 
     // z window of this column: phi(z), 0 outside the grid
     auto ld = [&](int z) { return (active && z >= 0 && z < nzg) ? phi[col + sxy * z] : 0.0; };
@@ -179,8 +179,9 @@ __global__ void __launch_bounds__(kNT, 4) k_weno_march(WenoArgs a) {
                 const double u = a.vel[d * nv + iv];
                 double mx, ex;
                 if (pre) {
-                    mx = a.wc[d * nv + iv];
-                    ex = a.we[d * nv + iv];
+                    const double2 ce = weno_scale(a.wce, d, nv, iv);
+                    mx = ce.x;
+                    ex = ce.y;
                 } else {
                     const double jd = a.jbn[4 * d * nv + iv] * (d == 0 ? a.sx : (d == 1 ? a.sy : a.sz));
                     // W(C v; eps) = C W(v; eps / C^2)
