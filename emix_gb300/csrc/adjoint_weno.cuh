@@ -1,5 +1,5 @@
-// adjoint_weno.cuh -- adjoint of one level-set TVD stage (weno_stage_body in
-// weno.cuh), of the mirrored padding, and of the tank objective.
+// adjoint_weno.cuh -- adjoint of one level-set TVD stage (weno_march_body in
+// weno_march.cuh), of the mirrored padding, and of the tank objective.
 #pragma once
 
 #include "adjoint_kernels.cuh"

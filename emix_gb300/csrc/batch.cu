@@ -9,6 +9,7 @@
 // a CUDA graph.  The work-list granularity (pencils per y/z block, cells per
 // pointwise item, resident CTAs per SM) is chosen by a timing autotuner.
 #include "plan.cuh"
+#include "weno_march.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -70,7 +71,8 @@ k_batch_cells(const typename Op::A *__restrict__ args, const long *__restrict__ 
     }
 }
 
-__global__ void __launch_bounds__(kWX *kWY *kWZ)
+// the z-marching stage body over (grid, column tile, z chunk) items
+__global__ void __launch_bounds__(kNT, 4)
 k_batch_weno(const WenoArgs *__restrict__ args, const long *__restrict__ start,
              const Shape *__restrict__ shape, int ngrid) {
     const long total = start[ngrid];
@@ -78,10 +80,9 @@ k_batch_weno(const WenoArgs *__restrict__ args, const long *__restrict__ start,
         const int g = find_grid(start, ngrid, vb);
         const long local = vb - start[g];
         const Shape sh = shape[g];
-        const uint3 bid = make_uint3((unsigned)(local % sh.gx), (unsigned)((local / sh.gx) % sh.gy),
-                                     (unsigned)(local / ((long)sh.gx * sh.gy)));
-        weno_stage_body(args[g], bid, threadIdx);
-        __syncthreads();   // the difference tiles are refilled by the next item
+        weno_march_body(args[g], (int)(local % sh.gx), (int)((local / sh.gx) % sh.gy),
+                        (int)(local / ((long)sh.gx * sh.gy)), sh.gz);
+        __syncthreads();   // the tiles are refilled by the next item
     }
 }
 
@@ -212,9 +213,10 @@ long point_count(const Launch &L) {
 Shape shape_of(const Launch &L, const BatchTune &t) {
     Shape s{1, 1, 1, 0};
     if (L.kind == LK_WENO) {
-        s.gx = (L.weno.rn[0] + kWX - 1) / kWX;
-        s.gy = (L.weno.rn[1] + kWY - 1) / kWY;
-        s.gz = (L.weno.rn[2] + kWZ - 1) / kWZ;
+        // 16 x 16 columns in z chunks of at most 32 planes
+        s.gx = (L.weno.rn[0] + kMX - 1) / kMX;
+        s.gy = (L.weno.rn[1] + kMY - 1) / kMY;
+        s.gz = (L.weno.rn[2] + 31) / 32;
     } else if (L.kind == LK_DERIV_X) {
         const long np = (long)L.deriv.ny * L.deriv.nz;
         s.gx = (int)((np + 127) / 128);
@@ -309,6 +311,18 @@ int ctas(const emix_batch *b, long total) {
     return (int)(c < 1 ? 1 : c);
 }
 
+// resident CTAs of the stage kernel (its register bound allows 4 per SM)
+int weno_ctas(const emix_batch *b, long total) {
+    static int per = 0;
+    if (per == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_weno, kNT, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per = 4;
+    }
+    long c = (long)b->sms * (per > 0 ? per : 1);
+    if (c > total) c = total;
+    return (int)(c < 1 ? 1 : c);
+}
+
 int issue(emix_batch *b) {
     const int G = (int)b->grids.size();
     cudaStream_t st = b->stream;
@@ -326,7 +340,7 @@ int issue(emix_batch *b) {
         case LK_BC: k_batch_cells<BcOp><<<nb, 256, 0, st>>>((const BcArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_CLOCK: k_batch_cells<ClockOp><<<nb, 256, 0, st>>>((const ImpClockArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_WENO:
-            k_batch_weno<<<nb, dim3(kWX, kWY, kWZ), 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
+            k_batch_weno<<<weno_ctas(b, P.total), kNT, 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
             break;
         case LK_DERIV_X: {
             const size_t shm = 4 * kXTile * sizeof(double);

@@ -66,7 +66,7 @@ extern "C" int emix_weno5_advect_dev_noalloc(double *phi, const double *vel, con
                                              int nxg, int nyg, int nzg, int ref_bugs,
                                              void *stream) {
     if (!phi || !vel || !jbn || nxg < 6 || nyg < 6 || nzg < 6 || !(hx > 0) || !(hy > 0) ||
-        !(hz > 0) || (nyg + kWY - 1) / kWY > 65535 || (nzg + kWZ - 1) / kWZ > 65535)
+        !(hz > 0) || (nyg + 15) / 16 > 65535)
         return EMIX_ERR_ARG;
     const long ng = (long)nxg * nyg * nzg;
     if (ng > kNoAllocMaxCells) {

@@ -6,10 +6,6 @@ namespace emix {
 
 int device_scratch(size_t bytes, double **out);
 
-__global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a) {
-    weno_stage_body(a, blockIdx, threadIdx);
-}
-
 __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wce, double sx,
                               double sy, double sz, long n) {
     double2 *ce = reinterpret_cast<double2 *>(wce);
@@ -74,8 +70,8 @@ int weno_advect_impl(double *phi, const double *vel, const double *jbn, double h
 }
 
 bool weno_dims_ok(int nxg, int nyg, int nzg) {
-    return nxg >= 6 && nyg >= 6 && nzg >= 6 && (nyg + kWY - 1) / kWY <= 65535 &&
-           (nzg + kWZ - 1) / kWZ <= 65535;
+    // the stage kernel's grid: 16 x 16 columns, y tiles in gridDim.y
+    return nxg >= 6 && nyg >= 6 && nzg >= 6 && (nyg + 15) / 16 <= 65535;
 }
 } // namespace
 

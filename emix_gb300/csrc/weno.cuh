@@ -8,11 +8,12 @@
 // (src/LevelSet/extrapol.cu:155-212), all on the ghost-padded grid, with the
 // reference's index rules at the padded-grid edges.
 //
-// One fused kernel per stage instead of five launches and ten field passes:
-// each block stages the backward differences of its tile (plus the stencil
-// halo) in shared memory once per direction, and each cell evaluates only
-// the upwind reconstruction its velocity selects (the other one is
-// multiplied by zero in the reference).
+// One fused kernel per stage instead of five launches and ten field passes
+// (weno_march_body, weno_march.cuh): each cell evaluates only the upwind
+// reconstruction its velocity selects (the other one is multiplied by zero in
+// the reference).  This header holds the pieces the stage kernel, the batched
+// form and the adjoint share: the arguments, the reconstruction, the edge
+// rules of the stencil and the mirrored padding.
 #pragma once
 
 #include "common.cuh"
@@ -41,10 +42,6 @@ struct WenoArgs {
     int ref_bugs;
 };
 
-constexpr int kWX = 32, kWY = 4, kWZ = 2;
-
-__global__ void __launch_bounds__(kWX *kWY *kWZ) k_weno_stage(WenoArgs a);
-
 // Padding with mirrored ghost cells: cuSwapToGhost followed by
 // cuGhostCellsMirror3dZ/Y/X (src/LevelSet/lsTools.cu:482-585,772-796).
 struct PadArgs {
@@ -59,8 +56,9 @@ __global__ void k_ghost_pad(PadArgs a);
 __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict__ ghost, int g,
                               int nx, int ny, int nz);
 
+// one stage on one grid (region rn[d] <= 0: the whole padded axis)
 int launch_weno_stage(const WenoArgs &a, cudaStream_t st);
-// the z-marching form of the stage (weno_march.cu); a's region normalised
+// the z-marching stage kernel (weno_march.cu); a's region normalised
 int launch_weno_march(const WenoArgs &a, cudaStream_t st);
 
 // the pairs (C_d, E_d) = (jbn_d / h_d, kWenoEps4 / C_d^2) of the precomputed-scale path
@@ -172,164 +170,6 @@ EMIX_DEV void pad_cell(const PadArgs &a, long q) {
     double v = a.val[mirror(X, g, nx) + (long)nx * (mirror(Y, g, ny) + (long)ny * mirror(Z, g, nz))];
     for (int c = 0; c < cnt; ++c) v *= a.dir;
     a.ghost[q] = v;
-}
-
-// One TVD stage on one (virtual) block of kWX x kWY x kWZ cells.
-EMIX_DEV void weno_stage_body(const WenoArgs &a, uint3 bid, uint3 tid3) {
-    // backward differences phi(p) - phi(p-1) (D(0) = phi(1) - phi(0)),
-    // unscaled, for the tile plus the [-2, +3] stencil halo of each axis
-    __shared__ double Dx[kWZ][kWY][kWX + 5];
-    __shared__ double Dy[kWZ][kWY + 5][kWX];
-    __shared__ double Dz[kWZ + 5][kWY][kWX];
-
-    const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
-    const int x0 = a.r0[0] + bid.x * kWX, y0 = a.r0[1] + bid.y * kWY,
-              z0 = a.r0[2] + bid.z * kWZ;
-    const int xe = a.r0[0] + a.rn[0], ye = a.r0[1] + a.rn[1], ze = a.r0[2] + a.rn[2];
-    const long sxy = (long)nxg * nyg;
-    const double *__restrict__ phi = a.phi;
-    const int tid = tid3.x + kWX * (tid3.y + kWY * tid3.z);
-    constexpr int NT = kWX * kWY * kWZ;
-
-    for (int t = tid; t < kWZ * kWY * (kWX + 5); t += NT) {
-        const int xi = t % (kWX + 5), yz = t / (kWX + 5);
-        const int yi = yz % kWY, zi = yz / kWY;
-        const int X = x0 - 2 + xi, Y = y0 + yi, Z = z0 + zi;
-        double v = 0.0;
-        if (X >= 0 && X < nxg && Y < nyg && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = X == 0 ? phi[id + 1] - phi[id] : phi[id] - phi[id - 1];
-        }
-        Dx[zi][yi][xi] = v;
-    }
-    for (int t = tid; t < kWZ * (kWY + 5) * kWX; t += NT) {
-        const int xi = t % kWX, yz = t / kWX;
-        const int yi = yz % (kWY + 5), zi = yz / (kWY + 5);
-        const int X = x0 + xi, Y = y0 - 2 + yi, Z = z0 + zi;
-        double v = 0.0;
-        if (X < nxg && Y >= 0 && Y < nyg && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = Y == 0 ? phi[id + nxg] - phi[id] : phi[id] - phi[id - nxg];
-        }
-        Dy[zi][yi][xi] = v;
-    }
-    for (int t = tid; t < (kWZ + 5) * kWY * kWX; t += NT) {
-        const int xi = t % kWX, yz = t / kWX;
-        const int yi = yz % kWY, zi = yz / kWY;
-        const int X = x0 + xi, Y = y0 + yi, Z = z0 - 2 + zi;
-        double v = 0.0;
-        if (X < nxg && Y < nyg && Z >= 0 && Z < nzg) {
-            const long id = X + (long)nxg * Y + sxy * Z;
-            v = Z == 0 ? phi[id + sxy] - phi[id] : phi[id] - phi[id - sxy];
-        }
-        Dz[zi][yi][xi] = v;
-    }
-    __syncthreads();
-
-    const int tx = tid3.x, ty = tid3.y, tz = tid3.z;
-    const int X = x0 + tx, Y = y0 + ty, Z = z0 + tz;
-    if (X >= xe || Y >= ye || Z >= ze) return;
-    const long id = X + (long)nxg * Y + sxy * Z;
-
-    // velocity and metric at the cell
-    long iv;
-    long nv;
-    if (a.reflect) {
-        const int nx = nxg - 2 * a.g, ny = nyg - 2 * a.g, nz = nzg - 2 * a.g;
-        iv = mirror(X, a.g, nx) + (long)nx * (mirror(Y, a.g, ny) + (long)ny * mirror(Z, a.g, nz));
-        nv = (long)nx * ny * nz;
-    } else {
-        iv = id;
-        nv = sxy * nzg;
-    }
-    const double ux = a.vel[iv], uy = a.vel[nv + iv], uz = a.vel[2 * nv + iv];
-    // scale of the differences: either multiply the five differences by
-    // C = jbn/h (as the reference does) or use the precomputed per-cell
-    // factors and rescale epsilon instead (one multiply per direction)
-    const bool pre = a.wce != nullptr;
-    double cx, cy, cz, ex, ey, ez, mx, my, mz;
-    if (pre) {
-        cx = 1.0; cy = 1.0; cz = 1.0;
-        const double2 sx2 = weno_scale(a.wce, 0, nv, iv), sy2 = weno_scale(a.wce, 1, nv, iv),
-                      sz2 = weno_scale(a.wce, 2, nv, iv);
-        mx = sx2.x; my = sy2.x; mz = sz2.x;
-        ex = sx2.y; ey = sy2.y; ez = sz2.y;
-    } else {
-        cx = a.jbn[iv] * a.sx; cy = a.jbn[4 * nv + iv] * a.sy; cz = a.jbn[8 * nv + iv] * a.sz;
-        mx = 1.0; my = 1.0; mz = 1.0;
-        ex = kWenoEps4; ey = kWenoEps4; ez = kWenoEps4;
-    }
-
-    int p[5];
-    double rs;
-    // x
-    {
-        if (__double_as_longlong(ux) >= 0) stencil_left(X, nxg, p); else stencil_right(X, nxg, p);
-        const double *d = &Dx[tz][ty][0];
-        const int o = x0 - 2;
-        double phx;
-        if (pre)
-            phx = mx * weno5(d[p[0] - o], d[p[1] - o], d[p[2] - o], d[p[3] - o], d[p[4] - o], ex);
-        else
-            phx = weno5(d[p[0] - o] * cx, d[p[1] - o] * cx, d[p[2] - o] * cx, d[p[3] - o] * cx,
-                        d[p[4] - o] * cx, ex);
-        rs = ux * phx;
-    }
-    // y
-    {
-        if (__double_as_longlong(uy) >= 0) stencil_left(Y, nyg, p); else stencil_right(Y, nyg, p);
-        const int o = y0 - 2;
-        const double v1 = Dy[tz][p[0] - o][tx], v2 = Dy[tz][p[1] - o][tx], v3 = Dy[tz][p[2] - o][tx],
-                     v4 = Dy[tz][p[3] - o][tx], v5 = Dy[tz][p[4] - o][tx];
-        double phy;
-        if (pre)
-            phy = my * weno5(v1, v2, v3, v4, v5, ey);
-        else
-            phy = weno5(v1 * cy, v2 * cy, v3 * cy, v4 * cy, v5 * cy, ey);
-        rs = rs + uy * phy;
-    }
-    // z
-    {
-        const bool left = __double_as_longlong(uz) >= 0;
-        if (left) stencil_left(Z, nzg, p); else stencil_right(Z, nzg, p);
-        const int o = z0 - 2;
-        double v5 = Dz[p[4] - o][ty][tx];
-        if (left && a.ref_bugs && Z == nzg - 1) {
-            // lsTools.cu:636: id_kp2 = id_jm1 -- the z-difference one row
-            // down in y (same cell when Y == 0) at the top layer
-            const int Yb = Y == 0 ? Y : Y - 1;
-            const long ib = X + (long)nxg * Yb + sxy * Z;
-            v5 = phi[ib] - phi[ib - sxy];
-        }
-        const double v1 = Dz[p[0] - o][ty][tx], v2 = Dz[p[1] - o][ty][tx], v3 = Dz[p[2] - o][ty][tx],
-                     v4 = Dz[p[3] - o][ty][tx];
-        double phz;
-        if (pre)
-            phz = mz * weno5(v1, v2, v3, v4, v5, ez);
-        else
-            phz = weno5(v1 * cz, v2 * cz, v3 * cz, v4 * cz, v5 * cz, ez);
-        rs = rs + uz * phz;
-    }
-
-    // TVD-RK3 stage (extrapol.cu:155-212)
-    const double pin = phi[id];
-    double v;
-    if (a.stage == 1) {
-        v = fma(-a.dt, rs, pin);
-    } else {
-        const double t = fma(-a.dt, rs, pin);
-        const double p0 = a.phi0[id];
-        v = a.stage == 2 ? fma(0.25, t, 0.75 * p0) : fma(2.0, t, p0) * (1.0 / 3.0);
-    }
-    if (a.out_interior) {
-        const int g = a.g;
-        const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
-        const int I = X - g, J = Y - g, K = Z - g;
-        if (I >= 0 && I < nx && J >= 0 && J < ny && K >= 0 && K < nz)
-            a.out[I + (long)nx * (J + (long)ny * K)] = v;
-    } else {
-        a.out[id] = v;
-    }
 }
 
 } // namespace emix

@@ -1,268 +1,13 @@
-// weno_march.cu -- the level-set TVD stage as a z-marching kernel.
-//
-// Same stage as weno_stage_body (weno.cuh), arranged to do fewer FP64
-// operations per cell:
-//   * each block owns a 16 x 16 column of (x, y) cells and walks a range of z;
-//     the z differences live in a per-thread register window (one new
-//     difference per plane, no z halo), and the next plane's phi tile is
-//     loaded into registers while the current plane is computed;
-//   * besides the backward differences D(p) = phi(p) - phi(p-1), the second
-//     differences A(p) = D(p) - D(p-1) are formed once per tile position, so
-//     that a WENO5 evaluation needs 6 operations for its d_k, e_k instead of 11
-//     (weno5a below);
-//   * a warp with a cell within 2-3 cells of the padded grid's x or y faces
-//     (where the reference's edge rules move the stencil) reads the five
-//     differences of every lane at the rule's positions from the same tile;
-//     planes near the z faces read them from global memory (weno_z_general).
-#include "weno.cuh"
+// weno_march.cu -- launch of the z-marching level-set TVD stage
+// (weno_march_body, weno_march.cuh) on one grid.
+#include "weno_march.cuh"
 
 namespace emix {
 
 namespace {
 
-constexpr int kMX = 16, kMY = 16, kNT = kMX * kMY;
-constexpr int kPX = kMX + 6, kPY = kMY + 6;   // phi tile: [x0-3, x0+kMX+3) x [y0-3, y0+kMY+3)
-constexpr int kPN = kPX * kPY;
-constexpr int kPR = (kPN + kNT - 1) / kNT;     // tile values each thread loads
-
-// WENO5 of weno5() (weno.cuh) with the five differences given as v3 and the
-// four consecutive second differences a_k = v_{k+1} - v_k:
-//   d1 = a2 - a1, d2 = a3 - a2, d3 = a4 - a3,
-//   e1 = d1 + 2 a2, e2 = -(a2 + a3), e3 = d3 - 2 a3.
-// With c12 = -12 the a_k given are the negated second differences: d, e and
-// r change sign, the smoothness terms do not, so the sign goes to the
-// denominator (the right-biased stencil reads its second differences in
-// reverse order with this sign, and needs no negations).
-EMIX_DEV double weno5a(double v3, double a1, double a2, double a3, double a4, double eps4, double c12) {
-    constexpr double c13 = 13.0 / 3.0;
-    const double d1 = a2 - a1, d2 = a3 - a2, d3 = a4 - a3;
-    const double e1 = fma(2.0, a2, d1);
-    const double e2 = -(a2 + a3);
-    const double e3 = fma(-2.0, a3, d3);
-    double t1 = fma(c13 * d1, d1, fma(e1, e1, eps4)); t1 *= t1;
-    double t2 = fma(c13 * d2, d2, fma(e2, e2, eps4)); t2 *= t2;
-    double t3 = fma(c13 * d3, d3, fma(e3, e3, eps4)); t3 *= t3;
-    const double w1 = t2 * t3;
-    const double w2 = (6.0 * t1) * t3;
-    const double w3 = (3.0 * t1) * t2;
-    const double r1 = fma(3.0, e1, d1);
-    const double r2 = fma(-3.0, e2, d2);
-    const double r3 = fma(-3.0, e3, d3);
-    const double num = fma(w1, r1, fma(w2, r2, w3 * r3));
-    const double den = c12 * (w1 + w2 + w3);
-    return fma(num, rcp_newton(den), v3);
-}
-
-// z direction of a plane near the z faces: the five differences at the edge
-// rule's positions, read from global memory
-EMIX_DEV void weno_z_general(const double *phi, long id, int Z, int nzg, bool left, bool ztop_bug, long nxg,
-                             long sxy, double v[5]) {
-    int p[5];
-    if (left) stencil_left(Z, nzg, p); else stencil_right(Z, nzg, p);
-    const long base = id - (long)Z * sxy;
-    for (int k = 0; k < 5; ++k) {
-        const int q = p[k];
-        v[k] = q == 0 ? phi[base + sxy] - phi[base] : phi[base + q * sxy] - phi[base + (q - 1) * sxy];
-    }
-    if (ztop_bug) {
-        // lsTools.cu:636: id_kp2 = id_jm1 -- the z difference one row down in y
-        // (the same cell on the first row) at the top layer
-        const long ib = ((id % sxy) / nxg == 0) ? id : id - nxg;
-        v[4] = phi[ib] - phi[ib - sxy];
-    }
-}
-
-struct Plane {
-    double v[kPR];
-};
-
-EMIX_DEV void load_plane(const double *__restrict__ phi, int x0, int y0, int Z, int nxg, int nyg, int nzg,
-                         long sxy, int tid, Plane &pl) {
-#pragma unroll
-    for (int r = 0; r < kPR; ++r) {
-        const int t = tid + r * kNT;
-        double v = 0.0;
-        if (t < kPN && Z >= 0 && Z < nzg) {
-            const int gx = x0 - 3 + t % kPX, gy = y0 - 3 + t / kPX;
-            if (gx >= 0 && gx < nxg && gy >= 0 && gy < nyg) v = phi[gx + (long)nxg * gy + sxy * Z];
-        }
-        pl.v[r] = v;
-    }
-}
-
 __global__ void __launch_bounds__(kNT, 4) k_weno_march(WenoArgs a) {
-    __shared__ double P[kPY][kPX];
-    __shared__ double Dx[kMY][kMX + 5];      // positions x0-2 .. x0+kMX+2
-    __shared__ double Ax[kMY][kMX + 4];      // positions x0-1 .. x0+kMX+2
-    __shared__ double Dy[kMY + 5][kMX];      // rows y0-2 .. y0+kMY+2
-    __shared__ double Ay[kMY + 4][kMX];      // rows y0-1 .. y0+kMY+2
-
-    const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
-    const long sxy = (long)nxg * nyg;
-    const double *__restrict__ phi = a.phi;
-    const int tid = threadIdx.x, tx = tid % kMX, ty = tid / kMX;
-    const int x0 = a.r0[0] + blockIdx.x * kMX, y0 = a.r0[1] + blockIdx.y * kMY;
-    const int xe = a.r0[0] + a.rn[0], ye = a.r0[1] + a.rn[1];
-    const int zr0 = a.r0[2], zrn = a.rn[2];
-    const int chunk = (zrn + gridDim.z - 1) / gridDim.z;
-    const int zs = zr0 + blockIdx.z * chunk, ze = min(zs + chunk, zr0 + zrn);
-    const int X = x0 + tx, Y = y0 + ty;
-    const bool active = X < xe && Y < ye;
-    const long col = (long)X + (long)nxg * Y;
-    // warps (two rows of 16 cells) with a cell whose x or y stencil follows
-    // an edge rule of the padded grid
-    const bool wedge_x = __any_sync(0xffffffffu, active && (X < 2 || X > nxg - 4));
-    const bool wedge_y = __any_sync(0xffffffffu, active && (Y < 2 || Y > nyg - 4));
-
-    const int g = a.g;
-    const int nx = nxg - 2 * g, ny = nyg - 2 * g, nz = nzg - 2 * g;
-    const long nv = a.reflect ? (long)nx * ny * nz : sxy * nzg;
-    const bool pre = a.wce != nullptr;
-
-    // z window of this column: phi(z), 0 outside the grid
-    auto ld = [&](int z) { return (active && z >= 0 && z < nzg) ? phi[col + sxy * z] : 0.0; };
-    // Dz[t] = D(Z - 2 + t), t = 0..5; Az[t] = A(Z - 1 + t), t = 0..4; fz = phi(Z + 3)
-    double Dz[6], Az[5], fz;
-    {
-        double f[7];
-#pragma unroll
-        for (int t = 0; t < 7; ++t) f[t] = ld(zs - 3 + t);
-#pragma unroll
-        for (int t = 0; t < 6; ++t) Dz[t] = (zs - 2 + t == 0) ? ld(1) - ld(0) : f[t + 1] - f[t];
-#pragma unroll
-        for (int t = 0; t < 5; ++t) Az[t] = Dz[t + 1] - Dz[t];
-        fz = f[6];
-    }
-
-    Plane pl;
-    if (zs < ze) load_plane(phi, x0, y0, zs, nxg, nyg, nzg, sxy, tid, pl);
-    for (int Z = zs; Z < ze; ++Z) {
-        // ---- this plane's tile (loaded during the previous plane) ----
-#pragma unroll
-        for (int r = 0; r < kPR; ++r) {
-            const int t = tid + r * kNT;
-            if (t < kPN) P[t / kPX][t % kPX] = pl.v[r];
-        }
-        __syncthreads();
-        // the next plane's tile and z value, in flight during this plane
-        if (Z + 1 < ze) load_plane(phi, x0, y0, Z + 1, nxg, nyg, nzg, sxy, tid, pl);
-        const double fnext = ld(Z + 4);
-        for (int t = tid; t < kMY * (kMX + 5); t += kNT) {
-            const int i = t % (kMX + 5), j = t / (kMX + 5);
-            const int gx = x0 - 2 + i;   // P column i + 1
-            Dx[j][i] = gx == 0 ? P[j + 3][i + 2] - P[j + 3][i + 1] : P[j + 3][i + 1] - P[j + 3][i];
-        }
-        for (int t = tid; t < (kMY + 5) * kMX; t += kNT) {
-            const int i = t % kMX, j = t / kMX;
-            const int gy = y0 - 2 + j;   // P row j + 1
-            Dy[j][i] = gy == 0 ? P[j + 2][i + 3] - P[j + 1][i + 3] : P[j + 1][i + 3] - P[j][i + 3];
-        }
-        __syncthreads();
-        for (int t = tid; t < kMY * (kMX + 4); t += kNT) {
-            const int i = t % (kMX + 4), j = t / (kMX + 4);
-            Ax[j][i] = Dx[j][i + 1] - Dx[j][i];
-        }
-        for (int t = tid; t < (kMY + 4) * kMX; t += kNT) {
-            const int i = t % kMX, j = t / kMX;
-            Ay[j][i] = Dy[j + 1][i] - Dy[j][i];
-        }
-        __syncthreads();
-
-        if (active) {
-            const long id = col + sxy * Z;
-            long iv = id;
-            if (a.reflect)
-                iv = mirror(X, g, nx) + (long)nx * (mirror(Y, g, ny) + (long)ny * mirror(Z, g, nz));
-            double rs = 0.0;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const double u = a.vel[d * nv + iv];
-                double mx, ex;
-                if (pre) {
-                    const double2 ce = weno_scale(a.wce, d, nv, iv);
-                    mx = ce.x;
-                    ex = ce.y;
-                } else {
-                    const double jd = a.jbn[4 * d * nv + iv] * (d == 0 ? a.sx : (d == 1 ? a.sy : a.sz));
-                    // W(C v; eps) = C W(v; eps / C^2)
-                    mx = jd;
-                    ex = kWenoEps4 / (jd * jd);
-                }
-                const bool left = __double_as_longlong(u) >= 0;
-                // the five differences as v3 and the second differences a1..a4;
-                // the upwind side is chosen by selects (no divergent WENO5)
-                double v3, a1, a2, a3, a4, c12 = left ? 12.0 : -12.0;
-                if ((d == 0 && !wedge_x) || (d == 1 && !wedge_y)) {
-                    // left: v3 = D(c), a = A(c-1..c+2); right: v3 = D(c+1),
-                    // a = -A(c+3..c), given as A(c+3..c) with the sign in c12
-                    // -- tile index of D(c) is t + 2, of A(c) t + 1
-                    const int o = left ? 0 : 4, st = left ? 1 : -1, ov = left ? 2 : 3;
-                    if (d == 0) {
-                        const double *ar = &Ax[ty][tx];
-                        v3 = Dx[ty][tx + ov];
-                        a1 = ar[o]; a2 = ar[o + st]; a3 = ar[o + 2 * st]; a4 = ar[o + 3 * st];
-                    } else {
-                        v3 = Dy[ty + ov][tx];
-                        a1 = Ay[ty + o][tx]; a2 = Ay[ty + o + st][tx]; a3 = Ay[ty + o + 2 * st][tx];
-                        a4 = Ay[ty + o + 3 * st][tx];
-                    }
-                } else if (d == 2 && Z >= 2 && Z <= nzg - 4) {
-                    v3 = left ? Dz[2] : Dz[3];
-                    a1 = left ? Az[0] : Az[4];
-                    a2 = left ? Az[1] : Az[3];
-                    a3 = Az[2];
-                    a4 = left ? Az[3] : Az[1];
-                } else {
-                    // edge rules: the differences at the rule's positions
-                    double v[5];
-                    if (d == 2) {
-                        const bool bug = left && a.ref_bugs && Z == nzg - 1;
-                        weno_z_general(phi, id, Z, nzg, left, bug, nxg, sxy, v);
-                    } else {
-                        int p[5];
-                        const int c = d == 0 ? X : Y, L = d == 0 ? nxg : nyg;
-                        if (left) stencil_left(c, L, p); else stencil_right(c, L, p);
-                        if (d == 0) {
-                            for (int k = 0; k < 5; ++k) v[k] = Dx[ty][p[k] - (x0 - 2)];
-                        } else {
-                            for (int k = 0; k < 5; ++k) v[k] = Dy[p[k] - (y0 - 2)][tx];
-                        }
-                    }
-                    v3 = v[2];
-                    a1 = v[1] - v[0]; a2 = v[2] - v[1]; a3 = v[3] - v[2]; a4 = v[4] - v[3];
-                    c12 = 12.0;
-                }
-                const double W = weno5a(v3, a1, a2, a3, a4, ex, c12);
-                rs = fma(u, mx * W, rs);
-            }
-            // TVD-RK3 stage (extrapol.cu:155-212)
-            const double pin = P[ty + 3][tx + 3];
-            double v;
-            if (a.stage == 1) {
-                v = fma(-a.dt, rs, pin);
-            } else {
-                const double t = fma(-a.dt, rs, pin);
-                const double p0 = a.phi0[id];
-                v = a.stage == 2 ? fma(0.25, t, 0.75 * p0) : fma(2.0, t, p0) * (1.0 / 3.0);
-            }
-            if (a.out_interior) {
-                const int I = X - g, J = Y - g, K = Z - g;
-                if (I >= 0 && I < nx && J >= 0 && J < ny && K >= 0 && K < nz)
-                    a.out[I + (long)nx * (J + (long)ny * K)] = v;
-            } else {
-                a.out[id] = v;
-            }
-        }
-        // ---- advance the z window ----
-#pragma unroll
-        for (int t = 0; t < 5; ++t) Dz[t] = Dz[t + 1];
-        Dz[5] = fnext - fz;   // D(Z + 4); Z + 4 > 0
-        fz = fnext;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) Az[t] = Az[t + 1];
-        Az[4] = Dz[5] - Dz[4];
-        __syncthreads();
-    }
+    weno_march_body(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.z);
 }
 
 } // namespace
