@@ -304,11 +304,17 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=N
     om, cs = w.impeller.omega, w.cs
     r.run(om, cs)                     # warm-up (graph capture, tables)
     r.adj.backward()
-    t0 = time.perf_counter()
-    J = r.run(om, cs)
-    t1 = time.perf_counter()
-    g = r.adj.backward()
-    t2 = time.perf_counter()
+    # forward (with checkpoints) and reverse sweep, three times: the medians
+    fw, bw = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        J = r.run(om, cs)
+        t1 = time.perf_counter()
+        g = r.adj.backward()
+        t2 = time.perf_counter()
+        fw.append(t1 - t0)
+        bw.append(t2 - t1)
+    t_fw, t_bw = float(np.median(fw)), float(np.median(bw))
     fds, rich = [], []
 
     def cfd(k, p0, h):
@@ -323,18 +329,20 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=N
         # omega moves the blades: a step small enough that no cell changes side
         h = (1e-3 if k == 0 else 1e-2) * abs(p0)
         rich.append((4.0 * cfd(k, p0, 0.5 * h) - cfd(k, p0, h)) / 3.0)
-    # plain steps without checkpoints, for the cost ratio
+    # plain steps without checkpoints, for the cost ratio (median of three)
     r.ctx.upload(w.um, w.phi)
     r.ctx.step(1, use_graph=True)
     torch.cuda.synchronize()
-    t3 = time.perf_counter()
-    r.ctx.step(nsteps, use_graph=True)
-    torch.cuda.synchronize()
-    t4 = time.perf_counter()
+    pl = []
+    for _ in range(3):
+        t3 = time.perf_counter()
+        r.ctx.step(nsteps, use_graph=True)
+        torch.cuda.synchronize()
+        pl.append(time.perf_counter() - t3)
     gib = r.adj.device_bytes() / 2**30
     r.close()
     cells = w.grid.ncell
-    plain = t4 - t3
+    plain = float(np.median(pl))
     return {
         "workload": f"stirred tank {n}x{n}x{nz or n} walls + rotating impeller, {nsteps} RK3 steps, "
                     "J = annulus kinetic energy + interface area",
@@ -343,10 +351,11 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=N
         "rel_err": [abs(g[0] - fds[0]) / abs(fds[0]), abs(g[1] - fds[1]) / abs(fds[1])] if fds else None,
         "richardson_fd": rich or None,
         "rel_err_richardson": [abs(g[i] - rich[i]) / abs(rich[i]) for i in range(2)] if rich else None,
-        "forward_s": round(t1 - t0, 4), "backward_s": round(t2 - t1, 4), "plain_steps_s": round(plain, 4),
-        "adjoint_over_forward": round((t2 - t1) / plain, 3),
+        "forward_s": round(t_fw, 4), "backward_s": round(t_bw, 4), "plain_steps_s": round(plain, 4),
+        "timing": "medians of three runs each",
+        "adjoint_over_forward": round(t_bw / plain, 3),
         "forward_value": round(cells * nsteps / plain / 1e6, 3),
-        "adjoint_value": round(cells * nsteps / (t2 - t1) / 1e6, 3),
+        "adjoint_value": round(cells * nsteps / t_bw / 1e6, 3),
         "unit": "Mcell-RK3-steps/s", "checkpoint_every": every, "adjoint_gib": round(gib, 2),
     }
 

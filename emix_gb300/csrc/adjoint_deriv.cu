@@ -5,7 +5,8 @@
 // the x pencils, whose lines stay in L1 across the walk).  Forward sweep of
 // A^T into the scratch w, backward sweep with a 7-value register window of z
 // from which out_j = sum_k B^T[j][k] z_{j+k-3} is finished as soon as its last
-// z is known.  The cyclic scheme is anti-self-adjoint (D^T = -D) and uses the
+// z is known (4 operations on the interior rows, where B^T is the
+// antisymmetric 5-point stencil).  The cyclic scheme is anti-self-adjoint (D^T = -D) and uses the
 // forward kernels with a negated table.
 #include "adjoint.cuh"
 
@@ -42,29 +43,53 @@ __global__ void __launch_bounds__(128) k_deriv_t(DerivTTable T, PencilFields F, 
         y = fma(-r.m, y, in[i * s] * r.ib);
         w[i * s] = y;
     }
-    // backward: z_i = y_i - g_i z_{i+1}; zq[t] = z_{i+t}
+    // backward: z_i = y_i - g_i z_{i+1}; zq[t] = z_{i+t}; out_j, j = i + 3,
+    // once z_i is known.  Three branch-free runs of j: the closure rows at the
+    // top, the interior rows (4 operations on the antisymmetric stencil), the
+    // closure rows at the bottom.
     double zq[7];
 #pragma unroll
     for (int t = 0; t < 7; ++t) zq[t] = 0.0;
     double z = 0.0;
-    for (int i = L - 1; i >= -3; --i) {
+    auto advance = [&](int i) {
 #pragma unroll
         for (int t = 6; t > 0; --t) zq[t] = zq[t - 1];
         if (i >= 0) {
-            z = (i == L - 1) ? w[i * s] : fma(-R[i].g, z, w[i * s]);
+            const double wi = w[i * s];
+            z = (i == L - 1) ? wi : fma(-R[i].g, z, wi);
             zq[0] = z;
         } else {
             zq[0] = 0.0;
         }
-        const int j = i + 3;
-        if (j < L) {
-            const double *b = BT + 7 * (long)j;
-            double o = b[0] * zq[0];
+    };
+    auto put = [&](int j, double o) {
+        if (ACC) out[j * s] += o;
+        else out[j * s] = o;
+    };
+    auto general = [&](int j) {
+        const double *b = BT + 7 * (long)j;
+        double o = b[0] * zq[0];
 #pragma unroll
-            for (int t = 1; t < 7; ++t) o = fma(b[t], zq[t], o);
-            if (ACC) out[j * s] += o;
-            else out[j * s] = o;
+        for (int t = 1; t < 7; ++t) o = fma(b[t], zq[t], o);
+        put(j, o);
+    };
+    const bool fast = T.jlo <= T.jhi;
+    const int jtop = fast ? T.jhi : -1;   // rows above jtop: closure rows
+    const int jbot = fast ? T.jlo : 0;    // rows below jbot: closure rows
+    int i = L - 1;
+    for (; i >= -3 && i + 3 > jtop; --i) {
+        advance(i);
+        if (i + 3 < L) general(i + 3);
+    }
+    if (fast) {
+        for (; i + 3 >= jbot; --i) {
+            advance(i);
+            put(i + 3, fma(T.ta, zq[2] - zq[4], T.tb * (zq[1] - zq[5])));
         }
+    }
+    for (; i >= -3; --i) {
+        advance(i);
+        general(i + 3);
     }
 }
 

@@ -88,6 +88,10 @@ struct DerivTTable {
     int n, periodic;
     const DerivTRow *rows;
     const double *bt;
+    // rows jlo..jhi of B^T are the interior's antisymmetric stencil
+    // tb z_{j-2} + ta z_{j-1} - ta z_{j+1} - tb z_{j+2} (jlo > jhi: none)
+    int jlo, jhi;
+    double ta, tb;
     DerivTable neg;
 };
 int get_deriv_t_table(int scheme, int n, double h, DerivTTable *out);

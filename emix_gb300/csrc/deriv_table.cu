@@ -355,6 +355,21 @@ int get_deriv_t_table(int scheme, int n, double h, DerivTTable *out) {
         EMIX_CUDA_TRY(cudaMemcpy(buf, host.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
         t.rows = reinterpret_cast<const DerivTRow *>(buf);
         t.bt = buf + 3 * (size_t)n;
+        // the run of rows around the middle equal to the middle row, when
+        // that row is the antisymmetric 5-point stencil
+        const double *mid = bt.data() + 7 * (size_t)(n / 2);
+        t.jlo = 1;
+        t.jhi = 0;
+        if (mid[0] == 0.0 && mid[3] == 0.0 && mid[6] == 0.0 && mid[4] == -mid[2] && mid[5] == -mid[1]) {
+            auto same = [&](int j) { return std::memcmp(bt.data() + 7 * (size_t)j, mid, 7 * sizeof(double)) == 0; };
+            int lo = n / 2, hi = n / 2;
+            while (lo > 0 && same(lo - 1)) --lo;
+            while (hi < n - 1 && same(hi + 1)) ++hi;
+            t.jlo = lo;
+            t.jhi = hi;
+            t.ta = mid[2];
+            t.tb = mid[1];
+        }
     }
     std::lock_guard<std::mutex> lock(g_t_mu);
     g_t_tables[key] = t;
