@@ -129,7 +129,8 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
     } else {
         double fm2 = in[(n - 2) * s], fm1 = in[(n - 1) * s], f0 = in[0], fp1 = in[s];
         double nxt = in[2 * s];
-        for (; i < n; ++i) {
+        // rows [0, ku) also accumulate y0 (branch-free runs)
+        auto prow = [&](int i, bool acc) {
             const double fp2 = nxt;
             int j = i + 3;
             if (j >= n) j -= n;
@@ -137,10 +138,13 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
             const DerivRow r = rows[i];
             const double v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * wp;
             w[i * s] = v;
-            if (i < T.ku) y0 += T.u0[i] * v;
+            if (acc) y0 += T.u0[i] * v;
             wp = v;
             fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
-        }
+        };
+        const int ku = T.ku < n ? T.ku : n;
+        for (; i < ku; ++i) prow(i, true);
+        for (; i < n; ++i) prow(i, false);
     }
 
     // backward sweep; w (and the accumulated output) from queues of four rows
@@ -160,7 +164,8 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
         o2 = n - 3 >= 0 ? out[(n - 3) * s] : 0.0;
         o3 = n - 4 >= 0 ? out[(n - 4) * s] : 0.0;
     }
-    for (i = n - 1; i >= 0; --i) {
+    // one row; the cyclic correction only where zz is nonzero
+    auto row = [&](int i, bool corr) {
         const double wi = w0, oi = o0;
         w0 = w1; w1 = w2; w2 = w3;
         if (i - 4 >= 0) w3 = w[(i - 4) * s];
@@ -171,9 +176,19 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
         const double y = wi - rows[i].g * yn;
         yn = y;
         double xv = y;
-        if (T.periodic && (i < T.zlo || i >= T.zhi)) xv = y - fact * T.zz[i];
+        if (corr) xv = y - fact * T.zz[i];
         if (EPI == EPI_ACCUM) xv += oi;
         out[i * s] = xv;
+    };
+    // branch-free runs: the correction rows [zhi, n) and [0, zlo) of the
+    // cyclic operator, none for the closed one
+    i = n - 1;
+    if (T.periodic) {
+        for (; i >= T.zhi; --i) row(i, true);
+        for (; i >= T.zlo; --i) row(i, false);
+        for (; i >= 0; --i) row(i, true);
+    } else {
+        for (; i >= 0; --i) row(i, false);
     }
 }
 
@@ -253,9 +268,22 @@ EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npen
                     }
                 }
             }
-            for (; r < cl; ++r) {
+            // one interior row (fp2 given); y0 accumulated on request
+            auto irow = [&](int r, double fp2, bool acc) {
                 const int i = c0 + r;
-                if (!T.periodic && i >= n - T.nhi) {
+                const DerivRow rw = rows[i];
+                const double v = rw.A * (fp1 - fm1) + rw.B * (fp2 - fm2) - rw.m * wp;
+                if (acc) y0 += T.u0[i] * v;
+                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+                t[r] = v;
+                wp = v;
+            };
+            // branch-free runs of rows
+            if (!T.periodic) {
+                const int rint = min(cl, n - T.nhi - c0);   // rows before the closures
+                for (; r < rint; ++r) irow(r, t[r + 2], false);
+                for (; r < cl; ++r) {
+                    const int i = c0 + r;
                     // closures on f_{n-1}..f_{n-4} (nhi == 2): at row n-2 the
                     // window holds exactly those four values
                     if (i == n - T.nhi) { tail0 = fp1; tail1 = f0; tail2 = fm1; tail3 = fm2; }
@@ -264,15 +292,16 @@ EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npen
                                      rows[i].m * wp;
                     t[r] = v;
                     wp = v;
-                    continue;
                 }
-                const double fp2 = (i + 2 < n) ? t[r + 2] : (i + 2 == n ? head0 : head1);
-                const DerivRow rw = rows[i];
-                const double v = rw.A * (fp1 - fm1) + rw.B * (fp2 - fm2) - rw.m * wp;
-                if (T.periodic && i < T.ku) y0 += T.u0[i] * v;
-                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
-                t[r] = v;
-                wp = v;
+            } else {
+                const int rku = max(r, min(cl, T.ku - c0));     // rows i < ku: accumulate y0
+                const int rnw = max(rku, min(cl, n - 2 - c0));  // rows i + 2 < n: no wrap
+                for (; r < rku; ++r) {
+                    const int i = c0 + r;
+                    irow(r, (i + 2 < n) ? t[r + 2] : (i + 2 == n ? head0 : head1), true);
+                }
+                for (; r < rnw; ++r) irow(r, t[r + 2], false);
+                for (; r < cl; ++r) irow(r, c0 + r + 2 == n ? head0 : head1, false);
             }
         }
         __syncwarp();
@@ -290,13 +319,21 @@ EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npen
             if (lane < cl) tile[q * kXLd + lane] = w[(long)q * n + c0 + lane];
         __syncwarp();
         if (mine) {
-            for (int r = cl - 1; r >= 0; --r) {
-                const int i = c0 + r;
-                const double y = t[r] - rows[i].g * yn;
-                yn = y;
-                double xv = y;
-                if (T.periodic && (i < T.zlo || i >= T.zhi)) xv = y - fact * T.zz[i];
-                t[r] = xv;
+            if (!T.periodic) {
+                for (int r = cl - 1; r >= 0; --r) {
+                    const double y = t[r] - rows[c0 + r].g * yn;
+                    yn = y;
+                    t[r] = y;
+                }
+            } else {
+                for (int r = cl - 1; r >= 0; --r) {
+                    const int i = c0 + r;
+                    const double y = t[r] - rows[i].g * yn;
+                    yn = y;
+                    double xv = y;
+                    if (i < T.zlo || i >= T.zhi) xv = y - fact * T.zz[i];
+                    t[r] = xv;
+                }
             }
         }
         __syncwarp();
