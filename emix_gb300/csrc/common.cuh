@@ -40,6 +40,37 @@ inline size_t ncell(int nx, int ny, int nz) { return (size_t)nx * (size_t)ny * (
 //   x_i  = w_i - g_i x_{i+1}                                        (backward)
 // where the 1/h scale and the Thomas pivot 1/bet_i are already folded into
 // A_i, B_i, C_{i,k}.  Periodic operators add the Sherman-Morrison terms.
+// Reciprocal seeded from the single-precision reciprocal of d's mantissa
+// (d's exponent applied by integer arithmetic), then one third-order step of
+// the iteration for 1/d: with e = 1 - d x, x <- x (1 + e + e^2), the first
+// terms of x / (1 - e) (J.-M. Muller et al., Handbook of Floating-Point
+// Arithmetic, 2nd ed., section 4.7, on Newton-Raphson-like iterations).  The
+// seed's relative error is below 2^-22, so the step's error e^3 is below
+// 2^-66: a correctly rounded result up to the last operation's rounding.
+// Three FMAs.  For normal d of either sign well inside the double range.
+EMIX_DEV double rcp_newton(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int ebits = (int)(b >> 52) & 0x7ff;                       // biased exponent
+    const unsigned int mant = (unsigned int)((b >> 29) & 0x7fffff); // top 23 mantissa bits
+    const float m = __uint_as_float(0x3f800000u | mant);            // in [1, 2)
+    const unsigned int rf = __float_as_uint(__frcp_rn(m));          // in (0.5, 1]
+    // rebuild 1/m as a double and scale by 2^-(ebits-1023)
+    const int fexp = (int)(rf >> 23) & 0xff;
+    const unsigned long long rm = ((unsigned long long)(fexp - 127 + 1023 - (ebits - 1023)) << 52) |
+                                  ((unsigned long long)(rf & 0x7fffff) << 29);
+    // d's sign on the seed: the step below then converges for negative d too
+    const double x = __longlong_as_double((long long)(rm | (b & 0x8000000000000000ull)));
+    const double e = fma(-d, x, 1.0);
+    return fma(x, fma(e, e, e), x);
+}
+
+// 1/d by rcp_newton where its exponent arithmetic is safe (|d| within
+// 2^-1021 .. 2^1020), by division otherwise (zero, subnormal, huge, inf, NaN).
+EMIX_DEV double rcp_fast(double d) {
+    const int ebits = (int)((unsigned long long)__double_as_longlong(d) >> 52) & 0x7ff;
+    return (ebits >= 2 && ebits <= 2043) ? rcp_newton(d) : 1.0 / d;
+}
+
 struct DerivRow {
     double A, B, m, g;
 };

@@ -33,7 +33,7 @@ struct PrimArgs {
 EMIX_DEV void prim_cell(const PrimArgs &a, long q) {
     const long n = a.n;
     const double r = a.um[q];
-    const double rr = 1.0 / r;
+    const double rr = rcp_fast(r);
     a.pres[q] = r * a.inv_m2;
     a.u[q] = a.um[n + q] * rr;
     a.u[n + q] = a.um[2 * n + q] * rr;
@@ -254,19 +254,30 @@ __host__ __device__ inline long rk_count(const RkArgs &a) {
 // RK3 combination of one cell (rungek_ico.f90:89-90, 153-154, 217-220)
 EMIX_DEV void rk_combine(const RkArgs &a, long q, double v[5]) {
     const long n = a.n;
-    const double dt = a.dt;
-    const double j11 = a.jbn[10 * n + q];
+    // the substep's weight of dt*R times the metric factor jbn(11), once per cell
+    const double w = a.stage == 1 ? a.dt : (a.stage == 2 ? 0.25 * a.dt : (2.0 / 3.0) * a.dt);
+    const double cj = w * a.jbn[10 * n + q];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-        const double rs = j11 * a.R[m * n + q];
         const double u0 = a.um0[m * n + q];
+        double b;
         if (a.stage == 1)
-            v[m] = u0 + dt * rs;
+            b = u0;
         else if (a.stage == 2)
-            v[m] = 0.75 * u0 + 0.25 * a.um[m * n + q] + (0.25 * dt) * rs;
+            b = fma(0.25, a.um[m * n + q], 0.75 * u0);
         else
-            v[m] = (1.0 / 3.0) * u0 + (2.0 / 3.0) * a.um[m * n + q] + ((2.0 / 3.0) * dt) * rs;
+            b = fma(2.0 / 3.0, a.um[m * n + q], (1.0 / 3.0) * u0);
+        v[m] = fma(cj, a.R[m * n + q], b);
     }
+}
+
+// fmax(-6, fmin(6, x)) by integer compares on the bit pattern (|x| > 6 takes
+// 6 with x's sign; a NaN also becomes +-6)
+EMIX_DEV double clip6(double x) {
+    const long long b = __double_as_longlong(x);
+    const long long six = 0x4018000000000000LL;   // 6.0
+    return (b & 0x7fffffffffffffffLL) > six ? __longlong_as_double((b & (long long)0x8000000000000000ULL) | six)
+                                            : x;
 }
 
 // varc_to_varnc + clip + mask + varc_to_varnc (:104-124), then the rebuild
@@ -280,19 +291,15 @@ EMIX_DEV void rk_convert(const RkArgs &a, long q, double v[5]) {
                             a.xyz[n + q], a.xyz[2 * n + q], v, nullptr);
     }
     const double r = v[0];
-    const double rr = 1.0 / r;
+    const double rr = rcp_fast(r);
     const double mk = a.mask[q];
+    // velocity, clipped and masked; the reference's masked momentum u r mk
+    // divided by r again is u mk
     double uu[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double x = v[d + 1] * rr;
-        x = fmin(6.0, x);
-        x = fmax(-6.0, x);
-        const double mom = x * r * mk;
-        uu[d] = mom * rr;
-    }
+    for (int d = 0; d < 3; ++d) uu[d] = clip6(v[d + 1] * rr) * mk;
     const double p = r * a.inv_m2;
-    const double r1 = p * a.mach * a.mach;
+    const double r1 = p * (a.mach * a.mach);
     a.out[q] = r1;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {

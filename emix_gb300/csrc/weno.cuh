@@ -70,30 +70,6 @@ EMIX_DEV double2 weno_scale(const double *wce, int d, long nv, long iv) {
     return reinterpret_cast<const double2 *>(wce)[d * nv + iv];
 }
 
-// Reciprocal seeded from the single-precision reciprocal of d's mantissa
-// (d's exponent applied by integer arithmetic), then one third-order step of
-// the iteration for 1/d: with e = 1 - d x, x <- x (1 + e + e^2), the first
-// terms of x / (1 - e) (J.-M. Muller et al., Handbook of Floating-Point
-// Arithmetic, 2nd ed., section 4.7, on Newton-Raphson-like iterations).  The
-// seed's relative error is below 2^-22, so the step's error e^3 is below
-// 2^-66: a correctly rounded result up to the last operation's rounding.
-// Three FMAs.  For normal d of either sign well inside the double range.
-EMIX_DEV double rcp_newton(double d) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const int ebits = (int)(b >> 52) & 0x7ff;                       // biased exponent
-    const unsigned int mant = (unsigned int)((b >> 29) & 0x7fffff); // top 23 mantissa bits
-    const float m = __uint_as_float(0x3f800000u | mant);            // in [1, 2)
-    const unsigned int rf = __float_as_uint(__frcp_rn(m));          // in (0.5, 1]
-    // rebuild 1/m as a double and scale by 2^-(ebits-1023)
-    const int fexp = (int)(rf >> 23) & 0xff;
-    const unsigned long long rm = ((unsigned long long)(fexp - 127 + 1023 - (ebits - 1023)) << 52) |
-                                  ((unsigned long long)(rf & 0x7fffff) << 29);
-    // d's sign on the seed: the step below then converges for negative d too
-    const double x = __longlong_as_double((long long)(rm | (b & 0x8000000000000000ull)));
-    const double e = fma(-d, x, 1.0);
-    return fma(x, fma(e, e, e), x);
-}
-
 // Jiang-Peng WENO5 reconstruction from five differences (Phi_x_WENO,
 // src/LevelSet/lsTools.cu:9-50).  Same weights 0.1/0.6/0.3 and
 // epsilon = 1e-6 on (beta + eps)^2, rearranged to cut FP64 operations:
