@@ -71,6 +71,33 @@ EMIX_DEV double rcp_fast(double d) {
     return (ebits >= 2 && ebits <= 2043) ? rcp_newton(d) : 1.0 / d;
 }
 
+// sqrt(x) from the single-precision reciprocal square root of x's mantissa
+// (exponent halved by integer arithmetic), then one third-order step: with
+// s = x y and e = 1 - s y, sqrt(x) = s (1 - e)^(-1/2) ~ s (1 + e/2 + 3e^2/8),
+// the first terms of the binomial series (the same family of iterations as
+// rcp_newton, Muller et al., section 4.7).  The seed's relative error is below
+// 2^-21, the step's below 2^-60: within an ulp of the correctly rounded root.
+// Five FP64 operations; zero, negative, subnormal, huge, inf and NaN
+// arguments go to sqrt().
+EMIX_DEV double sqrt_fast(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ebits = (int)(b >> 52) & 0x7ff;
+    if (ebits < 2 || ebits > 2045 || (b >> 63)) return sqrt(x);
+    const int e = ebits - 1023;   // x = m 2^e, m in [1, 2)
+    const int odd = e & 1;
+    // f = m 2^odd in [1, 4), top 23 mantissa bits
+    const float f = __uint_as_float(((127u + (unsigned)odd) << 23) | (unsigned int)((b >> 29) & 0x7fffff));
+    const unsigned int rb = __float_as_uint(rsqrtf(f));
+    // y = rsqrt(f) 2^-((e - odd) / 2)
+    const int half = (e - odd) / 2;
+    const int fexp = (int)(rb >> 23) & 0xff;
+    const double y = __longlong_as_double(
+        (long long)(((unsigned long long)(fexp - 127 + 1023 - half) << 52) | ((unsigned long long)(rb & 0x7fffff) << 29)));
+    const double s = x * y;
+    const double ee = fma(-s, y, 1.0);
+    return fma(s, ee * fma(0.375, ee, 0.5), s);
+}
+
 struct DerivRow {
     double A, B, m, g;
 };

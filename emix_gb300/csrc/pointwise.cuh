@@ -71,22 +71,23 @@ EMIX_DEV void flux_cell(const FluxArgs &a, long q) {
     const double sxz = j1 * dv[2 * n] + j9 * dv[6 * n];    // :79-81 and :147-149
     const double syz = j9 * dv[7 * n] + j5 * dv[5 * n];    // :123-125 and :157-159
     const double vxy = vs * sxy, vxz = vs * sxz, vyz = vs * syz;
+    const double vs2 = vs + vs;   // the normal viscous terms' 2 vis
     // equation 1
     a.F[0][q] = JX * (-um2);
     a.F[1][q] = JY * (-um3);
     a.F[2][q] = JZ * (-um4);
     // equation 2
-    a.F[3][q] = JX * ((-um2 * u1 - p) + vs * (2.0 * sxx));
+    a.F[3][q] = JX * ((-um2 * u1 - p) + vs2 * sxx);
     a.F[4][q] = JY * (-um3 * u1 + vxy);
     a.F[5][q] = JZ * (-um4 * u1 + vxz);
     // equation 3
     a.F[6][q] = JX * (-um2 * u2 + vxy);
-    a.F[7][q] = JY * ((-um3 * u2 - p) + vs * (2.0 * syy));
+    a.F[7][q] = JY * ((-um3 * u2 - p) + vs2 * syy);
     a.F[8][q] = JZ * (-um4 * u2 + vyz);
     // equation 4
     a.F[9][q] = JX * (-um2 * u3 + vxz);
     a.F[10][q] = JY * (-um3 * u3 + vyz);
-    a.F[11][q] = JZ * ((-um4 * u3 - p) + vs * (2.0 * szz));
+    a.F[11][q] = JZ * ((-um4 * u3 - p) + vs2 * szz);
     // equation 5
     a.F[12][q] = JX * (-u1 * um5);
     a.F[13][q] = JY * (-u2 * um5);
@@ -111,7 +112,7 @@ EMIX_DEV void smag_cell(const SmagArgs &a, long q) {
     const double s12 = 0.5 * (uy + vx), s13 = 0.5 * (uz + wx), s23 = 0.5 * (vz + wy);
     const double ss = ux * ux + vy * vy + wz * wz + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23);
     const double cd = a.cs * a.dxyz[q];
-    const double am = cd * cd * sqrt(2.0 * ss);
+    const double am = cd * cd * sqrt_fast(2.0 * ss);
     if (a.amut) a.amut[q] = am;
     a.vis[q] = a.c4 * 1.0 + am;
 }
@@ -163,7 +164,7 @@ EMIX_DEV void sf_cell(const SfArgs &a, long q) {
     x = (U[p] - U[m]) * r; y = (V[p] - V[m]) * r; z = (W[p] - W[m]) * r;
     s = s + x * x + y * y + z * z;
     s = s * (1.0 / 6.0);
-    a.amut[q] = a.amu0 * sqrt(s) * a.dxyz[q];
+    a.amut[q] = a.amu0 * sqrt_fast(s) * a.dxyz[q];
 }
 
 // VORT (:330-341)
