@@ -97,8 +97,8 @@ IMPELLER = True
 # stirred_tank_192.txt, profiles/weno_stage_stirred_tank_192.txt).
 FP64_OPS_PER_CELL = {
     "weno_stage": 125.2, "grad_x": 18.0, "grad_y": 18.0, "grad_z": 18.0,
-    "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 45.0, "sgs": 31.0,
-    "rk_post": 31.9,
+    "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 43.0, "sgs": 28.0,
+    "rk_post": 22.8,
 }
 
 # DRAM bytes (read + write) per cell a launch covers, from the same ncu
