@@ -36,10 +36,11 @@ EMIX_DEV double weno5_grad(double v1, double v2, double v3, double v4, double v5
     const double r1 = d1 + 3.0 * e1, r2 = d2 - 3.0 * e2, r3 = d3 - 3.0 * e3;
     const double S = w1 + w2 + w3;
     const double N = w1 * r1 + w2 * r2 + w3 * r3;
-    const double q = 1.0 / (12.0 * S);
+    const double iS = rcp_fast(S);
+    const double q = iS * (1.0 / 12.0);
     const double W = v3 + N * q;
     // dW = dv3 + q (sum w_k dr_k + sum dw_k (r_k - N/S))
-    const double NS = N / S;
+    const double NS = N * iS;
     const double a1 = q * (r1 - NS), a2 = q * (r2 - NS), a3 = q * (r3 - NS);
     // dw: dt1 (6 t3 a2 + 3 t2 a3) + dt2 (t3 a1 + 3 t1 a3) + dt3 (t2 a1 + 6 t1 a2)
     const double lt1 = 6.0 * t3 * a2 + 3.0 * t2 * a3;
@@ -61,7 +62,7 @@ EMIX_DEV double weno5_grad(double v1, double v2, double v3, double v4, double v5
 // ---- primitive variables ---------------------------------------------------
 EMIX_DEV void prim_adj(const double um[4], double inv_m2, const double lu[3], double lp,
                        double lum[4]) {
-    const double r = um[0], rr = 1.0 / r;
+    const double r = um[0], rr = rcp_fast(r);
     double l0 = lp * inv_m2;
     for (int d = 0; d < 3; ++d) {
         lum[d + 1] += lu[d] * rr;
@@ -118,10 +119,10 @@ EMIX_DEV double smag_adj(const double dv[9], double j1, double j5, double j9, do
     const double uz = j9 * dv[6], vz = j9 * dv[7], wz = j9 * dv[8];
     const double s12 = 0.5 * (uy + vx), s13 = 0.5 * (uz + wx), s23 = 0.5 * (vz + wy);
     const double ss = ux * ux + vy * vy + wz * wz + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23);
-    const double root = sqrt(2.0 * ss);
+    const double root = sqrt_fast(2.0 * ss);
     const double cd = cs * delta;
     if (root > 0.0) {
-        const double lss = lvis * cd * cd / root;
+        const double lss = lvis * cd * cd * rcp_fast(root);
         const double l12 = 2.0 * lss * s12, l13 = 2.0 * lss * s13, l23 = 2.0 * lss * s23;
         ldv[0] += j1 * 2.0 * ux * lss;
         ldv[4] += j5 * 2.0 * vy * lss;
@@ -158,7 +159,7 @@ EMIX_DEV void convert_adj(const RkArgs &a, long q, const double v_in[5], const d
         }
     }
     // conversions at v
-    const double r = v[0], rr = 1.0 / r, mk = a.mask[q];
+    const double r = v[0], rr = rcp_fast(r), mk = a.mask[q];
     double lr = lo[0] + lp * a.inv_m2;
     for (int d = 0; d < 3; ++d) {
         const double c = v[d + 1] * rr;

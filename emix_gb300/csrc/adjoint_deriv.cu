@@ -1,8 +1,8 @@
 // adjoint_deriv.cu -- D^T, the transpose of the compact first derivative
 // D = (1/h) A^{-1} B of every scheme: D^T = (1/h) B^T A^{-T}.
 //
-// One thread per pencil (lanes along x for the y and z pencils; along y for
-// the x pencils, whose lines stay in L1 across the walk).  Forward sweep of
+// One thread per pencil: lanes along x for the y and z pencils; for the x
+// pencils (contiguous rows) 32-row chunks staged through shared memory.  Forward sweep of
 // A^T into the scratch w, backward sweep with a 7-value register window of z
 // from which out_j = sum_k B^T[j][k] z_{j+k-3} is finished as soon as its last
 // z is known (4 operations on the interior rows, where B^T is the
@@ -93,6 +93,115 @@ __global__ void __launch_bounds__(128) k_deriv_t(DerivTTable T, PencilFields F, 
     }
 }
 
+// x pencils (contiguous rows): a warp owns 32 pencils and stages 32-row
+// chunks through a per-warp [32][kXLd] shared tile, loaded and stored with
+// coalesced row accesses; each lane then walks its own pencil through the tile
+// (as k_deriv_x does for D).  In the backward walk the output row j = i + 3 is
+// written into the tile slot of w row j, which the descending walk has already
+// consumed (slots up to 34 for the 3 rows past a 32-row chunk).
+template <int ACC>
+__global__ void __launch_bounds__(128) k_deriv_t_x(DerivTTable T, PencilFields F, long np) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *tile = smem + warp * kXTile;
+    const long p0 = ((long)blockIdx.x * (blockDim.x >> 5) + warp) * 32;
+    if (p0 >= np) return;   // whole warp
+    const int npw = (int)min((long)32, np - p0);
+    const int f = blockIdx.y;
+    const int n = T.n;
+    const double *in = pick(F.in, f) + p0 * n;
+    double *w = pick(F.w, f) + p0 * n;
+    double *out = pick(F.out, f) + p0 * n;
+    const DerivTRow *R = T.rows;
+    const double *BT = T.bt;
+    double *t = tile + lane * kXLd;
+    const bool mine = lane < npw;
+
+    // forward: y_i = in_i ib_i - m_i y_{i-1}, chunk by chunk into w
+    double y = 0.0;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        const int cl = min(32, n - c0);
+        for (int q = 0; q < npw; ++q)
+            if (lane < cl) tile[q * kXLd + lane] = in[(long)q * n + c0 + lane];
+        __syncwarp();
+        if (mine) {
+            for (int r = 0; r < cl; ++r) {
+                const DerivTRow rw = R[c0 + r];
+                y = fma(-rw.m, y, t[r] * rw.ib);
+                t[r] = y;
+            }
+        }
+        __syncwarp();
+        for (int q = 0; q < npw; ++q)
+            if (lane < cl) w[(long)q * n + c0 + lane] = tile[q * kXLd + lane];
+        __syncwarp();
+    }
+
+    // backward: z_i = w_i - g_i z_{i+1}; zq[t] = z_{i+t}; out_j, j = i + 3
+    double zq[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) zq[k] = 0.0;
+    double z = 0.0;
+    const bool fast = T.jlo <= T.jhi;
+    const int jtop = fast ? T.jhi : -1, jbot = fast ? T.jlo : 0;
+    for (int c0 = ((n - 1) / 32) * 32; c0 >= 0; c0 -= 32) {
+        const int cl = min(32, n - c0);
+        for (int q = 0; q < npw; ++q)
+            if (lane < cl) tile[q * kXLd + lane] = w[(long)q * n + c0 + lane];
+        __syncwarp();
+        if (mine) {
+            auto advance = [&](int i) {
+#pragma unroll
+                for (int k = 6; k > 0; --k) zq[k] = zq[k - 1];
+                if (i >= 0) {
+                    const double wi = t[i - c0];
+                    z = (i == n - 1) ? wi : fma(-R[i].g, z, wi);
+                    zq[0] = z;
+                } else {
+                    zq[0] = 0.0;
+                }
+            };
+            auto general = [&](int j) {
+                const double *b = BT + 7 * (long)j;
+                double o = b[0] * zq[0];
+#pragma unroll
+                for (int k = 1; k < 7; ++k) o = fma(b[k], zq[k], o);
+                t[j - c0] = o;
+            };
+            const int iend = c0 == 0 ? -3 : c0;   // the last chunk also finishes rows 0..2
+            int i = c0 + cl - 1;
+            // three branch-free runs of j = i + 3: closure rows at the top, the
+            // interior (4 operations), closure rows at the bottom
+            for (; i >= iend && i + 3 > jtop; --i) {
+                advance(i);
+                if (i + 3 < n) general(i + 3);
+            }
+            if (fast) {
+                for (; i >= iend && i + 3 >= jbot; --i) {
+                    advance(i);
+                    t[i + 3 - c0] = fma(T.ta, zq[2] - zq[4], T.tb * (zq[1] - zq[5]));
+                }
+            }
+            for (; i >= iend; --i) {
+                advance(i);
+                general(i + 3);
+            }
+        }
+        __syncwarp();
+        // out rows [c0 + 3, c0 + cl + 3) (from row 0 in the last chunk), below n
+        const int js = c0 == 0 ? 0 : c0 + 3, je = min(c0 + cl + 3, n);
+        for (int q = 0; q < npw; ++q) {
+            for (int j = js + lane; j < je; j += 32) {
+                double v = tile[q * kXLd + j - c0];
+                double *o = out + (long)q * n + j;
+                if (ACC) v += *o;
+                *o = v;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 } // namespace
 
 int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double *const *in,
@@ -110,8 +219,16 @@ int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double
     }
     const long np = axis == 0 ? (long)ny * nz : (axis == 1 ? (long)nx * nz : (long)nx * ny);
     dim3 grid((unsigned)((np + 127) / 128), nf);
-    if (acc) k_deriv_t<1><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
-    else k_deriv_t<0><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
+    if (axis == 0) {
+        // four warps of 32 pencils per block, one staging tile per warp
+        const size_t shm = 4 * kXTile * sizeof(double);
+        if (acc) k_deriv_t_x<1><<<grid, 128, shm, st>>>(T, F, np);
+        else k_deriv_t_x<0><<<grid, 128, shm, st>>>(T, F, np);
+    } else if (acc) {
+        k_deriv_t<1><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
+    } else {
+        k_deriv_t<0><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
+    }
     EMIX_CUDA_TRY(cudaGetLastError());
     return EMIX_OK;
 }

@@ -53,6 +53,36 @@ def test_deriv_transpose_dot_product(emix, oracle, scheme, axis):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("scheme", [F.SCHEME_A, F.SCHEME_B, F.SCHEME_C])
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_deriv_transpose_long_pencils(emix, oracle, scheme, axis):
+    """Pencils of 70 rows (x pencils cross two 32-row staging chunks and end
+    in a partial one; 35 pencils leave a partial warp): every pencil of D^T y
+    against the dense transpose of the oracle's operator, both forms."""
+    shape = [2, 5, 7, 6]               # (fields, nz, ny, nx)
+    shape[3 - axis] = 70
+    shape = tuple(shape)
+    y = F.uniform(95, axis, shape)
+    x = F.uniform(96, axis, shape)
+    n = 70
+    h = 1.0 / (n - 1)
+    cols = []
+    for k in range(n):
+        shp = [1, 1, 1]
+        shp[2 - axis] = n
+        f = np.zeros(shp)
+        f.reshape(-1)[k] = 1.0
+        cols.append(oracle.deriv3d(scheme, axis, f, h).reshape(-1))
+    Dm = np.stack(cols, axis=1)
+    ax = 3 - axis
+    want = np.moveaxis(np.tensordot(Dm.T, np.moveaxis(y, ax, 0), axes=1), 0, ax)
+    got = emix.deriv_t_dev(_dev(y), axis, h, scheme).cpu().numpy()
+    assert_close(got, want, tol=1e-12, what="D^T")
+    acc = _dev(x)
+    emix.deriv_t_dev(_dev(y), axis, h, scheme, out=acc)
+    assert_close(acc.cpu().numpy(), x + want, tol=1e-12, what="accumulate")
+
+
 def _tank_case(n=20, steps=2):
     w = F.stirred_tank(n=n, impeller=True, impeller_omega=1.3, height=2.0)
     # the free surface inside the box so the interface term is active
