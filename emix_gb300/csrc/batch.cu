@@ -2,12 +2,14 @@
 //
 // A batch owns one context per grid (each with its own arena, tables and
 // plan).  Position k of every plan is the same kernel kind, so a batched step
-// issues one launch per position: a persistent kernel whose CTAs walk a work
-// list of (grid, virtual block) items covering every grid's launch of that
-// position.  Small grids, which alone fill a fraction of the GPU and are
-// bound by launch overhead, then share the machine.  The step is captured in
-// a CUDA graph.  The work-list granularity (pencils per y/z block, cells per
-// pointwise item, resident CTAs per SM) is chosen by a timing autotuner.
+// issues one launch per position over a work list of (grid, virtual block)
+// items covering every grid's launch of that position: pointwise positions as
+// persistent kernels whose CTAs walk the list, pencil and level-set positions
+// with one CTA per item.  Small grids, which alone fill a fraction of the GPU
+// and are bound by launch overhead, then share the machine.  The step is
+// captured in a CUDA graph.  The work-list granularity (pencils per y/z block,
+// cells per pointwise item, resident CTAs per SM of the persistent kernels)
+// is chosen by a timing autotuner.
 #include "plan.cuh"
 #include "weno_march.cuh"
 
@@ -311,16 +313,13 @@ int ctas(const emix_batch *b, long total) {
     return (int)(c < 1 ? 1 : c);
 }
 
-// resident CTAs of the stage kernel (its register bound allows 4 per SM)
-int weno_ctas(const emix_batch *b, long total) {
-    static int per = 0;
-    if (per == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_weno, kNT, 0) != cudaSuccess) {
-        cudaGetLastError();
-        per = 4;
-    }
-    long c = (long)b->sms * (per > 0 ? per : 1);
-    if (c > total) c = total;
-    return (int)(c < 1 ? 1 : c);
+// one CTA per work item: the pencil walks and the stage's z marches are long
+// and latency-bound, so the hardware scheduler keeps as many of them resident
+// as registers and shared memory allow (a persistent grid of a few CTAs per SM
+// would cap the resident warps)
+int all_items(long total) {
+    const long c = total < 1 ? 1 : (total > 2147483647L ? 2147483647L : total);
+    return (int)c;
 }
 
 int issue(emix_batch *b) {
@@ -340,21 +339,21 @@ int issue(emix_batch *b) {
         case LK_BC: k_batch_cells<BcOp><<<nb, 256, 0, st>>>((const BcArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_CLOCK: k_batch_cells<ClockOp><<<nb, 256, 0, st>>>((const ImpClockArgs *)P.args, P.start, G, b->tune.cpb); break;
         case LK_WENO:
-            k_batch_weno<<<weno_ctas(b, P.total), kNT, 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
+            k_batch_weno<<<all_items(P.total), kNT, 0, st>>>((const WenoArgs *)P.args, P.start, P.shape, G);
             break;
         case LK_DERIV_X: {
             const size_t shm = 4 * kXTile * sizeof(double);
             if (P.epi == EPI_STORE)
-                k_batch_deriv_x<EPI_STORE><<<nb, 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+                k_batch_deriv_x<EPI_STORE><<<all_items(P.total), 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
             else
-                k_batch_deriv_x<EPI_ACCUM><<<nb, 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+                k_batch_deriv_x<EPI_ACCUM><<<all_items(P.total), 128, shm, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
             break;
         }
         case LK_DERIV_YZ:
             if (P.epi == EPI_STORE)
-                k_batch_deriv_yz<EPI_STORE><<<nb, b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+                k_batch_deriv_yz<EPI_STORE><<<all_items(P.total), b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
             else
-                k_batch_deriv_yz<EPI_ACCUM><<<nb, b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
+                k_batch_deriv_yz<EPI_ACCUM><<<all_items(P.total), b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
             break;
         default:
             return EMIX_ERR_ARG;
