@@ -98,6 +98,26 @@ EMIX_DEV double sqrt_fast(double x) {
     return fma(s, ee * fma(0.375, ee, 0.5), s);
 }
 
+// 1/sqrt(x): the seed of sqrt_fast, then one third-order step
+// y (1 + e/2 + 3e^2/8) with e = 1 - x y^2 (the same binomial series).  Five
+// FP64 operations; zero, negative, subnormal, huge, inf and NaN arguments go
+// to 1 / sqrt().
+EMIX_DEV double rsqrt_fast(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ebits = (int)(b >> 52) & 0x7ff;
+    if (ebits < 2 || ebits > 2045 || (b >> 63)) return 1.0 / sqrt(x);
+    const int e = ebits - 1023;
+    const int odd = e & 1;
+    const float f = __uint_as_float(((127u + (unsigned)odd) << 23) | (unsigned int)((b >> 29) & 0x7fffff));
+    const unsigned int rb = __float_as_uint(rsqrtf(f));
+    const int half = (e - odd) / 2;
+    const int fexp = (int)(rb >> 23) & 0xff;
+    const double y = __longlong_as_double(
+        (long long)(((unsigned long long)(fexp - 127 + 1023 - half) << 52) | ((unsigned long long)(rb & 0x7fffff) << 29)));
+    const double ee = fma(-x * y, y, 1.0);
+    return fma(y, ee * fma(0.375, ee, 0.5), y);
+}
+
 struct DerivRow {
     double A, B, m, g;
 };

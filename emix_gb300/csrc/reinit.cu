@@ -8,10 +8,12 @@
 //   |grad phi| by the Godunov upwinding of the left- and right-biased WENO5
 //   derivatives (PhiDevPlus/MinusParameterJB, lsTools.cu:587-770).
 //
-// One fused kernel per stage: both WENO5 reconstructions of each direction,
-// the Godunov combination, the speed and the stage update; stages ping-pong
-// between two scratch fields so that stencil reads never meet a write.
-#include "weno.cuh"
+// One fused kernel per stage: both WENO5 reconstructions of each direction
+// (away from the padded grid's edges from six shared differences and their
+// second differences, weno5a), the Godunov combination, the speed and the
+// stage update; stages ping-pong between two scratch fields so that stencil
+// reads never meet a write.
+#include "weno_march.cuh"
 
 namespace emix {
 
@@ -44,26 +46,41 @@ __global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
         const double p0 = a.phi0[id];
         const double ta = (double)(p0 > 0.0) - (double)(p0 < 0.0);
         double r = 0.0;
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
             const double C = sc[d] * a.jbn[4 * d * ng + id];
-            const double eps = kWenoEps4 / (C * C);
+            const double eps = kWenoEps4 * rcp_fast(C * C);
             const long base = id - c3[d] * s3[d];
-            int p[5];
-            // left-biased (phi^-)
-            stencil_left(c3[d], L3[d], p);
-            double v5 = bd(a.src, base, s3[d], p[4]);
-            if (d == 2 && a.ref_bugs && c3[2] == nzg - 1) {
-                // lsTools.cu:636: id_kp2 = id_jm1 at the top layer
-                const long ib = c3[1] == 0 ? id : id - nxg;
-                v5 = a.src[ib] - a.src[ib - sxy];
+            const int c = c3[d];
+            double am, bp;
+            if (c >= 2 && c <= L3[d] - 4) {
+                // both reconstructions from the six differences D(c-2..c+3)
+                // and their five second differences (weno5a)
+                double v[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) v[k] = bd(a.src, base, s3[d], c - 2 + k);
+                const double A0 = v[1] - v[0], A1 = v[2] - v[1], A2 = v[3] - v[2], A3 = v[4] - v[3],
+                             A4 = v[5] - v[4];
+                am = C * weno5a(v[2], A0, A1, A2, A3, eps, 12.0);    // phi^-: D(c), A(c-1..c+2)
+                bp = C * weno5a(v[3], A4, A3, A2, A1, eps, -12.0);   // phi^+: D(c+1), -A(c+3..c)
+            } else {
+                int p[5];
+                // left-biased (phi^-)
+                stencil_left(c, L3[d], p);
+                double v5 = bd(a.src, base, s3[d], p[4]);
+                if (d == 2 && a.ref_bugs && c == nzg - 1) {
+                    // lsTools.cu:636: id_kp2 = id_jm1 at the top layer
+                    const long ib = c3[1] == 0 ? id : id - nxg;
+                    v5 = a.src[ib] - a.src[ib - sxy];
+                }
+                am = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
+                               bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]), v5, eps);
+                // right-biased (phi^+)
+                stencil_right(c, L3[d], p);
+                bp = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
+                               bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]),
+                               bd(a.src, base, s3[d], p[4]), eps);
             }
-            const double am = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
-                                        bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]), v5, eps);
-            // right-biased (phi^+)
-            stencil_right(c3[d], L3[d], p);
-            const double bp = C * weno5(bd(a.src, base, s3[d], p[0]), bd(a.src, base, s3[d], p[1]),
-                                        bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]),
-                                        bd(a.src, base, s3[d], p[4]), eps);
             double pmax = fmax(am, 0.0) * fmax(am, 0.0), pmin = fmin(bp, 0.0) * fmin(bp, 0.0);
             double rd = 0.5 * (ta + 1.0) * fmax(pmax, pmin);
             pmax = fmax(bp, 0.0) * fmax(bp, 0.0);
@@ -72,12 +89,12 @@ __global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
             r += rd;
         }
         const double dm = a.dmins[id];
-        const double rs = (p0 / sqrt(p0 * p0 + dm * dm)) * (sqrt(r) - 1.0);
+        const double rs = (p0 * rsqrt_fast(fma(p0, p0, dm * dm))) * (sqrt_fast(r) - 1.0);
         const double t = a.src[id] - a.dt * rs;
         double o;
         if (a.stage == 1) o = t;
         else if (a.stage == 2) o = 0.75 * a.phi[id] + 0.25 * t;
-        else o = (a.phi[id] + 2.0 * t) / 3.0;
+        else o = fma(2.0, t, a.phi[id]) * (1.0 / 3.0);
         a.out[id] = o;
     }
 }
