@@ -83,14 +83,15 @@ __global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__
         if (k > 0 && k < nz - 1) { dzm = Z[q] - Z[q - sz]; dzp = Z[q + sz] - Z[q]; }
         else if (k == 0) { dzp = Z[q + sz] - Z[q]; dzm = dzp; }
         else { dzm = Z[q] - Z[q - sz]; dzp = dzm; }
-        const double d = pow(fmax(dxm, dxp) * fmax(dym, dyp) * fmax(dzm, dzp), 1.0 / 3.0);
+        // the reference's **(1/3) (sgdm_incomp.f90:89,97-108) as cube roots
+        const double d = cbrt(fmax(dxm, dxp) * fmax(dym, dyp) * fmax(dzm, dzp));
         dxyz[q] = d;
-        ratios[q] = pow(d / dxp, 1.0 / 3.0);
-        ratios[n + q] = pow(d / dxm, 1.0 / 3.0);
-        ratios[2 * n + q] = pow(d / dyp, 1.0 / 3.0);
-        ratios[3 * n + q] = pow(d / dym, 1.0 / 3.0);
-        ratios[4 * n + q] = pow(d / dzp, 1.0 / 3.0);
-        ratios[5 * n + q] = pow(d / dzm, 1.0 / 3.0);
+        ratios[q] = cbrt(d / dxp);
+        ratios[n + q] = cbrt(d / dxm);
+        ratios[2 * n + q] = cbrt(d / dyp);
+        ratios[3 * n + q] = cbrt(d / dym);
+        ratios[4 * n + q] = cbrt(d / dzp);
+        ratios[5 * n + q] = cbrt(d / dzm);
     }
 }
 
