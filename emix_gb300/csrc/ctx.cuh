@@ -45,6 +45,10 @@ struct emix_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
     bool overlap = false;
+    // the level-set stages' plane tiles by TMA (emix_ctx_set_tma; on by
+    // default where the copy unit's alignment rules hold), one map per stage
+    bool tma = true;
+    CUtensorMap weno_tmap[3];
 };
 
 namespace emix {

@@ -50,6 +50,7 @@ struct Launch {
         ImpClockArgs clock;
         ImpInterpArgs interp;
     };
+    const CUtensorMap *tmap;   // LK_WENO: plane tiles by TMA (null: register-staged loads)
 };
 
 int launch_single(const Launch &L, cudaStream_t st);

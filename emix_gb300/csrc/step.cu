@@ -45,7 +45,7 @@ int launch_single(const Launch &L, cudaStream_t st) {
         k_ghost_pad<<<cells_grid(L.pad.ng), 256, 0, st>>>(L.pad);
         break;
     case LK_WENO:
-        return launch_weno_stage(L.weno, st);
+        return launch_weno_stage(L.weno, st, L.tmap);
     case LK_DERIV_X:
     case LK_DERIV_YZ:
         return launch_deriv(L.deriv.T, L.deriv.axis, L.deriv.epi, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
@@ -196,6 +196,7 @@ void build_plan(emix_ctx *c) {
                 if (s == 2) { a.r0[d] = g - 3; a.rn[d] = dims[d] + 6; }
                 if (s == 3) { a.r0[d] = g; a.rn[d] = dims[d]; }
             }
+            if (c->tma && weno_tma_map(&c->weno_tmap[s - 1], a)) L.tmap = &c->weno_tmap[s - 1];
             P.push_back(L);
         }
         // velocity gradients (cudaDeriv; dT/dx_i feeds nothing on this path:
@@ -512,6 +513,20 @@ int emix_ctx_destroy(emix_ctx *c) {
     cudaFree(c->arena);
     delete c;
     return EMIX_OK;
+}
+
+int emix_ctx_set_tma(emix_ctx *c, int on) {
+    if (!c || (on != 0 && on != 1)) return EMIX_ERR_ARG;
+    c->tma = on == 1;
+    ctx_rebuild_plan(c);
+    return EMIX_OK;
+}
+
+int emix_ctx_tma_stages(emix_ctx *c) {
+    if (!c) return -1;
+    int k = 0;
+    for (const Launch &L : c->plan) k += (L.kind == LK_WENO && L.tmap) ? 1 : 0;
+    return k;
 }
 
 int emix_ctx_set_overlap(emix_ctx *c, int on) {

@@ -32,14 +32,14 @@ __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict
     }
 }
 
-int launch_weno_stage(const WenoArgs &a_in, cudaStream_t st) {
+int launch_weno_stage(const WenoArgs &a_in, cudaStream_t st, const CUtensorMap *tmap) {
     WenoArgs a = a_in;
     const int dims[3] = {a.nxg, a.nyg, a.nzg};
     for (int d = 0; d < 3; ++d) {
         if (a.rn[d] <= 0) { a.r0[d] = 0; a.rn[d] = dims[d]; }   // default: whole padded grid
         if (a.r0[d] < 0 || a.r0[d] + a.rn[d] > dims[d]) return EMIX_ERR_ARG;
     }
-    return launch_weno_march(a, st);
+    return launch_weno_march(a, st, tmap);
 }
 
 namespace {

@@ -18,6 +18,8 @@
 
 #include "common.cuh"
 
+#include <cuda.h>   // CUtensorMap (the driver entry point is fetched at run time)
+
 namespace emix {
 
 struct WenoArgs {
@@ -56,10 +58,15 @@ __global__ void k_ghost_pad(PadArgs a);
 __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict__ ghost, int g,
                               int nx, int ny, int nz);
 
-// one stage on one grid (region rn[d] <= 0: the whole padded axis)
-int launch_weno_stage(const WenoArgs &a, cudaStream_t st);
+// one stage on one grid (region rn[d] <= 0: the whole padded axis); with a
+// tensor map of a.phi (weno_tma_map) the plane tiles come by TMA copies
+int launch_weno_stage(const WenoArgs &a, cudaStream_t st, const CUtensorMap *tmap = nullptr);
 // the z-marching stage kernel (weno_march.cu); a's region normalised
-int launch_weno_march(const WenoArgs &a, cudaStream_t st);
+int launch_weno_march(const WenoArgs &a, cudaStream_t st, const CUtensorMap *tmap = nullptr);
+// the tiled-copy description of a.phi's plane tiles; false (and no map) when
+// the copy unit's rules do not hold: a.phi 16-byte aligned, an even padded x
+// extent (row pitch a multiple of 16 bytes), extents at least the tile's
+bool weno_tma_map(CUtensorMap *m, const WenoArgs &a);
 
 // the pairs (C_d, E_d) = (jbn_d / h_d, kWenoEps4 / C_d^2) of the precomputed-scale path
 __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict__ wce, double sx,

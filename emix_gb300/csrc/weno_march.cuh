@@ -91,9 +91,52 @@ EMIX_DEV void load_plane(const double *__restrict__ phi, int x0, int y0, int Z, 
     }
 }
 
+// TMA staging of the phi plane tiles (k_weno_march_tma): a 3-D tiled copy of
+// a kTY x kTW box per plane into one of two shared buffers, completion on an
+// mbarrier; the box starts at an even x (16-byte rule of the copy unit), so the
+// tile sits kdx = 0 or 1 columns into the buffer.
+constexpr int kTW = kPX + 2;                        // 24 doubles: 192 bytes per row
+constexpr int kTY = kPY;                            // 22 rows
+constexpr unsigned kTileBytes = kTW * kTY * 8;      // 4224
+constexpr long kTmaWaitLimit = 1L << 22;            // polls (with 64 ns pauses) before giving up
+
+EMIX_DEV unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// bounded wait for phase `parity` of the mbarrier at shared address bar:
+// non-blocking tests with 64 ns pauses, about 0.3 s in all before giving up
+EMIX_DEV bool mbar_wait(unsigned bar, unsigned parity) {
+    for (long it = 0; it < kTmaWaitLimit; ++it) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+// one thread: expect the tile's bytes on bar, then copy the box at (x, y, z)
+EMIX_DEV void tma_plane(const void *tmap, unsigned dst, unsigned bar, int x, int y, int z) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(kTileBytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];"
+                 :: "r"(dst), "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(z), "r"(bar)
+                 : "memory");
+}
+
+// count of stage blocks that gave up waiting for a plane copy (read by
+// emix_weno_tma_timeouts; the TMA kernel and that reader are in weno_march.cu)
+static __device__ int g_weno_tma_timeouts = 0;
+
 // One (virtual) block: column tile (bx, by) of the region, z chunk bz of gz.
-EMIX_DEV void weno_march_body(const WenoArgs &a, int bx, int by, int bz, int gz) {
-    __shared__ double P[kPY][kPX];
+// TMA: the plane tiles come by tiled bulk copies described by *tmap (a
+// __grid_constant__ kernel parameter); otherwise by register-staged loads.
+template <bool TMA>
+EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int gz, const void *tmap) {
+    __shared__ __align__(128) double Pbuf[2 * kTY * kTW];   // register path: [kPY][kPX]; TMA: [2][kTY][kTW]
     __shared__ double Dx[kMY][kMX + 5];      // positions x0-2 .. x0+kMX+2
     __shared__ double Ax[kMY][kMX + 4];      // positions x0-1 .. x0+kMX+2
     __shared__ double Dy[kMY + 5][kMX];      // rows y0-2 .. y0+kMY+2
@@ -136,30 +179,83 @@ EMIX_DEV void weno_march_body(const WenoArgs &a, int bx, int by, int bz, int gz)
         fz = f[6];
     }
 
+    // plane tiles: register path one [kPY][kPX] tile, loaded into registers
+    // during the previous plane; TMA path two [kTY][kTW] buffers, plane Z in
+    // buffer (Z - zs) & 1, the copy of plane Z + 2 issued once plane Z is read
+    const int xs = (x0 - 3) & ~1, kdx = (x0 - 3) - xs;   // box origin (even x), tile offset
+    __shared__ __align__(8) unsigned long long mbar[2];
+    __shared__ int s_ok;
     Plane pl;
-    if (zs < ze) load_plane(phi, x0, y0, zs, nxg, nyg, nzg, sxy, tid, pl);
-    for (int Z = zs; Z < ze; ++Z) {
-        // ---- this plane's tile (loaded during the previous plane) ----
-#pragma unroll
-        for (int r = 0; r < kPR; ++r) {
-            const int t = tid + r * kNT;
-            if (t < kPN) P[t / kPX][t % kPX] = pl.v[r];
+    if constexpr (TMA) {
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&mbar[0])), "r"(1) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&mbar[1])), "r"(1) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         __syncthreads();
-        // the next plane's tile and z value, in flight during this plane
-        if (Z + 1 < ze) load_plane(phi, x0, y0, Z + 1, nxg, nyg, nzg, sxy, tid, pl);
+        if (tid == 0) {
+            if (zs < ze) tma_plane(tmap, smem_u32(Pbuf), smem_u32(&mbar[0]), xs, y0 - 3, zs);
+            if (zs + 1 < ze) tma_plane(tmap, smem_u32(Pbuf + kTY * kTW), smem_u32(&mbar[1]), xs, y0 - 3, zs + 1);
+        }
+    } else {
+        if (zs < ze) load_plane(phi, x0, y0, zs, nxg, nyg, nzg, sxy, tid, pl);
+    }
+    for (int Z = zs; Z < ze; ++Z) {
+        const int kk = Z - zs, b = kk & 1;
+        const double *Pz;
+        int pld, pcx;
+        if constexpr (TMA) {
+            if (tid == 0) s_ok = mbar_wait(smem_u32(&mbar[b]), (unsigned)((kk >> 1) & 1));
+            __syncthreads();
+            if (!s_ok) {
+                // the copy did not arrive: count it, let the copies in flight
+                // land (bounded), and leave this block's planes unwritten
+                if (tid == 0) {
+                    atomicAdd(&g_weno_tma_timeouts, 1);
+                    mbar_wait(smem_u32(&mbar[b]), (unsigned)((kk >> 1) & 1));
+                    if (Z + 1 < ze) mbar_wait(smem_u32(&mbar[b ^ 1]), (unsigned)(((kk + 1) >> 1) & 1));
+                }
+                return;
+            }
+            Pz = Pbuf + b * kTY * kTW;
+            pld = kTW;
+            pcx = kdx;
+        } else {
+            // ---- this plane's tile (loaded during the previous plane) ----
+#pragma unroll
+            for (int r = 0; r < kPR; ++r) {
+                const int t = tid + r * kNT;
+                if (t < kPN) Pbuf[t] = pl.v[r];
+            }
+            __syncthreads();
+            // the next plane's tile, in flight during this plane
+            if (Z + 1 < ze) load_plane(phi, x0, y0, Z + 1, nxg, nyg, nzg, sxy, tid, pl);
+            Pz = Pbuf;
+            pld = kPX;
+            pcx = 0;
+        }
+        auto P = [&](int py, int px) { return Pz[py * pld + px + pcx]; };
         const double fnext = ld(Z + 4);
         for (int t = tid; t < kMY * (kMX + 5); t += kNT) {
             const int i = t % (kMX + 5), j = t / (kMX + 5);
             const int gx = x0 - 2 + i;   // P column i + 1
-            Dx[j][i] = gx == 0 ? P[j + 3][i + 2] - P[j + 3][i + 1] : P[j + 3][i + 1] - P[j + 3][i];
+            Dx[j][i] = gx == 0 ? P(j + 3, i + 2) - P(j + 3, i + 1) : P(j + 3, i + 1) - P(j + 3, i);
         }
         for (int t = tid; t < (kMY + 5) * kMX; t += kNT) {
             const int i = t % kMX, j = t / kMX;
             const int gy = y0 - 2 + j;   // P row j + 1
-            Dy[j][i] = gy == 0 ? P[j + 2][i + 3] - P[j + 1][i + 3] : P[j + 1][i + 3] - P[j][i + 3];
+            Dy[j][i] = gy == 0 ? P(j + 2, i + 3) - P(j + 1, i + 3) : P(j + 1, i + 3) - P(j, i + 3);
         }
+        const double pin = active ? P(ty + 3, tx + 3) : 0.0;
         __syncthreads();
+        if constexpr (TMA) {
+            // buffer b is read: the copy of plane Z + 2 may overwrite it
+            if (tid == 0 && Z + 2 < ze) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tma_plane(tmap, smem_u32(Pbuf + b * kTY * kTW), smem_u32(&mbar[b]), xs, y0 - 3, Z + 2);
+            }
+        }
         for (int t = tid; t < kMY * (kMX + 4); t += kNT) {
             const int i = t % (kMX + 4), j = t / (kMX + 4);
             Ax[j][i] = Dx[j][i + 1] - Dx[j][i];
@@ -238,7 +334,6 @@ EMIX_DEV void weno_march_body(const WenoArgs &a, int bx, int by, int bz, int gz)
                 rs = fma(u, mx * W, rs);
             }
             // TVD-RK3 stage (extrapol.cu:155-212)
-            const double pin = P[ty + 3][tx + 3];
             double v;
             if (a.stage == 1) {
                 v = fma(-a.dt, rs, pin);
@@ -265,6 +360,17 @@ EMIX_DEV void weno_march_body(const WenoArgs &a, int bx, int by, int bz, int gz)
         Az[4] = Dz[5] - Dz[4];
         __syncthreads();
     }
+    if constexpr (TMA) {
+        if (tid == 0) {
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(smem_u32(&mbar[0])) : "memory");
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(smem_u32(&mbar[1])) : "memory");
+        }
+    }
+}
+
+// the register-staged form (the batched ensemble walks it over many grids)
+EMIX_DEV void weno_march_body(const WenoArgs &a, int bx, int by, int bz, int gz) {
+    weno_march_body_t<false>(a, bx, by, bz, gz, nullptr);
 }
 
 

@@ -370,6 +370,13 @@ def ghost_unpad_dev(ghost, g):
     return out
 
 
+def weno_tma_timeouts() -> int:
+    """Level-set stage blocks that gave up waiting for a TMA plane copy (0 in a correct run)."""
+    out = C.c_int()
+    check(_lib.load().emix_weno_tma_timeouts(C.byref(out)), "emix_weno_tma_timeouts")
+    return out.value
+
+
 def fp64_peak() -> float:
     """Measured FP64 FMA lane-operations per second of the current device."""
     v = C.c_double()
@@ -437,6 +444,14 @@ class Context:
 
     def set_overlap(self, on: bool):
         check(self.lib.emix_ctx_set_overlap(self._h, 1 if on else 0), "emix_ctx_set_overlap")
+
+    def set_tma(self, on: bool):
+        """Plane tiles of the level-set stages by TMA copies (default) or by
+        register-staged loads; the results are bitwise the same."""
+        check(self.lib.emix_ctx_set_tma(self._h, 1 if on else 0), "emix_ctx_set_tma")
+
+    def tma_stages(self) -> int:
+        return int(self.lib.emix_ctx_tma_stages(self._h))
 
     @property
     def time(self) -> float:

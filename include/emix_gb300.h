@@ -351,6 +351,19 @@ int emix_ctx_set_stream(emix_ctx *ctx, void *stream);
  * GB300 both sides are FP64-bound and the overlap gains nothing measurable. */
 int emix_ctx_set_overlap(emix_ctx *ctx, int on);
 
+/* 1 (default): the level-set stages bring their phi plane tiles into shared
+ * memory with TMA tiled copies (one 3-D tensor map per stage) wherever the
+ * copy unit's rules hold (padded x extent even, at least 24 x 22 cells);
+ * 0: register-staged loads.  Results are bitwise the same either way.
+ * emix_ctx_tma_stages gives how many of the step's stages use the copies. */
+int emix_ctx_set_tma(emix_ctx *ctx, int on);
+int emix_ctx_tma_stages(emix_ctx *ctx);
+
+/* Stage blocks (since the library was loaded, on the current device) that
+ * gave up waiting for a plane copy after about 0.3 s and left their cells
+ * unwritten; 0 in every correct run. */
+int emix_weno_tma_timeouts(int *count);
+
 /* Static inputs from host memory: jbn[11], mask, grid coordinates xyz[3]
  * (used to build the SGS filter width, as INISGDM). */
 int emix_ctx_set_static(emix_ctx *ctx, const double *jbn, const double *mask,

@@ -306,3 +306,28 @@ def test_taylor_green_64_ten_steps(emix, oracle):
     for m in range(5):
         assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
     assert_close(phi, rphi, tol=1e-11, what="phi")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nz", [(24, 24), (30, 21), (23, 26)])
+def test_tma_plane_tiles_give_the_same_bits(emix, n, nz):
+    """The level-set stages with their phi plane tiles brought by TMA tiled
+    copies and with register-staged loads give identical results; odd padded
+    x extents (n = 23: 33 cells) fall back to the loads by themselves."""
+    w = F.stirred_tank(n=n, nz=nz, impeller=True)
+    a = emix.Context(w, bc_walls=1)
+    b = emix.Context(w, bc_walls=1)
+    b.set_tma(False)
+    assert b.tma_stages() == 0
+    assert a.tma_stages() == (3 if (n + 10) % 2 == 0 else 0)
+    for use_graph in (False, True):
+        a.upload(w.um, w.phi); a.time = 0.0
+        b.upload(w.um, w.phi); b.time = 0.0
+        a.step(3, use_graph=use_graph)
+        b.step(3, use_graph=use_graph)
+        ua, pa = a.download()
+        ub, pb = b.download()
+        assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+    a.close()
+    b.close()
+    assert emix.weno_tma_timeouts() == 0
