@@ -307,12 +307,6 @@ int build(emix_batch *b) {
     return EMIX_OK;
 }
 
-int ctas(const emix_batch *b, long total) {
-    long c = (long)b->sms * b->tune.ctas_sm;
-    if (c > total) c = total;
-    return (int)(c < 1 ? 1 : c);
-}
-
 // one CTA per work item: the pencil walks and the stage's z marches are long
 // and latency-bound, so the hardware scheduler keeps as many of them resident
 // as registers and shared memory allow (a persistent grid of a few CTAs per SM
@@ -320,6 +314,15 @@ int ctas(const emix_batch *b, long total) {
 int all_items(long total) {
     const long c = total < 1 ? 1 : (total > 2147483647L ? 2147483647L : total);
     return (int)c;
+}
+
+// CTAs of a pointwise position: a persistent grid of ctas_sm per SM, or (0)
+// one CTA per item
+int ctas(const emix_batch *b, long total) {
+    if (b->tune.ctas_sm == 0) return all_items(total);
+    long c = (long)b->sms * b->tune.ctas_sm;
+    if (c > total) c = total;
+    return (int)(c < 1 ? 1 : c);
 }
 
 int issue(emix_batch *b) {
@@ -491,7 +494,7 @@ int emix_batch_step_per_grid(emix_batch *b, int nsteps, int use_graph) {
 }
 
 int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int ctas_per_sm) {
-    if (!b || cells_per_thread < 1 || cells_per_thread > 64 || ctas_per_sm < 1 || ctas_per_sm > 64 ||
+    if (!b || cells_per_thread < 1 || cells_per_thread > 64 || ctas_per_sm < 0 || ctas_per_sm > 64 ||
         (yz_block != 32 && yz_block != 64 && yz_block != 128))
         return EMIX_ERR_ARG;
     b->tune = BatchTune{cells_per_thread, yz_block, ctas_per_sm};
@@ -515,7 +518,7 @@ int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms) {
     if (!b || nsteps < 1) return EMIX_ERR_ARG;
     const int cpbs[] = {1, 4};
     const int bss[] = {32, 64, 128};
-    const int ctass[] = {2, 4, 8};
+    const int ctass[] = {0, 2, 4, 8};
     BatchTune best = b->tune;
     float best_t = 1e30f;
     cudaEvent_t e0, e1;

@@ -439,7 +439,8 @@ int emix_batch_step_per_grid(emix_batch *b, int nsteps, int use_graph);
 
 /* Work-list granularity of the batched launches: cells per thread of the
  * pointwise items (x256 per item), threads per y/z pencil block (32, 64 or
- * 128) and resident CTAs per SM of the persistent grids. */
+ * 128) and resident CTAs per SM of the persistent pointwise grids (0: one
+ * CTA per pointwise item instead of a persistent grid). */
 int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int ctas_per_sm);
 int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, int *ctas_per_sm);
 

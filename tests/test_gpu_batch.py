@@ -24,7 +24,7 @@ def test_batched_equals_per_grid(emix, sgs):
     b = emix.Batch(ws)
     b.step_per_grid(2)
     ref = [b.download(g) for g in range(len(ws))]
-    for tuning in [(1, 32, 2), (4, 64, 4), (4, 128, 8)]:
+    for tuning in [(1, 32, 2), (4, 64, 4), (4, 128, 8), (2, 32, 0)]:
         b.upload()
         b.set_tuning(*tuning)
         b.step(2, use_graph=(tuning[0] == 4))
