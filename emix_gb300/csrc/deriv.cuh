@@ -281,6 +281,9 @@ EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npen
             // branch-free runs of rows
             if (!T.periodic) {
                 const int rint = min(cl, n - T.nhi - c0);   // rows before the closures
+                // unrolled: the walk through the tile reads shared memory only,
+                // and later rows' stencils overlap the recurrence
+#pragma unroll 4
                 for (; r < rint; ++r) irow(r, t[r + 2], false);
                 for (; r < cl; ++r) {
                     const int i = c0 + r;
@@ -320,6 +323,7 @@ EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npen
         __syncwarp();
         if (mine) {
             if (!T.periodic) {
+#pragma unroll 4
                 for (int r = cl - 1; r >= 0; --r) {
                     const double y = t[r] - rows[c0 + r].g * yn;
                     yn = y;
