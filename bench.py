@@ -497,6 +497,26 @@ def main():
                  "unit": "G FP64 lane-ops/s", "frac": round(fp64_ach / fp64_peak, 4),
                  "peak_source": "measured live (emix_fp64_peak: FMA chains)"},
     }
+    # the whole step against the FP64 issue limit and against HBM at the
+    # algorithmic floor of 2064 B per cell-step (every field of every
+    # substep's kernel contracts read or written once, Smagorinsky)
+    ops_step = 0.0
+    for k, v in kernels.items():
+        cnt = 3 * n if k == "rk_post" else cells_per_launch(k, (N_GRID,) * 3, G) * v["launches_per_step"]
+        ops_step += FP64_OPS_PER_CELL.get(k, 0.0) * cnt
+    sec_step = ms / args.steps * 1e-3
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    issue = 2.0 * sms * (clocks.get("sm_max_mhz") or 2070.0) * 1e6
+    floor_b = 2064.0
+    step_roofline = {
+        "fp64_ops_per_cell_step": round(ops_step / n, 1),
+        "fp64_achieved_gops": round(ops_step / sec_step / 1e9, 1),
+        "fp64_issue_limit_gops": round(issue / 1e9, 1),
+        "fp64_frac_of_issue_limit": round(ops_step / sec_step / issue, 4),
+        "hbm_floor_bytes_per_cell_step": floor_b,
+        "hbm_achieved_gbs": round(floor_b * n / sec_step / 1e9, 1),
+        "hbm_frac": round(floor_b * n / sec_step / 1e9 / hbm_peak, 4),
+    }
     ctx.close()
 
     line = {
@@ -511,6 +531,7 @@ def main():
                 "api": "emix_step_host (pinned host buffers, H2D um+phi, one step, D2H um+phi)"},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline,
+        "step_roofline": step_roofline,
         "kernels": kernels,
         "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
     }
