@@ -105,3 +105,10 @@ extern "C" int emix_weno_tma_timeouts(int *count) {
     EMIX_CUDA_TRY(cudaMemcpyFromSymbol(count, emix::g_weno_tma_timeouts, sizeof(int)));
     return EMIX_OK;
 }
+
+extern "C" int emix_weno_tma_test_drop(int on) {
+    if (on != 0 && on != 1) return EMIX_ERR_ARG;
+    EMIX_CUDA_TRY(cudaMemcpyToSymbol(emix::g_weno_tma_drop, &on, sizeof(int)));
+    EMIX_CUDA_TRY(cudaDeviceSynchronize());
+    return EMIX_OK;
+}

@@ -130,6 +130,9 @@ EMIX_DEV void tma_plane(const void *tmap, unsigned dst, unsigned bar, int x, int
 // count of stage blocks that gave up waiting for a plane copy (read by
 // emix_weno_tma_timeouts; the TMA kernel and that reader are in weno_march.cu)
 static __device__ int g_weno_tma_timeouts = 0;
+// test hook (emix_weno_tma_test_drop): nonzero makes the TMA stage issue no
+// copies, so that its bounded waits run out and the timeout path is exercised
+static __device__ int g_weno_tma_drop = 0;
 
 // One (virtual) block: column tile (bx, by) of the region, z chunk bz of gz.
 // TMA: the plane tiles come by tiled bulk copies described by *tmap (a
@@ -194,7 +197,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !g_weno_tma_drop) {
             if (zs < ze) tma_plane(tmap, smem_u32(Pbuf), smem_u32(&mbar[0]), xs, y0 - 3, zs);
             if (zs + 1 < ze) tma_plane(tmap, smem_u32(Pbuf + kTY * kTW), smem_u32(&mbar[1]), xs, y0 - 3, zs + 1);
         }
@@ -251,7 +254,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
         __syncthreads();
         if constexpr (TMA) {
             // buffer b is read: the copy of plane Z + 2 may overwrite it
-            if (tid == 0 && Z + 2 < ze) {
+            if (tid == 0 && Z + 2 < ze && !g_weno_tma_drop) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 tma_plane(tmap, smem_u32(Pbuf + b * kTY * kTW), smem_u32(&mbar[b]), xs, y0 - 3, Z + 2);
             }

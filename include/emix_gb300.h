@@ -364,6 +364,13 @@ int emix_ctx_tma_stages(emix_ctx *ctx);
  * unwritten; 0 in every correct run. */
 int emix_weno_tma_timeouts(int *count);
 
+/* Test hook for the bounded waits: 1 makes the TMA level-set stages issue no
+ * plane copies (current device), so every stage block gives up after its
+ * waits (about a second), counts itself and leaves its cells unwritten; the
+ * context stays usable.  0 restores normal operation.  Never set in a
+ * production run. */
+int emix_weno_tma_test_drop(int on);
+
 /* Static inputs from host memory: jbn[11], mask, grid coordinates xyz[3]
  * (used to build the SGS filter width, as INISGDM). */
 int emix_ctx_set_static(emix_ctx *ctx, const double *jbn, const double *mask,
