@@ -332,3 +332,30 @@ def test_tma_plane_tiles_give_the_same_bits(emix, n, nz):
     a.close()
     b.close()
     assert emix.weno_tma_timeouts() == timeouts
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", SCHEMES)
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_longest_pencils(emix, oracle, scheme, axis):
+    """Pencils of the longest supported length (4096 rows; the x pencils walk
+    128 staging chunks) against the oracle, D^T against D by the dot-product
+    identity, and one row more rejected with EMIX_ERR_ARG."""
+    shape = [6, 7, 6]                  # the other axes at the minimum of 6 cells
+    shape[axis] = 4096
+    nx, ny, nz = shape
+    w = F.random_box(nx, ny, nz, seed=12, periodic=(scheme == F.SCHEME_BPER))
+    f = np.ascontiguousarray(w.um[1:3])
+    h = w.grid.h(axis)
+    got = host(emix.deriv_dev(dev(f), axis, h, scheme))
+    for c in range(2):
+        ref = oracle.deriv3d(scheme, axis, f[c], h)
+        assert_close(got[c], ref, what=f"scheme {scheme} axis {axis} comp {c}")
+    y = np.ascontiguousarray(w.um[3:5])
+    dty = host(emix.deriv_t_dev(dev(y), axis, h, scheme))
+    lhs, rhs = float((got * y).sum()), float((f * dty).sum())
+    assert abs(lhs - rhs) <= 1e-12 * (np.abs(got).sum() * np.abs(y).max())
+    shape[axis] = 4097
+    too_long = np.zeros((1, shape[2], shape[1], shape[0]))
+    with pytest.raises(Exception):
+        emix.deriv_dev(dev(too_long), axis, h, scheme)
