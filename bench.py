@@ -161,10 +161,8 @@ class ClockSampler:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from emix_gb300 import replicas
+    return replicas.world_from_env()
 
 
 def cpu_sample(steps: int, warmup: int):
@@ -209,14 +207,20 @@ def run_reference(args):
     return 0
 
 
-def ensemble_leg(steps: int, warmup: int, stream=None):
+def ensemble_leg(steps: int, warmup: int, stream=None, world: int = 1, rank: int = 0):
     """The uneven 48-grid ensemble (seed 7): batched persistent launches (autotuned,
     graph-replayed) against the same grids stepped one by one (each grid's own
-    graph).  Returns a dict for the JSON line."""
+    graph).  Under torchrun the grids are split between the ranks (largest
+    first, to the least-loaded rank; no collective on the data path) and the
+    job's time is the slowest rank's.  Returns a dict for the JSON line."""
     import torch
     from emix_gb300 import fields as F
     from emix_gb300 import ops
-    ws = F.ensemble(ngrids=48, seed=7)
+    from emix_gb300 import replicas
+    costs = [nx * ny * nz for nx, ny, nz in F.ensemble_shapes(48, 7)]
+    total_cells = sum(costs)
+    part = replicas.shard_by_cost(costs, world)[rank]
+    ws = F.ensemble(ngrids=48, seed=7, only=set(part))
     b = ops.Batch(ws)
     s = stream or torch.cuda.Stream()
     b.set_stream(s.cuda_stream)
@@ -235,19 +239,22 @@ def ensemble_leg(steps: int, warmup: int, stream=None):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / steps
 
-    ms_b = timed(lambda k: b.step(k, use_graph=True))
-    ms_g = timed(lambda k: b.step_per_grid(k, use_graph=True))
+    replicas.barrier(world)
+    ms_b = replicas.max_over_ranks(timed(lambda k: b.step(k, use_graph=True)), world)
+    replicas.barrier(world)
+    ms_g = replicas.max_over_ranks(timed(lambda k: b.step_per_grid(k, use_graph=True)), world)
     # the batched result agrees with the per-grid result (to rounding)
     b.upload(); b.step(1, use_graph=True); a0 = b.download(0)[0]
     b.upload(); b.step_per_grid(1, use_graph=True); a1 = b.download(0)[0]
-    diff = float(np.max(np.abs(a0 - a1)) / np.max(np.abs(a1)))
+    diff = replicas.max_over_ranks(float(np.max(np.abs(a0 - a1)) / np.max(np.abs(a1))), world)
     tune = b.tuning()
     b.close()
     return {
         "workload": "48 periodic grids, nx,ny,nz each from {32,48,...,160} (seed 7), omega~U[0.5,2]",
-        "cells": ncell, "steps": steps,
-        "batched": {"value": round(ncell / (ms_b * 1e-3) / 1e6, 3), "ms_per_step": round(ms_b, 3)},
-        "per_grid": {"value": round(ncell / (ms_g * 1e-3) / 1e6, 3), "ms_per_step": round(ms_g, 3)},
+        "cells": total_cells, "steps": steps, "ranks": world,
+        "grids_per_rank": len(part), "cells_rank0": ncell,
+        "batched": {"value": round(total_cells / (ms_b * 1e-3) / 1e6, 3), "ms_per_step": round(ms_b, 3)},
+        "per_grid": {"value": round(total_cells / (ms_g * 1e-3) / 1e6, 3), "ms_per_step": round(ms_g, 3)},
         "speedup": round(ms_g / ms_b, 3), "max_rel_diff_vs_per_grid": diff,
         "tuning": {"cells_per_thread": tune[0], "yz_block": tune[1], "ctas_per_sm": tune[2],
                    "autotune_best_ms": round(tuned_ms, 3)},
@@ -402,16 +409,13 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
+    from emix_gb300 import replicas
+
     def barrier():
-        if world > 1:
-            dist.barrier()
+        replicas.barrier(world)
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(x, world, "cuda")
 
     w = F.stirred_tank(n=N_GRID, impeller=IMPELLER)
     n = w.grid.ncell
@@ -535,9 +539,11 @@ def main():
         "kernels": kernels,
         "clocks": {k: clocks[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
     }
-    # the side workloads run at N = 1 only (the scaling runs time the headline step)
-    if world == 1 and not args.no_ensemble:
-        line["ensemble"] = ensemble_leg(min(args.steps, 10), 3, stream)
+    # the single-grid side workloads run at N = 1 only (the scaling runs time
+    # the headline step); the ensemble splits its grids between the ranks
+    if not args.no_ensemble:
+        # N = 1: the whole ensemble; N > 1: the grids split between the ranks
+        line["ensemble"] = ensemble_leg(min(args.steps, 10), 3, stream, world, rank)
     if world == 1 and not args.no_large:
         line["large"] = large_leg(min(args.steps, 5), 3, stream)
     if world == 1 and not args.no_adjoint:

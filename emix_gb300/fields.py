@@ -318,16 +318,29 @@ def random_box(nx, ny, nz, seed=5, periodic=False, scheme=None, mach=0.1) -> Wor
 ENSEMBLE_SIZES = tuple(range(32, 161, 16))   # {32, 48, ..., 160}
 
 
+def ensemble_shapes(ngrids=48, seed=7, sizes=ENSEMBLE_SIZES) -> list:
+    """(nx, ny, nz) of every grid of ensemble(ngrids, seed, sizes=sizes)."""
+    draws = uniform(seed, 100, (ngrids, 4))
+    out = []
+    for g in range(ngrids):
+        idx = np.minimum(((draws[g, :3] + 1.0) * 0.5 * len(sizes)).astype(int), len(sizes) - 1)
+        out.append(tuple(int(sizes[i]) for i in idx))
+    return out
+
+
 def ensemble(ngrids=48, seed=7, cfl=0.3, mach=0.1, scheme=SCHEME_BPER, sizes=ENSEMBLE_SIZES,
-             noise=1e-3) -> list:
+             noise=1e-3, only=None) -> list:
     """Uneven ensemble: grid g has nx, ny, nz drawn independently from
     ``sizes`` and its own rotation rate omega_g ~ U[0.5, 2.0] (seeded), with
     the periodic Taylor-Green fields of the 64^3 configuration scaled by
-    omega_g."""
+    omega_g.  ``only``: build just these grid indices (same grids as in the
+    full ensemble)."""
     draws = uniform(seed, 100, (ngrids, 4))
     out = []
     L = 2.0 * math.pi
     for g in range(ngrids):
+        if only is not None and g not in only:
+            continue
         idx = np.minimum(((draws[g, :3] + 1.0) * 0.5 * len(sizes)).astype(int), len(sizes) - 1)
         nx, ny, nz = (sizes[i] for i in idx)
         omega = 0.5 + 1.5 * 0.5 * (draws[g, 3] + 1.0)
