@@ -31,6 +31,15 @@ struct ReinitArgs {
     int stage, ref_bugs;
 };
 
+// max(x, 0) and max(-x, 0) by the sign bit; x*x of the larger of two
+// non-negative doubles (their bit patterns order as integers)
+EMIX_DEV double pos_part(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
+EMIX_DEV double neg_mag(double x) { return __double_as_longlong(x) < 0 ? -x : 0.0; }
+EMIX_DEV double sq_of_larger(double a, double b) {
+    const double m = __double_as_longlong(a) >= __double_as_longlong(b) ? a : b;
+    return m * m;
+}
+
 EMIX_DEV double bd(const double *f, long base, long s, int p) {
     return p == 0 ? f[base + s] - f[base] : f[base + p * s] - f[base + (p - 1) * s];
 }
@@ -44,7 +53,7 @@ __global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
         const long s3[3] = {1, nxg, sxy};
         const double sc[3] = {a.sx, a.sy, a.sz};
         const double p0 = a.phi0[id];
-        const double ta = (double)(p0 > 0.0) - (double)(p0 < 0.0);
+        const int tsg = (p0 > 0.0) - (p0 < 0.0);   // sign of phi0
         double r = 0.0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -81,12 +90,13 @@ __global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
                                bd(a.src, base, s3[d], p[2]), bd(a.src, base, s3[d], p[3]),
                                bd(a.src, base, s3[d], p[4]), eps);
             }
-            double pmax = fmax(am, 0.0) * fmax(am, 0.0), pmin = fmin(bp, 0.0) * fmin(bp, 0.0);
-            double rd = 0.5 * (ta + 1.0) * fmax(pmax, pmin);
-            pmax = fmax(bp, 0.0) * fmax(bp, 0.0);
-            pmin = fmin(am, 0.0) * fmin(am, 0.0);
-            rd += 0.5 * fabs(ta - 1.0) * fmax(pmax, pmin);
-            r += rd;
+            // Godunov: phi0 > 0 takes max(max(a-, 0)^2, min(b+, 0)^2), phi0 < 0
+            // max(max(b+, 0)^2, min(a-, 0)^2), phi0 = 0 their mean; the larger
+            // of two non-negative magnitudes squared, the magnitudes picked by
+            // sign and compared as integers (squaring is monotone)
+            const double g1 = sq_of_larger(pos_part(am), neg_mag(bp));
+            const double g2 = sq_of_larger(pos_part(bp), neg_mag(am));
+            r += tsg > 0 ? g1 : (tsg < 0 ? g2 : fma(0.5, g2, 0.5 * g1));
         }
         const double dm = a.dmins[id];
         const double rs = (p0 * rsqrt_fast(fma(p0, p0, dm * dm))) * (sqrt_fast(r) - 1.0);
