@@ -126,9 +126,11 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs a) {
         w[d] = (l >= 0 && l < L) ? f[l * s] * J[l * s] : 0.0;
     }
     double y = 0.0;
-    for (int l = 0; l < L; ++l) {
+    // one row: the 11-point right-hand side on the interior rows, the value
+    // itself on the five rows at each end (branch-free runs of rows)
+    auto row = [&](int l, bool interior) {
         double r;
-        if (l >= 5 && l < L - 5)
+        if (interior)
             r = a.ca * w[5] + a.cb * (w[6] + w[4]) + a.cc * (w[7] + w[3]) + a.cd * (w[8] + w[2]) +
                 a.ce * (w[9] + w[1]) + a.cf * (w[10] + w[0]);
         else
@@ -140,7 +142,12 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs a) {
         for (int d = 0; d < 10; ++d) w[d] = w[d + 1];
         const int ln = l + 6;
         w[10] = ln < L ? f[ln * s] * J[ln * s] : 0.0;
-    }
+    };
+    const int lo = L < 5 ? L : 5, hi = L - 5 > lo ? L - 5 : lo;
+    int l = 0;
+    for (; l < lo; ++l) row(l, false);
+    for (; l < hi; ++l) row(l, true);
+    for (; l < L; ++l) row(l, false);
     double x = y;
     f[(long)(L - 1) * s] = x * IJ[(long)(L - 1) * s];
     for (int l = L - 2; l >= 0; --l) {
