@@ -294,10 +294,13 @@ def large_leg(steps: int, warmup: int, stream=None):
     }
 
 
-def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=None, fd=True):
+def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=None, fd=True):
     """dJ/d(omega, Cs) of the tank objective after nsteps steps on the n^3 tank
     by the hand-written adjoint, its cost against the forward steps, and the
-    central finite differences (h = 1e-6) it is checked against."""
+    central finite differences (h = 1e-6) it is checked against.  every = 0:
+    every step's tape kept from the forward pass (the tapes of 128^3 x 8 steps
+    fit in HBM, so nothing is recomputed); every >= 1: checkpoints every
+    `every` steps, each step recomputed with its tape in the reverse sweep."""
     import torch
     from emix_gb300 import fields as F
     from emix_gb300 import ops
@@ -350,6 +353,28 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=N
     r.close()
     cells = w.grid.ncell
     plain = float(np.median(pl))
+    # for comparison: checkpoints every step, each step recomputed with its tape
+    recompute = None
+    if every == 0:
+        r1 = ops.TankGradient(w, nsteps, 1, bc_walls=WALLS)
+        r1.ctx.set_stream(s.cuda_stream)
+        r1.run(om, cs)
+        r1.adj.backward()
+        fw1, bw1 = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r1.run(om, cs)
+            t1 = time.perf_counter()
+            r1.adj.backward()
+            t2 = time.perf_counter()
+            fw1.append(t1 - t0)
+            bw1.append(t2 - t1)
+        gib1 = r1.adj.device_bytes() / 2**30
+        r1.close()
+        f1, b1 = float(np.median(fw1)), float(np.median(bw1))
+        recompute = {"checkpoint_every": 1, "forward_s": round(f1, 4), "backward_s": round(b1, 4),
+                     "adjoint_over_forward": round(b1 / plain, 3),
+                     "gradient_over_forward": round((f1 + b1) / plain, 3), "adjoint_gib": round(gib1, 2)}
     return {
         "workload": f"stirred tank {n}x{n}x{nz or n} walls + rotating impeller, {nsteps} RK3 steps, "
                     "J = annulus kinetic energy + interface area",
@@ -361,9 +386,12 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 1, stream=None, nz=N
         "forward_s": round(t_fw, 4), "backward_s": round(t_bw, 4), "plain_steps_s": round(plain, 4),
         "timing": "medians of three runs each",
         "adjoint_over_forward": round(t_bw / plain, 3),
+        "gradient_over_forward": round((t_fw + t_bw) / plain, 3),
+        "mode": "tapes kept from the forward pass" if every == 0 else f"checkpoints every {every}, recomputed",
         "forward_value": round(cells * nsteps / plain / 1e6, 3),
         "adjoint_value": round(cells * nsteps / t_bw / 1e6, 3),
         "unit": "Mcell-RK3-steps/s", "checkpoint_every": every, "adjoint_gib": round(gib, 2),
+        "recompute": recompute,
     }
 
 

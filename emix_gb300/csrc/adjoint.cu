@@ -7,8 +7,10 @@
 // Reverse: per segment of `every` steps (last first), the states of the
 // segment are recomputed from its checkpoint; per step (last first), the step
 // is recomputed once more with a tape of every substep's inputs (u, pres,
-// dvel, vis, divergence R, the substep's um), then the step's adjoint runs
-// substep by substep in reverse:
+// dvel, vis, divergence R, the substep's um), then the step's adjoint runs.
+// With every = 0, where HBM holds every step's tape, the forward pass tapes
+// each step as it runs and the reverse sweep recomputes nothing.  The step's
+// adjoint runs substep by substep in reverse:
 //   RK update (conversions, impeller, walls, combination) -> divergence (D^T)
 //   -> fluxes -> Smagorinsky -> gradients (D^T) -> level-set stage (WENO5)
 // and finally the primitive variables and the transposed ghost padding.
@@ -20,9 +22,19 @@
 #include <new>
 #include <vector>
 
+// the inputs of one step's substeps that its adjoint reads; in the mode that
+// keeps every step's tape (every = 0) also the level-set stages' padded
+// inputs and the impeller clock, which the context overwrites step by step
+struct Tape {
+    double *um0 = nullptr, *u[3] = {}, *p[3] = {}, *dvel[3] = {}, *vis[3] = {}, *R[3] = {}, *umc[3] = {};
+    double *phig[3] = {};   // keep mode: stage inputs (else the context's buffers)
+    double *clock = nullptr; // keep mode: the step's impeller clock (kImpClockLen)
+};
+
 struct emix_adj {
     emix_ctx *c = nullptr;
     int nsteps = 0, every = 1;
+    bool keep = false;               // every = 0: every step's tape kept, no recomputation
     emix_objective obj{};
     double *arena = nullptr;
     size_t bytes = 0;
@@ -32,8 +44,10 @@ struct emix_adj {
     std::vector<double> seg_clock;
     double *final_state = nullptr;   // 6n, restored after the reverse sweep
     double final_clock[2] = {0, 0};
-    // tape of one step
-    double *t_um0, *t_u[3], *t_p[3], *t_dvel[3], *t_vis[3], *t_R[3], *t_umc[3];
+    // tape of the step being differentiated (tapes[k] in the keep mode)
+    Tape *tape = nullptr;
+    std::vector<Tape> tapes;
+    double *final_clock_full = nullptr;   // keep mode: the clock after the last step
     // adjoint fields
     double *Lum0, *LA, *LB, *LU0, *LU1, *LP0, *LP1, *LR, *LF, *Ldvel, *Lvis, *T5, *W;
     double *Lphi, *Lphi_prev, *Lphig0, *LphiA, *LphiB, *LD;
@@ -102,21 +116,24 @@ int taped_step(emix_adj *a) {
     emix_ctx *c = a->c;
     const long n = c->n;
     cudaStream_t st = c->stream;
-    int rc = copy(a->t_um0, c->um0, 5 * n, st);
+    Tape &T = *a->tape;
+    int rc = copy(T.um0, c->um0, 5 * n, st);
     if (rc) return rc;
     int s = 0;
     for (const Launch &L : c->plan) {
         if (L.kind == LK_WENO) {
             ++s;
-            if ((rc = copy(a->t_u[s - 1], c->u, 3 * n, st))) return rc;
-            if ((rc = copy(a->t_p[s - 1], c->pres, n, st))) return rc;
-            if (s >= 2 && (rc = copy(a->t_umc[s - 1], c->um, 5 * n, st))) return rc;
+            if ((rc = copy(T.u[s - 1], c->u, 3 * n, st))) return rc;
+            if ((rc = copy(T.p[s - 1], c->pres, n, st))) return rc;
+            if (s >= 2 && (rc = copy(T.umc[s - 1], c->um, 5 * n, st))) return rc;
+            if (T.phig[s - 1] && (rc = copy(T.phig[s - 1], L.weno.phi, c->ng, st))) return rc;
         }
         if ((rc = launch_single(L, st))) return rc;
+        if (L.kind == LK_CLOCK && T.clock && (rc = copy(T.clock, c->clock, kImpClockLen, st))) return rc;
         if (s >= 1) {
-            if (L.cls == CLS_GRADZ && (rc = copy(a->t_dvel[s - 1], c->dvel, 9 * n, st))) return rc;
-            if (L.kind == LK_SMAG && (rc = copy(a->t_vis[s - 1], c->vis, n, st))) return rc;
-            if (L.cls == CLS_DIVZ && (rc = copy(a->t_R[s - 1], c->R, 5 * n, st))) return rc;
+            if (L.cls == CLS_GRADZ && (rc = copy(T.dvel[s - 1], c->dvel, 9 * n, st))) return rc;
+            if (L.kind == LK_SMAG && (rc = copy(T.vis[s - 1], c->vis, n, st))) return rc;
+            if (L.cls == CLS_DIVZ && (rc = copy(T.R[s - 1], c->R, 5 * n, st))) return rc;
         }
     }
     return s == 3 ? EMIX_OK : EMIX_ERR_ARG;
@@ -153,15 +170,16 @@ int step_adjoint(emix_adj *a) {
     double *Lo = a->LA, *Lnext = a->LB;          // adjoint of the substep's um output / input
     double *LuOut = nullptr, *LpOut = nullptr;   // adjoint of its u / pres outputs
     double *LuIn = a->LU0, *LpIn = a->LP0;
+    const Tape &T = *a->tape;
     for (int s = 3; s >= 1; --s) {
         const Launch *Lrk = plan_rk(c, s), *Lw = plan_weno(c, s);
         if (!Lrk || !Lw) return EMIX_ERR_ARG;
-        const double *umc = s == 1 ? a->t_um0 : a->t_umc[s - 1];
+        const double *umc = s == 1 ? T.um0 : T.umc[s - 1];
         // RK update
         RkAdjArgs A{};
         A.a = Lrk->rk;
-        A.a.R = a->t_R[s - 1];
-        A.a.um0 = a->t_um0;
+        A.a.R = T.R[s - 1];
+        A.a.um0 = T.um0;
         A.a.um = umc;
         A.lo = Lo; A.lu = LuOut; A.lp = LpOut; A.T5 = a->T5; A.red = a->red;
         k_adj_rk_a<<<grid_n(n), 256, 0, st>>>(A);
@@ -186,14 +204,14 @@ int step_adjoint(emix_adj *a) {
         }
         // fluxes
         FluxAdjArgs F{};
-        F.lF = a->LF; F.umc = umc; F.u = a->t_u[s - 1]; F.vis = a->t_vis[s - 1];
-        F.dvel = a->t_dvel[s - 1]; F.jbn = c->jbn; F.jx = c->jx; F.jy = c->jy; F.jz = c->jz;
+        F.lF = a->LF; F.umc = umc; F.u = T.u[s - 1]; F.vis = T.vis[s - 1];
+        F.dvel = T.dvel[s - 1]; F.jbn = c->jbn; F.jx = c->jx; F.jy = c->jy; F.jz = c->jz;
         F.lumc = s >= 2 ? Lnext : a->Lum0;
         F.lu = LuIn; F.lp = LpIn; F.ldvel = a->Ldvel; F.lvis = a->Lvis; F.n = n;
         k_adj_flux<<<grid_n(n), 256, 0, st>>>(F);
         // Smagorinsky
         SmagAdjArgs S{};
-        S.dvel = a->t_dvel[s - 1]; S.jbn = c->jbn; S.dxyz = c->dxyz; S.lvis = a->Lvis;
+        S.dvel = T.dvel[s - 1]; S.jbn = c->jbn; S.dxyz = c->dxyz; S.lvis = a->Lvis;
         S.cs = p.sgs_model == EMIX_SGS_NONE ? 0.0 : p.cs; S.ldvel = a->Ldvel; S.red = a->red; S.n = n;
         k_adj_smag<<<grid_n(n), 256, 0, st>>>(S);
         // velocity gradients: LuIn[c] += D_ax^T Ldvel[3 ax + c]
@@ -211,11 +229,11 @@ int step_adjoint(emix_adj *a) {
         if ((rc = zero(a->LD, 3 * ng, st))) return rc;
         const WenoArgs &wa = Lw->weno;
         WenoAdjArgs G{};
-        G.phi = wa.phi;
+        G.phi = T.phig[s - 1] ? T.phig[s - 1] : wa.phi;
         G.lout = s == 3 ? a->Lphi : (s == 2 ? a->LphiB : a->LphiA);
         G.lphi0 = a->Lphig0;
         G.lphiin = s == 1 ? a->Lphig0 : (s == 2 ? a->LphiA : a->LphiB);
-        G.lD = a->LD; G.lu = LuIn; G.vel = a->t_u[s - 1]; G.wce = wa.wce;
+        G.lD = a->LD; G.lu = LuIn; G.vel = T.u[s - 1]; G.wce = wa.wce;
         G.nxg = wa.nxg; G.nyg = wa.nyg; G.nzg = wa.nzg; G.g = wa.g;
         for (int d = 0; d < 3; ++d) { G.r0[d] = wa.r0[d]; G.rn[d] = wa.rn[d]; }
         G.dt = wa.dt; G.stage = s;
@@ -228,7 +246,7 @@ int step_adjoint(emix_adj *a) {
         double *t = Lo; Lo = Lnext; Lnext = t;
     }
     // primitive variables of substep 1 (u, pres from um0); LuOut holds their adjoint
-    k_adj_prim<<<grid_n(n), 256, 0, st>>>(a->t_um0, LuOut, LpOut, 1.0 / (p.mach * p.mach), a->Lum0, n);
+    k_adj_prim<<<grid_n(n), 256, 0, st>>>(T.um0, LuOut, LpOut, 1.0 / (p.mach * p.mach), a->Lum0, n);
     if ((rc = zero(a->Lphi_prev, n, st))) return rc;
     k_adj_unpad<<<grid_n(n), 256, 0, st>>>(a->Lphig0, a->Lphi_prev, p.ls_ghost, nx, ny, nz);
     EMIX_CUDA_TRY(cudaGetLastError());
@@ -295,7 +313,7 @@ int run_steps(emix_adj *a, int nsteps, double *store, std::vector<double> *store
 extern "C" {
 
 int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *obj, emix_adj **out) {
-    if (!c || !out || !obj || nsteps < 1 || every < 1 || every > nsteps) return EMIX_ERR_ARG;
+    if (!c || !out || !obj || nsteps < 1 || every < 0 || every > nsteps) return EMIX_ERR_ARG;
     *out = nullptr;
     const emix_params &p = c->p;
     if (!c->static_set || !p.level_set || p.sgs_model == EMIX_SGS_STRUCTURE || !p.imp.on ||
@@ -309,7 +327,8 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     if (!a) return EMIX_ERR_ALLOC;
     a->c = c;
     a->nsteps = nsteps;
-    a->every = every;
+    a->keep = every == 0;
+    a->every = a->keep ? 1 : every;
     a->obj = *obj;
     const int dims[3] = {p.nx, p.ny, p.nz};
     for (int d = 0; d < 3; ++d) {
@@ -317,9 +336,14 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
         if (rc) { delete a; return rc; }
     }
     const long n = c->n, ng = c->ng;
-    const int ncp = (nsteps + every - 1) / every;
-    const long cnt = (long)ncp * 6 * n + (long)every * 6 * n + 6 * n        // checkpoints, segment, final
-                     + 5 * n + 3 * (3 + 1 + 9 + 1 + 5) * n + 2 * 5 * n    // tape
+    const bool keep = a->keep;
+    const int ncp = keep ? 0 : (nsteps + every - 1) / every;
+    const int nseg = keep ? 0 : every;
+    const int ntape = keep ? nsteps : 1;
+    const long tape_cnt = 5 * n + 3 * (3 + 1 + 9 + 1 + 5) * n + 2 * 5 * n      // 72 fields
+                          + (keep ? 3 * ng + kImpClockLen : 0);
+    const long cnt = (long)ncp * 6 * n + (long)nseg * 6 * n + 6 * n        // checkpoints, segment, final
+                     + (long)ntape * tape_cnt + (keep ? kImpClockLen : 0)  // tapes, final clock
                      + 5 * n * 3 + 3 * n * 2 + n * 2 + 5 * n + 15 * n + 9 * n + n + 5 * n + 6 * n
                      + 2 * n + 3 * ng + 3 * ng + 8 + 2048;
     a->bytes = (size_t)cnt * sizeof(double);
@@ -331,17 +355,26 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     }
     double *q = a->arena;
     a->cp = take(q, (long)ncp * 6 * n);
-    a->seg = take(q, (long)every * 6 * n);
+    a->seg = take(q, (long)nseg * 6 * n);
     a->final_state = take(q, 6 * n);
-    a->t_um0 = take(q, 5 * n);
-    for (int s = 0; s < 3; ++s) {
-        a->t_u[s] = take(q, 3 * n);
-        a->t_p[s] = take(q, n);
-        a->t_dvel[s] = take(q, 9 * n);
-        a->t_vis[s] = take(q, n);
-        a->t_R[s] = take(q, 5 * n);
-        a->t_umc[s] = s >= 1 ? take(q, 5 * n) : nullptr;
+    a->tapes.resize(ntape);
+    for (Tape &T : a->tapes) {
+        T.um0 = take(q, 5 * n);
+        for (int s = 0; s < 3; ++s) {
+            T.u[s] = take(q, 3 * n);
+            T.p[s] = take(q, n);
+            T.dvel[s] = take(q, 9 * n);
+            T.vis[s] = take(q, n);
+            T.R[s] = take(q, 5 * n);
+            T.umc[s] = s >= 1 ? take(q, 5 * n) : nullptr;
+        }
+        if (keep) {
+            for (int s = 0; s < 3; ++s) T.phig[s] = take(q, ng);
+            T.clock = take(q, kImpClockLen);
+        }
     }
+    a->tape = &a->tapes[0];
+    a->final_clock_full = keep ? take(q, kImpClockLen) : nullptr;
     a->Lum0 = take(q, 5 * n); a->LA = take(q, 5 * n); a->LB = take(q, 5 * n);
     a->LU0 = take(q, 3 * n); a->LU1 = take(q, 3 * n);
     a->LP0 = take(q, n); a->LP1 = take(q, n);
@@ -352,7 +385,7 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     a->LD = take(q, 3 * ng);
     a->red = take(q, 8 + 2048);   // [0] dJ/domega, [1] dJ/dCs, [2] J, then J's block partials
     a->cp_clock.assign(2 * (size_t)ncp, 0.0);
-    a->seg_clock.assign(2 * (size_t)every, 0.0);
+    a->seg_clock.assign(2 * (size_t)nseg, 0.0);
     *out = a;
     return EMIX_OK;
 }
@@ -374,6 +407,20 @@ int emix_adj_device_bytes(emix_adj *a, size_t *bytes) {
 int emix_adj_forward(emix_adj *a, double *J) {
     if (!a || !J) return EMIX_ERR_ARG;
     int rc;
+    if (a->keep) {
+        // every step taped as it runs: the reverse sweep recomputes nothing
+        emix_ctx *c = a->c;
+        for (int k = 0; k < a->nsteps; ++k) {
+            a->tape = &a->tapes[k];
+            if ((rc = taped_step(a))) return rc;
+            ++c->step_index;   // as emix_step counts its steps
+        }
+        if ((rc = copy(a->final_clock_full, c->clock, kImpClockLen, c->stream))) return rc;
+        if ((rc = save_state(a, a->final_state, a->final_clock))) return rc;
+        if ((rc = objective(a, false, J))) return rc;
+        a->J = *J;
+        return EMIX_OK;
+    }
     // checkpoints every `every` steps from the context's current state
     for (int k = 0; k < a->nsteps; k += a->every) {
         const int cpi = k / a->every;
@@ -392,12 +439,24 @@ int emix_adj_backward(emix_adj *a, double *dJ) {
     emix_ctx *c = a->c;
     const long n = c->n;
     int rc;
+    const long step_index = c->step_index;   // the recomputations below advance it
     if ((rc = zero(a->red, 2, c->stream))) return rc;
     // adjoint of J at the final state: a->LA (um0), a->Lphi (phi)
     if ((rc = load_state(a, a->final_state, a->final_clock))) return rc;
     double J;
     if ((rc = objective(a, true, &J))) return rc;
-    const int ncp = (a->nsteps + a->every - 1) / a->every;
+    if (a->keep) {
+        // the tapes of the forward pass; each step's impeller clock restored
+        for (int k = a->nsteps - 1; k >= 0; --k) {
+            a->tape = &a->tapes[k];
+            if ((rc = copy(c->clock, a->tapes[k].clock, kImpClockLen, c->stream))) return rc;
+            if ((rc = step_adjoint(a))) return rc;
+            double *t = a->LA; a->LA = a->Lum0; a->Lum0 = t;
+            t = a->Lphi; a->Lphi = a->Lphi_prev; a->Lphi_prev = t;
+        }
+        if ((rc = copy(c->clock, a->final_clock_full, kImpClockLen, c->stream))) return rc;
+    }
+    const int ncp = a->keep ? 0 : (a->nsteps + a->every - 1) / a->every;
     for (int cpi = ncp - 1; cpi >= 0; --cpi) {
         const int first = cpi * a->every;
         const int m = first + a->every <= a->nsteps ? a->every : a->nsteps - first;
@@ -421,6 +480,7 @@ int emix_adj_backward(emix_adj *a, double *dJ) {
     dJ[1] = h[1];
     // leave the context at the final state of the forward pass
     if ((rc = load_state(a, a->final_state, a->final_clock))) return rc;
+    c->step_index = step_index;
     return EMIX_OK;
 }
 

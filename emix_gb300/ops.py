@@ -631,7 +631,9 @@ def tank_objective(workload, r_in=0.2, r_out=0.5, radius=1.0, w_ke=1.0, w_if=1.0
 
 
 class Adjoint:
-    """Forward steps with checkpoints and the reverse sweep (``emix_adj``)."""
+    """Forward steps with checkpoints and the reverse sweep (``emix_adj``);
+    every = 0 keeps every step's tape from the forward pass (no recomputation),
+    for runs whose tapes fit in HBM."""
 
     def __init__(self, ctx: "Context", nsteps: int, every: int = 1, objective=None):
         self.lib = _lib.load()

@@ -478,8 +478,12 @@ typedef struct emix_objective {
 typedef struct emix_adj emix_adj;
 
 /* An adjoint of `nsteps` steps of ctx with a checkpoint every `every` steps
- * (1 = every step; larger values trade recomputation for memory).  Covers the
- * tank step: level set on, Smagorinsky (or no SGS), impeller on, no filter. */
+ * (1 = every step; larger values trade recomputation for memory; the reverse
+ * sweep recomputes each step once with its tape).  every = 0: the forward
+ * pass keeps every step's tape (72 fields, the level-set stages' 3 padded
+ * inputs and the impeller clock per step) and the reverse sweep recomputes
+ * nothing, for runs whose tapes fit in HBM.  Covers the tank step: level set
+ * on, Smagorinsky (or no SGS), impeller on, no filter. */
 int emix_adj_create(emix_ctx *ctx, int nsteps, int every, const emix_objective *obj,
                     emix_adj **adj);
 int emix_adj_destroy(emix_adj *adj);

@@ -95,7 +95,7 @@ def _runner(emix, w, steps, every=1):
     return emix.TankGradient(w, steps, every, bc_walls=1)
 
 
-@pytest.mark.parametrize("every", [1, 2])
+@pytest.mark.parametrize("every", [0, 1, 2])
 def test_parameter_gradient_matches_finite_differences(emix, every):
     w = _tank_case()
     r = _runner(emix, w, 3, every)
@@ -119,6 +119,31 @@ def test_parameter_gradient_matches_finite_differences(emix, every):
         fd6 = cfd(k, p0, h6)
         assert abs(g - fd6) <= 1e-6 * abs(fd) + 20 * 2.2e-16 * abs(J) / h6, (k, g, fd6)
     r.close()
+
+
+def test_kept_tapes_give_the_recomputed_gradient(emix):
+    """every = 0 (every step's tape kept from the forward pass, nothing
+    recomputed) against checkpoints every step with recomputation: the same
+    J, dJ/d(omega, Cs) and initial-state adjoint, and the context left at the
+    same final state."""
+    import torch
+    w = _tank_case()
+    out = []
+    for every in (0, 1):
+        r = _runner(emix, w, 3, every)
+        J = r.run(1.3, 0.1)
+        g = r.adj.backward()
+        lum, lphi = r.adj.state_gradient()
+        um, phi = r.ctx.download()
+        out.append((J, g, lum.cpu().numpy(), lphi.cpu().numpy(), um, phi, r.ctx.step_index))
+        r.close()
+    (J0, g0, l0, p0, u0, f0, k0), (J1, g1, l1, p1, u1, f1, k1) = out
+    assert J0 == J1 and k0 == k1
+    assert abs(g0[0] - g1[0]) <= 1e-14 * abs(g1[0]) and abs(g0[1] - g1[1]) <= 1e-14 * abs(g1[1])
+    assert_close(l0, l1, tol=1e-13, what="lum")
+    assert_close(p0, p1, tol=1e-13, what="lphi")
+    assert np.array_equal(u0, u1) and np.array_equal(f0, f1)
+    torch.cuda.synchronize()
 
 
 def test_state_gradient_matches_directional_derivative(emix):
