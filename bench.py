@@ -70,6 +70,8 @@ def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1, dims=None, g: in
         return d * (2 * r[0] + 6 * n + 3 * r[1] + 6 * n + 3 * r[2] + 6 * n) / 3.0
     if name in ("grad_x", "grad_y", "grad_z"):
         return d * 6 * n           # 3 in, 3 out
+    if name == "grad_yz":
+        return d * 9 * n           # 3 in (read once), 6 out
     if name == "div_x":
         return d * 10 * n          # 5 in, 5 out
     if name in ("div_y", "div_z"):
@@ -96,7 +98,7 @@ IMPELLER = True
 # covers, measured with ncu on the 192^3 tank (profiles/step_kernels_full_
 # stirred_tank_192.txt, profiles/weno_stage_stirred_tank_192.txt).
 FP64_OPS_PER_CELL = {
-    "weno_stage": 125.2, "grad_x": 18.0, "grad_y": 18.0, "grad_z": 18.0,
+    "weno_stage": 125.2, "grad_x": 18.0, "grad_y": 18.0, "grad_z": 18.0, "grad_yz": 36.0,
     "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 43.0, "sgs": 28.0,
     "rk_post": 22.8,
 }

@@ -122,6 +122,14 @@ struct DerivRow {
     double A, B, m, g;
 };
 
+// The same factorisation on the scaled unknowns u_i = w_i / k_i, z_i = x_i / k_i,
+// k_i = A_i on stencil rows and 1 on closure rows: a stencil row's forward step
+// is u_i = (d1 + c d2) - mu u_{i-1}, the backward z_i = u_i - gu z_{i+1}, and
+// x_i = k z_i.  Used where the result is accumulated (out += k z in one FMA).
+struct DerivRowU {
+    double c, mu, gu, k;
+};
+
 constexpr int kMaxClosure = 4;   // closure rows at each end
 constexpr int kTableMaxN = 4096; // longest supported pencil
 
@@ -140,6 +148,9 @@ struct DerivTable {
     const double *chi;     // nhi x 4: row n-1-k, coefficients of f_{n-1}..f_{n-4}
     const double *u0;      // ku weights (periodic)
     const double *zz;      // n values (periodic)
+    const DerivRowU *urows;  // n rows of the scaled form
+    const double *u0s;     // ku weights of the scaled form: u0_k k_k (periodic)
+    double sm1s;           // sm1 k_{n-1} (periodic)
 };
 
 // Build the table for (scheme, n, h); rows/u0/zz returned in host vectors.

@@ -5,7 +5,10 @@
 // FP64 pipe (about 0.5 T lane-ops/s) is the binding resource, so the kernels
 // are written to minimise FP64 instructions: per interior cell 2 DADD + 1 DMUL
 // + 1 DFMA for the stencil, 1 DFMA forward, 1 DFMA backward, and no divides
-// (the pivots live in the factor table).
+// (the pivots live in the factor table).  The accumulating y/z form (out +=
+// D f) runs the sweeps on unknowns scaled by the stencil's leading
+// coefficient and restores the scale in the accumulating FMA: 6 operations
+// per cell instead of 7.
 //
 //   y/z pencils: lanes map to consecutive x, so every load and store of a
 //                warp is one 256-byte coalesced access; the pencil walk keeps
@@ -76,6 +79,104 @@ EMIX_DEV double rhs_row(const DerivTable &T, const double *__restrict__ fp, long
 //   axis 2 (z): pencils (x, y), element stride nx*ny, other stride nx
 // grid: (ceil(nx/blockDim.x), nother, nf)
 // ---------------------------------------------------------------------------
+// out += D f along one y/z pencil, on the scaled unknowns of DerivRowU: a
+// stencil row costs 2 DADD + 2 DFMA forward and 2 DFMA backward (the second
+// one restores the scale and accumulates), one FP64 operation fewer than a
+// store followed by an add.
+EMIX_DEV void deriv_yz_accum(const DerivTable &T, const double *__restrict__ in, double *w,
+                             double *out, long s) {
+    const int n = T.n;
+    const DerivRowU *__restrict__ ur = T.urows;
+    double up = 0.0, y0 = 0.0;
+    int i = 0;
+    if (!T.periodic) {
+        // closure rows: k = 1, so u = w
+        for (; i < T.nlo; ++i) {
+            const double v = rhs_row(T, in, s, i) - ur[i].mu * up;
+            w[i * s] = v;
+            up = v;
+        }
+        const int iend = n - T.nhi;
+        if (i < iend) {
+            double fm2 = in[(i - 2) * s], fm1 = in[(i - 1) * s], f0 = in[i * s], fp1 = in[(i + 1) * s];
+            double q0 = in[(i + 2) * s];
+            double q1 = i + 3 < n ? in[(i + 3) * s] : 0.0;
+            double q2 = i + 4 < n ? in[(i + 4) * s] : 0.0;
+            double q3 = i + 5 < n ? in[(i + 5) * s] : 0.0;
+            for (; i < iend; ++i) {
+                const double fp2 = q0;
+                q0 = q1; q1 = q2; q2 = q3;
+                if (i + 6 < n) q3 = in[(i + 6) * s];
+                const DerivRowU r = ur[i];
+                const double t = fma(r.c, fp2 - fm2, fp1 - fm1);
+                const double v = t - r.mu * up;
+                w[i * s] = v;
+                up = v;
+                fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+            }
+        }
+        for (; i < n; ++i) {
+            const double v = rhs_row(T, in, s, i) - ur[i].mu * up;
+            w[i * s] = v;
+            up = v;
+        }
+    } else {
+        double fm2 = in[(n - 2) * s], fm1 = in[(n - 1) * s], f0 = in[0], fp1 = in[s];
+        double nxt = in[2 * s];
+        auto prow = [&](int i, bool acc) {
+            const double fp2 = nxt;
+            int j = i + 3;
+            if (j >= n) j -= n;
+            nxt = in[j * s];
+            const DerivRowU r = ur[i];
+            const double t = fma(r.c, fp2 - fm2, fp1 - fm1);
+            const double v = t - r.mu * up;
+            w[i * s] = v;
+            if (acc) y0 += T.u0s[i] * v;
+            up = v;
+            fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+        };
+        const int ku = T.ku < n ? T.ku : n;
+        for (; i < ku; ++i) prow(i, true);
+        for (; i < n; ++i) prow(i, false);
+    }
+
+    double fact = 0.0;
+    if (T.periodic) fact = (y0 + T.sm1s * up) * T.sm2;
+    double zn = 0.0;
+    double w0 = w[(n - 1) * s];
+    double w1 = w[(n - 2) * s];
+    double w2 = w[(n - 3) * s];
+    double w3 = w[(n - 4) * s];
+    double o0 = out[(n - 1) * s];
+    double o1 = out[(n - 2) * s];
+    double o2 = out[(n - 3) * s];
+    double o3 = out[(n - 4) * s];
+    auto row = [&](int i, bool corr) {
+        const double wi = w0, oi = o0;
+        w0 = w1; w1 = w2; w2 = w3;
+        o0 = o1; o1 = o2; o2 = o3;
+        if (i - 4 >= 0) {
+            w3 = w[(i - 4) * s];
+            o3 = out[(i - 4) * s];
+        }
+        const DerivRowU r = ur[i];
+        const double z = wi - r.gu * zn;
+        zn = z;
+        double acc = oi;
+        if (corr) acc = oi - fact * T.zz[i];
+        out[i * s] = fma(r.k, z, acc);
+    };
+    i = n - 1;
+    if (T.periodic) {
+        for (; i >= T.zhi; --i) row(i, true);
+        for (; i >= T.zlo; --i) row(i, false);
+        for (; i >= 0; --i) row(i, true);
+    } else {
+        for (; i >= 0; --i) row(i, false);
+    }
+}
+
 // Body for one (virtual) block: bid = (x block, pencil row, field).
 template <int EPI>
 EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, int nother, long s,
@@ -88,6 +189,10 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
     const double *__restrict__ in = pick(F.in, f) + base;
     double *w = pick(F.w, f) + base;
     double *out = pick(F.out, f) + base;
+    if constexpr (EPI == EPI_ACCUM) {
+        deriv_yz_accum(T, in, w, out, s);
+        return;
+    }
     const int n = T.n;
     const DerivRow *__restrict__ rows = T.rows;
 
@@ -147,37 +252,25 @@ EMIX_DEV void deriv_yz_body(const DerivTable &T, const PencilFields &F, int nx, 
         for (; i < n; ++i) prow(i, false);
     }
 
-    // backward sweep; w (and the accumulated output) from queues of four rows
-    // loaded four iterations early
+    // backward sweep; w from a queue of four rows loaded four iterations
+    // early (pencils have at least 6 rows)
     double fact = 0.0;
     if (T.periodic) fact = (y0 + T.sm1 * wp) * T.sm2;
     double yn = 0.0;
-    // w0..w3 = w(i) .. w(i-3), o0..o3 the same rows of out
+    // w0..w3 = w(i) .. w(i-3)
     double w0 = w[(n - 1) * s];
-    double w1 = n - 2 >= 0 ? w[(n - 2) * s] : 0.0;
-    double w2 = n - 3 >= 0 ? w[(n - 3) * s] : 0.0;
-    double w3 = n - 4 >= 0 ? w[(n - 4) * s] : 0.0;
-    double o0 = 0.0, o1 = 0.0, o2 = 0.0, o3 = 0.0;
-    if (EPI == EPI_ACCUM) {
-        o0 = out[(n - 1) * s];
-        o1 = n - 2 >= 0 ? out[(n - 2) * s] : 0.0;
-        o2 = n - 3 >= 0 ? out[(n - 3) * s] : 0.0;
-        o3 = n - 4 >= 0 ? out[(n - 4) * s] : 0.0;
-    }
+    double w1 = w[(n - 2) * s];
+    double w2 = w[(n - 3) * s];
+    double w3 = w[(n - 4) * s];
     // one row; the cyclic correction only where zz is nonzero
     auto row = [&](int i, bool corr) {
-        const double wi = w0, oi = o0;
+        const double wi = w0;
         w0 = w1; w1 = w2; w2 = w3;
         if (i - 4 >= 0) w3 = w[(i - 4) * s];
-        if (EPI == EPI_ACCUM) {
-            o0 = o1; o1 = o2; o2 = o3;
-            if (i - 4 >= 0) o3 = out[(i - 4) * s];
-        }
         const double y = wi - rows[i].g * yn;
         yn = y;
         double xv = y;
         if (corr) xv = y - fact * T.zz[i];
-        if (EPI == EPI_ACCUM) xv += oi;
         out[i * s] = xv;
     };
     // branch-free runs: the correction rows [zhi, n) and [0, zlo) of the
@@ -198,6 +291,15 @@ __global__ void __launch_bounds__(128)
 k_deriv_yz(DerivTable T, PencilFields F, int nx, int nother, long s, long os) {
     deriv_yz_body<EPI>(T, F, nx, nother, s, os, blockIdx, threadIdx.x, blockDim.x);
 }
+
+// Two y/z derivatives of the same kind in one launch: fields [0, nfa) along
+// the first table's axis, the rest along the second's.  The velocity
+// gradients' y and z pencils then fill the GPU as one grid of 6 fields, not
+// two grids of 3 whose last waves leave most SMs idle.
+// grid: (ceil(nx/blockDim.x), max(na, nb), nfa + nfb)
+__global__ void __launch_bounds__(128)
+k_deriv_yz_pair(DerivTable Ta, DerivTable Tb, PencilFields F, int nfa, int nx, int na, long sa,
+                long osa, int nb, long sb, long osb);
 
 // ---------------------------------------------------------------------------
 // x pencils: a warp owns 32 consecutive pencils (flattened (j,k)).  Rows are
@@ -365,5 +467,12 @@ k_deriv_x(DerivTable T, PencilFields F, long npencil) {
 int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
                  double *const *w, double *const *out, int nx, int ny, int nz,
                  cudaStream_t st);
+
+// Stored y and z derivatives in one launch (k_deriv_yz_pair): nfa fields
+// along axis 1 (in/out [0, nfa)), nfb along axis 2 (the next nfb); w = out.
+// The outputs must not alias each other or the inputs.
+int launch_deriv_yz_pair(const DerivTable &Ty, const DerivTable &Tz, int nfa, int nfb,
+                         const double *const *in, double *const *out, int nx, int ny, int nz,
+                         cudaStream_t st);
 
 } // namespace emix

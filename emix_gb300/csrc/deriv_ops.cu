@@ -70,6 +70,35 @@ int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *c
     return EMIX_OK;
 }
 
+__global__ void __launch_bounds__(128)
+k_deriv_yz_pair(DerivTable Ta, DerivTable Tb, PencilFields F, int nfa, int nx, int na, long sa,
+                long osa, int nb, long sb, long osb) {
+    if ((int)blockIdx.z < nfa)
+        deriv_yz_body<EPI_STORE>(Ta, F, nx, na, sa, osa, blockIdx, threadIdx.x, blockDim.x);
+    else
+        deriv_yz_body<EPI_STORE>(Tb, F, nx, nb, sb, osb, blockIdx, threadIdx.x, blockDim.x);
+}
+
+int launch_deriv_yz_pair(const DerivTable &Ty, const DerivTable &Tz, int nfa, int nfb,
+                         const double *const *in, double *const *out, int nx, int ny, int nz,
+                         cudaStream_t st) {
+    if (nfa < 1 || nfb < 1 || nfa + nfb > kMaxFields || Ty.n != ny || Tz.n != nz) return EMIX_ERR_ARG;
+    if (ny > 65535 || nz > 65535) return EMIX_ERR_ARG;
+    PencilFields F{};
+    for (int f = 0; f < nfa + nfb; ++f) {
+        F.in[f] = in[f];
+        F.w[f] = out[f];
+        F.out[f] = out[f];
+    }
+    const int bs = nx <= 32 ? 32 : (nx <= 64 ? 64 : 128);
+    // axis 1: pencils (x, z); axis 2: pencils (x, y)
+    dim3 grid((nx + bs - 1) / bs, ny > nz ? ny : nz, nfa + nfb);
+    k_deriv_yz_pair<<<grid, bs, 0, st>>>(Ty, Tz, F, nfa, nx, nz, (long)nx, (long)nx * ny, ny,
+                                         (long)nx * ny, (long)nx);
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
+
 namespace {
 
 bool dims_ok(int nx, int ny, int nz) {

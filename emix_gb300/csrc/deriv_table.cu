@@ -232,8 +232,26 @@ int get_table_signed(int scheme, int n, double h, double sign, DerivTable *out) 
     int rc = build_table_signed(scheme, n, h, sign, t, rows.data(), clo.data(), chi.data(),
                                 u0.data(), zz.data());
     if (rc) return rc;
-    // one allocation: rows | clo | chi | u0 | zz
-    const size_t nd = (size_t)4 * n + 8 * kMaxClosure + 2 * (size_t)n;
+    // the scaled form: k_i = A_i on stencil rows, 1 on the closure rows
+    std::vector<double> kap(n), u0s(n, 0.0);
+    std::vector<DerivRowU> urows(n);
+    for (int i = 0; i < n; ++i) {
+        const bool closure = !t.periodic && (i < t.nlo || i >= n - t.nhi);
+        kap[i] = closure ? 1.0 : rows[i].A;
+        if (kap[i] == 0.0 || !std::isfinite(kap[i])) return EMIX_ERR_ARG;
+    }
+    for (int i = 0; i < n; ++i) {
+        const bool closure = !t.periodic && (i < t.nlo || i >= n - t.nhi);
+        DerivRowU &u = urows[i];
+        u.c = closure ? 0.0 : rows[i].B / rows[i].A;
+        u.mu = i == 0 ? 0.0 : rows[i].m * (kap[i - 1] / kap[i]);
+        u.gu = i == n - 1 ? 0.0 : rows[i].g * (kap[i + 1] / kap[i]);
+        u.k = kap[i];
+    }
+    for (int k = 0; k < t.ku; ++k) u0s[k] = u0[k] * kap[k];
+    t.sm1s = t.sm1 * kap[n - 1];
+    // one allocation: rows | clo | chi | u0 | zz | urows | u0s
+    const size_t nd = (size_t)4 * n + 8 * kMaxClosure + 2 * (size_t)n + 4 * (size_t)n + n;
     double *buf = nullptr;
     if (cudaMalloc(&buf, nd * sizeof(double)) != cudaSuccess) {
         set_last_message("cudaMalloc of a derivative table failed");
@@ -246,12 +264,16 @@ int get_table_signed(int scheme, int n, double h, double sign, DerivTable *out) 
     std::memcpy(p + 4 * kMaxClosure, chi.data(), 4 * kMaxClosure * sizeof(double));
     std::memcpy(p + 8 * kMaxClosure, u0.data(), (size_t)n * sizeof(double));
     std::memcpy(p + 8 * kMaxClosure + n, zz.data(), (size_t)n * sizeof(double));
+    std::memcpy(p + 8 * kMaxClosure + 2 * n, urows.data(), (size_t)n * sizeof(DerivRowU));
+    std::memcpy(p + 8 * kMaxClosure + 6 * n, u0s.data(), (size_t)n * sizeof(double));
     EMIX_CUDA_TRY(cudaMemcpy(buf, host.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
     t.rows = reinterpret_cast<const DerivRow *>(buf);
     t.clo = buf + 4 * (size_t)n;
     t.chi = t.clo + 4 * kMaxClosure;
     t.u0 = t.chi + 4 * kMaxClosure;
     t.zz = t.u0 + n;
+    t.urows = reinterpret_cast<const DerivRowU *>(t.zz + n);
+    t.u0s = t.zz + 5 * (size_t)n;
     g_tables[key] = t;
     *out = t;
     return EMIX_OK;

@@ -295,10 +295,20 @@ EMIX_DEV void rk_convert(const RkArgs &a, long q, double v[5]) {
     const double rr = rcp_fast(r);
     const double mk = a.mask[q];
     // velocity, clipped and masked; the reference's masked momentum u r mk
-    // divided by r again is u mk
+    // divided by r again is u mk.  A mask of exactly 1 or +0 (the usual
+    // case) applies by bit operations: c * 1 = c, and c * 0 = +-0 with c's
+    // sign for the finite clipped c; any other mask value multiplies
     double uu[3];
+    const long long mb = __double_as_longlong(mk);
+    if (mb == 0x3FF0000000000000LL || mb == 0) {
+        const long long keep = mb ? -1LL : (long long)0x8000000000000000ULL;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) uu[d] = clip6(v[d + 1] * rr) * mk;
+        for (int d = 0; d < 3; ++d)
+            uu[d] = __longlong_as_double(__double_as_longlong(clip6(v[d + 1] * rr)) & keep);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) uu[d] = clip6(v[d + 1] * rr) * mk;
+    }
     const double p = r * a.inv_m2;
     const double r1 = p * (a.mach * a.mach);
     a.out[q] = r1;

@@ -96,7 +96,7 @@ using namespace emix;
 
 static const char *kClassNames[] = {
     "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
-    "div_x", "div_y", "div_z", "rk_post", "filter"};
+    "div_x", "div_y", "div_z", "rk_post", "filter", "grad_yz"};
 
 namespace emix {
 const std::vector<Launch> &ctx_plan(emix_ctx *c) { return c->plan; }
@@ -201,10 +201,12 @@ void build_plan(emix_ctx *c) {
         }
         // velocity gradients (cudaDeriv; dT/dx_i feeds nothing on this path:
         // the m=5 viscous fluxes are zero, flujos_compact.f90:187-214)
+        // (the y and z records run as one launch in a single-grid step)
         for (int ax = 0; ax < 3; ++ax) {
             const double *in[3] = {c->u, c->u + n, c->u + 2 * n};
             double *out[3] = {c->dvel + 3 * ax * n, c->dvel + (3 * ax + 1) * n, c->dvel + (3 * ax + 2) * n};
             P.push_back(deriv_launch(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, CLS_GRADX + ax));
+            if (ax == 1) P.back().deriv.pair = 1;
         }
         // SGS viscosity
         if (p.sgs_model == EMIX_SGS_STRUCTURE) {
@@ -291,7 +293,24 @@ int issue_step(emix_ctx *c) {
     const bool fork = c->overlap && c->side && !c->prof;
     int s = 0;
     bool joined = true;
-    for (const Launch &L : c->plan) {
+    const size_t np = c->plan.size();
+    int launches = 0;
+    for (size_t k = 0; k < np; ++k) {
+        const Launch &L = c->plan[k];
+        if (L.kind == LK_DERIV_YZ && L.deriv.pair && k + 1 < np && c->plan[k + 1].kind == LK_DERIV_YZ) {
+            // the gradients' y and z records as one launch
+            const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
+            const double *in[kMaxFields];
+            double *out[kMaxFields];
+            for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
+            for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
+            ProfScope ps(c, CLS_GRADYZ);
+            int rc = launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, c->stream);
+            if (rc) return rc;
+            ++k;
+            ++launches;
+            continue;
+        }
         if (fork && L.kind == LK_WENO) {
             EMIX_CUDA_TRY(cudaEventRecord(c->fork_ev[s], c->stream));
             EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->fork_ev[s], 0));
@@ -300,6 +319,7 @@ int issue_step(emix_ctx *c) {
             EMIX_CUDA_TRY(cudaEventRecord(c->join_ev[s], c->side));
             joined = false;
             ++s;
+            ++launches;
             continue;
         }
         if (fork && !joined && L.kind == LK_RK) {
@@ -309,9 +329,10 @@ int issue_step(emix_ctx *c) {
         ProfScope ps(c, L.cls);
         int rc = launch_single(L, c->stream);
         if (rc) return rc;
+        ++launches;
     }
     if (fork && !joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
-    c->launches = (int)c->plan.size();
+    c->launches = launches;
     return EMIX_OK;
 }
 
@@ -692,7 +713,15 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
 
 int emix_ctx_launches_per_step(emix_ctx *c) {
     if (!c) return -1;
-    return (int)c->plan.size();
+    // every record is one launch, except a pair of gradient records (one)
+    int k = 0;
+    const size_t np = c->plan.size();
+    for (size_t q = 0; q < np; ++q) {
+        const Launch &L = c->plan[q];
+        if (L.kind == LK_DERIV_YZ && L.deriv.pair && q + 1 < np && c->plan[q + 1].kind == LK_DERIV_YZ) ++q;
+        ++k;
+    }
+    return k;
 }
 
 long long emix_ctx_device_bytes(emix_ctx *c) { return c ? (long long)c->arena_bytes : -1; }
