@@ -78,6 +78,8 @@ def algorithmic_bytes(name: str, n: int, ng: int, sgs: int = 1, dims=None, g: in
         return d * 15 * n          # 5 in, 5 accumulated (read + write)
     if name == "flux":
         return d * 40 * n          # um 5, u 3, p, dvel 9, vis, jbn 3, J*metric 3 -> 15
+    if name == "sgs_flux":
+        return d * 41 * n          # the flux reads with dxyz for vis -> vis and the 15 fluxes
     if name == "sgs":
         return d * (14 if sgs == 1 else 20) * n
     if name == "rk_post":
@@ -99,7 +101,7 @@ IMPELLER = True
 # stirred_tank_192.txt, profiles/weno_stage_stirred_tank_192.txt).
 FP64_OPS_PER_CELL = {
     "weno_stage": 125.2, "grad_x": 18.0, "grad_y": 18.0, "grad_z": 18.0, "grad_yz": 36.0,
-    "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 43.0, "sgs": 28.0,
+    "div_x": 30.1, "div_y": 35.1, "div_z": 35.1, "flux": 43.0, "sgs": 28.0, "sgs_flux": 59.0,
     "rk_post": 22.8,
 }
 

@@ -23,7 +23,7 @@ enum LaunchKind {
 // profile classes (emix_ctx_profile)
 enum {
     CLS_PRIM, CLS_PAD, CLS_WENO, CLS_GRADX, CLS_GRADY, CLS_GRADZ, CLS_SGS, CLS_FLUX,
-    CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_FILTER, CLS_GRADYZ, CLS_COUNT
+    CLS_DIVX, CLS_DIVY, CLS_DIVZ, CLS_RK, CLS_FILTER, CLS_GRADYZ, CLS_SGSFLUX, CLS_COUNT
 };
 
 struct DerivArgs {

@@ -98,6 +98,9 @@ __global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__
 __global__ void k_prim(PrimArgs a) { EMIX_FOR_CELLS(q, a.n) prim_cell(a, q); }
 __global__ void __launch_bounds__(256, 2) k_flux_all(FluxArgs a) { EMIX_FOR_CELLS(q, a.n) flux_cell(a, q); }
 __global__ void k_sgs_smag(SmagArgs a) { EMIX_FOR_CELLS(q, a.n) smag_cell(a, q); }
+__global__ void __launch_bounds__(256, 2) k_smag_flux(SmagArgs s, FluxArgs f) {
+    EMIX_FOR_CELLS(q, f.n) smag_flux_cell(s, f, q);
+}
 __global__ void k_sgs_sf(SfArgs a) { EMIX_FOR_CELLS(q, a.n) sf_cell(a, q); }
 __global__ void k_vort(VortArgs a) { EMIX_FOR_CELLS(q, a.n) vort_cell(a, q); }
 __global__ void k_selective(SelArgs a) { EMIX_FOR_CELLS(q, a.n) select_cell(a, q); }

@@ -56,45 +56,65 @@ struct FluxArgs {
     long n;
 };
 
-EMIX_DEV void flux_cell(const FluxArgs &a, long q) {
+// ---- velocity-gradient pieces shared by the SGS viscosity and the fluxes ----
+// The physical normal gradients sxx = ux, syy = vy, szz = wz (dvel times the
+// metric terms jbn1, jbn5, jbn9) and the shear sums sxy = uy + vx, sxz = uz +
+// wx, syz = vz + wy (flujos_compact.f90:68-70, :79-81, :123-125).
+struct Strain {
+    double sxx, syy, szz, sxy, sxz, syz;
+};
+
+EMIX_DEV Strain strain_cell(const double *__restrict__ jbn, const double *__restrict__ dvel, long n, long q) {
+    const double j1 = jbn[q], j5 = jbn[4 * n + q], j9 = jbn[8 * n + q];
+    const double *dv = dvel + q;
+    Strain s;
+    s.sxx = j1 * dv[0];
+    s.syy = j5 * dv[4 * n];
+    s.szz = j9 * dv[8 * n];
+    s.sxy = fma(j5, dv[3 * n], j1 * dv[n]);
+    s.sxz = fma(j9, dv[6 * n], j1 * dv[2 * n]);
+    s.syz = fma(j9, dv[7 * n], j5 * dv[5 * n]);
+    return s;
+}
+
+// fluxes of the cell from its strain pieces and viscosity vs
+EMIX_DEV void flux_from(const FluxArgs &a, long q, const Strain &s, double vs) {
     const long n = a.n;
     const double um2 = a.um[n + q], um3 = a.um[2 * n + q], um4 = a.um[3 * n + q],
                  um5 = a.um[4 * n + q];
     const double u1 = a.u[q], u2 = a.u[n + q], u3 = a.u[2 * n + q];
-    const double p = a.pres[q], vs = a.vis[q];
-    const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
-    const double *dv = a.dvel + q;
+    const double p = a.pres[q];
     const double JX = a.jx[q], JY = a.jy[q], JZ = a.jz[q];
-    // strain pieces shared by the viscous fluxes of equations 2..4
-    const double sxx = j1 * dv[0], syy = j5 * dv[4 * n], szz = j9 * dv[8 * n];
-    const double sxy = j1 * dv[n] + j5 * dv[3 * n];        // p1+p2 of :68-70 and :102-104
-    const double sxz = j1 * dv[2 * n] + j9 * dv[6 * n];    // :79-81 and :147-149
-    const double syz = j9 * dv[7 * n] + j5 * dv[5 * n];    // :123-125 and :157-159
-    const double vxy = vs * sxy, vxz = vs * sxz, vyz = vs * syz;
+    const double vxy = vs * s.sxy, vxz = vs * s.sxz, vyz = vs * s.syz;
     const double vs2 = vs + vs;   // the normal viscous terms' 2 vis
     // equation 1
     a.F[0][q] = JX * (-um2);
     a.F[1][q] = JY * (-um3);
     a.F[2][q] = JZ * (-um4);
     // equation 2
-    a.F[3][q] = JX * ((-um2 * u1 - p) + vs2 * sxx);
-    a.F[4][q] = JY * (-um3 * u1 + vxy);
-    a.F[5][q] = JZ * (-um4 * u1 + vxz);
+    a.F[3][q] = JX * fma(vs2, s.sxx, fma(-um2, u1, -p));
+    a.F[4][q] = JY * fma(-um3, u1, vxy);
+    a.F[5][q] = JZ * fma(-um4, u1, vxz);
     // equation 3
-    a.F[6][q] = JX * (-um2 * u2 + vxy);
-    a.F[7][q] = JY * ((-um3 * u2 - p) + vs2 * syy);
-    a.F[8][q] = JZ * (-um4 * u2 + vyz);
+    a.F[6][q] = JX * fma(-um2, u2, vxy);
+    a.F[7][q] = JY * fma(vs2, s.syy, fma(-um3, u2, -p));
+    a.F[8][q] = JZ * fma(-um4, u2, vyz);
     // equation 4
-    a.F[9][q] = JX * (-um2 * u3 + vxz);
-    a.F[10][q] = JY * (-um3 * u3 + vyz);
-    a.F[11][q] = JZ * ((-um4 * u3 - p) + vs2 * szz);
+    a.F[9][q] = JX * fma(-um2, u3, vxz);
+    a.F[10][q] = JY * fma(-um3, u3, vyz);
+    a.F[11][q] = JZ * fma(vs2, s.szz, fma(-um4, u3, -p));
     // equation 5
     a.F[12][q] = JX * (-u1 * um5);
     a.F[13][q] = JY * (-u2 * um5);
     a.F[14][q] = JZ * (-u3 * um5);
 }
 
+EMIX_DEV void flux_cell(const FluxArgs &a, long q) {
+    flux_from(a, q, strain_cell(a.jbn, a.dvel, a.n, q), a.vis[q]);
+}
+
 // ---- Smagorinsky: amut = (Cs*Delta)^2 sqrt(2 S_ij S_ij), vis = c4 + amut ------
+// 2 S_ij S_ij = 2 (ux^2 + vy^2 + wz^2) + sxy^2 + sxz^2 + syz^2
 struct SmagArgs {
     const double *dvel, *jbn, *dxyz;
     double cs, c4;
@@ -102,19 +122,29 @@ struct SmagArgs {
     long n;
 };
 
+EMIX_DEV double smag_amut(const Strain &s, double cs, double delta) {
+    const double nn = fma(s.szz, s.szz, fma(s.syy, s.syy, s.sxx * s.sxx));
+    const double sh = fma(s.syz, s.syz, fma(s.sxz, s.sxz, s.sxy * s.sxy));
+    const double cd = cs * delta;
+    return (cd * cd) * sqrt_fast(fma(2.0, nn, sh));
+}
+
 EMIX_DEV void smag_cell(const SmagArgs &a, long q) {
-    const long n = a.n;
-    const double j1 = a.jbn[q], j5 = a.jbn[4 * n + q], j9 = a.jbn[8 * n + q];
-    const double *dv = a.dvel + q;
-    const double ux = j1 * dv[0], vx = j1 * dv[n], wx = j1 * dv[2 * n];
-    const double uy = j5 * dv[3 * n], vy = j5 * dv[4 * n], wy = j5 * dv[5 * n];
-    const double uz = j9 * dv[6 * n], vz = j9 * dv[7 * n], wz = j9 * dv[8 * n];
-    const double s12 = 0.5 * (uy + vx), s13 = 0.5 * (uz + wx), s23 = 0.5 * (vz + wy);
-    const double ss = ux * ux + vy * vy + wz * wz + 2.0 * (s12 * s12 + s13 * s13 + s23 * s23);
-    const double cd = a.cs * a.dxyz[q];
-    const double am = cd * cd * sqrt_fast(2.0 * ss);
+    const double am = smag_amut(strain_cell(a.jbn, a.dvel, a.n, q), a.cs, a.dxyz[q]);
     if (a.amut) a.amut[q] = am;
-    a.vis[q] = a.c4 * 1.0 + am;
+    a.vis[q] = a.c4 + am;
+}
+
+// Smagorinsky and the fluxes of one cell from one set of strain pieces (the
+// two launches of a substep as one: the same values as smag_cell followed by
+// flux_cell, bit for bit, with the strain pieces formed once)
+EMIX_DEV void smag_flux_cell(const SmagArgs &sa, const FluxArgs &fa, long q) {
+    const Strain s = strain_cell(fa.jbn, fa.dvel, fa.n, q);
+    const double am = smag_amut(s, sa.cs, sa.dxyz[q]);
+    if (sa.amut) sa.amut[q] = am;
+    const double vs = sa.c4 + am;
+    sa.vis[q] = vs;
+    flux_from(fa, q, s, vs);
 }
 
 // ---- selective structure-function model (solver/sgdm_incomp.f90) ------------
@@ -396,6 +426,7 @@ EMIX_DEV void rk_cell(const RkArgs &a, long q) {
 __global__ void k_prim(PrimArgs a);
 __global__ void k_flux_all(FluxArgs a);
 __global__ void k_sgs_smag(SmagArgs a);
+__global__ void k_smag_flux(SmagArgs s, FluxArgs f);
 __global__ void k_sgs_sf(SfArgs a);
 __global__ void k_vort(VortArgs a);
 __global__ void k_selective(SelArgs a);

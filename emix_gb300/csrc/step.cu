@@ -96,7 +96,7 @@ using namespace emix;
 
 static const char *kClassNames[] = {
     "prim", "ghost_pad", "weno_stage", "grad_x", "grad_y", "grad_z", "sgs", "flux",
-    "div_x", "div_y", "div_z", "rk_post", "filter", "grad_yz"};
+    "div_x", "div_y", "div_z", "rk_post", "filter", "grad_yz", "sgs_flux"};
 
 namespace emix {
 const std::vector<Launch> &ctx_plan(emix_ctx *c) { return c->plan; }
@@ -289,6 +289,22 @@ void build_plan(emix_ctx *c) {
     }
 }
 
+// Records k and k+1 of a single-grid plan that run as one launch: the
+// gradients' y and z records (1), Smagorinsky and the fluxes that read its
+// viscosity (2); 0 otherwise.  The records stay separate in the plan: the
+// batched step and the adjoint's taped step run them one by one.
+int fused_with_next(const std::vector<Launch> &P, size_t k) {
+    if (k + 1 >= P.size()) return 0;
+    const Launch &L = P[k], &M = P[k + 1];
+    if (L.kind == LK_DERIV_YZ && L.deriv.pair && M.kind == LK_DERIV_YZ && L.deriv.epi == EPI_STORE &&
+        M.deriv.epi == EPI_STORE && L.deriv.nf + M.deriv.nf <= kMaxFields)
+        return 1;
+    if (L.kind == LK_SMAG && M.kind == LK_FLUX && M.flux.vis == L.smag.vis && M.flux.dvel == L.smag.dvel &&
+        M.flux.jbn == L.smag.jbn && M.flux.n == L.smag.n)
+        return 2;
+    return 0;
+}
+
 int issue_step(emix_ctx *c) {
     const bool fork = c->overlap && c->side && !c->prof;
     int s = 0;
@@ -297,7 +313,8 @@ int issue_step(emix_ctx *c) {
     int launches = 0;
     for (size_t k = 0; k < np; ++k) {
         const Launch &L = c->plan[k];
-        if (L.kind == LK_DERIV_YZ && L.deriv.pair && k + 1 < np && c->plan[k + 1].kind == LK_DERIV_YZ) {
+        const int fuse = fused_with_next(c->plan, k);
+        if (fuse == 1) {
             // the gradients' y and z records as one launch
             const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
             const double *in[kMaxFields];
@@ -307,6 +324,15 @@ int issue_step(emix_ctx *c) {
             ProfScope ps(c, CLS_GRADYZ);
             int rc = launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, c->stream);
             if (rc) return rc;
+            ++k;
+            ++launches;
+            continue;
+        }
+        if (fuse == 2) {
+            ProfScope ps(c, CLS_SGSFLUX);
+            const FluxArgs &fa = c->plan[k + 1].flux;
+            k_smag_flux<<<cells_grid(fa.n), 256, 0, c->stream>>>(L.smag, fa);
+            EMIX_CUDA_TRY(cudaGetLastError());
             ++k;
             ++launches;
             continue;
@@ -713,12 +739,11 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
 
 int emix_ctx_launches_per_step(emix_ctx *c) {
     if (!c) return -1;
-    // every record is one launch, except a pair of gradient records (one)
+    // every record is one launch, except the pairs that run as one
     int k = 0;
     const size_t np = c->plan.size();
     for (size_t q = 0; q < np; ++q) {
-        const Launch &L = c->plan[q];
-        if (L.kind == LK_DERIV_YZ && L.deriv.pair && q + 1 < np && c->plan[q + 1].kind == LK_DERIV_YZ) ++q;
+        if (fused_with_next(c->plan, q)) ++q;
         ++k;
     }
     return k;
