@@ -49,6 +49,13 @@ struct emix_ctx {
     // default where the copy unit's alignment rules hold), one map per stage
     bool tma = true;
     CUtensorMap weno_tmap[3];
+    // emix_step_host's last step: the copies of phi and um back to the host
+    // start on `side` as soon as each part is final (phi after the last
+    // level-set stage, um by z-slabs of the last RK update)
+    static constexpr int kE2eSlabs = 4;
+    double *e2e_um = nullptr, *e2e_phi = nullptr;
+    bool e2e_um_done = false;
+    cudaEvent_t e2e_ev[kE2eSlabs + 2] = {};
 };
 
 namespace emix {

@@ -33,6 +33,18 @@ void set_last_message(const char *msg) { t_last_error = msg ? msg : ""; }
 const char *last_error() { return t_last_error.c_str(); }
 
 // ---- launch helper ------------------------------------------------------
+// Block width of the y/z pencil kernels: the one of 128, 64, 32 threads that
+// leaves the fewest idle lanes in the last block of a row (ties to the wider),
+// e.g. 64 for nx = 192 where 128 would idle a quarter of the threads.
+int yz_block(int nx) {
+    int best = 128, waste = ((nx + 127) / 128) * 128 - nx;
+    for (int bs : {64, 32}) {
+        const int w = ((nx + bs - 1) / bs) * bs - nx;
+        if (w < waste) { best = bs; waste = w; }
+    }
+    return best;
+}
+
 int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *const *in,
                  double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st) {
     if (nf < 1 || nf > kMaxFields) return EMIX_ERR_ARG;
@@ -55,7 +67,7 @@ int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *c
         else
             k_deriv_x<EPI_ACCUM><<<grid, 32 * warps, shm, st>>>(T, F, np);
     } else {
-        const int bs = nx <= 32 ? 32 : (nx <= 64 ? 64 : 128);
+        const int bs = yz_block(nx);
         const int nother = axis == 1 ? nz : ny;
         const long s = axis == 1 ? (long)nx : (long)nx * ny;
         const long os = axis == 1 ? (long)nx * ny : (long)nx;
@@ -90,7 +102,7 @@ int launch_deriv_yz_pair(const DerivTable &Ty, const DerivTable &Tz, int nfa, in
         F.w[f] = out[f];
         F.out[f] = out[f];
     }
-    const int bs = nx <= 32 ? 32 : (nx <= 64 ? 64 : 128);
+    const int bs = yz_block(nx);
     // axis 1: pencils (x, z); axis 2: pencils (x, y)
     dim3 grid((nx + bs - 1) / bs, ny > nz ? ny : nz, nfa + nfb);
     k_deriv_yz_pair<<<grid, bs, 0, st>>>(Ty, Tz, F, nfa, nx, nz, (long)nx, (long)nx * ny, ny,

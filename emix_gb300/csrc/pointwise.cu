@@ -104,7 +104,11 @@ __global__ void __launch_bounds__(256, 2) k_smag_flux(SmagArgs s, FluxArgs f) {
 __global__ void k_sgs_sf(SfArgs a) { EMIX_FOR_CELLS(q, a.n) sf_cell(a, q); }
 __global__ void k_vort(VortArgs a) { EMIX_FOR_CELLS(q, a.n) vort_cell(a, q); }
 __global__ void k_selective(SelArgs a) { EMIX_FOR_CELLS(q, a.n) select_cell(a, q); }
-__global__ void k_rk_post(RkArgs a) { EMIX_FOR_CELLS(q, rk_count(a)) rk_cell(a, q); }
+__global__ void k_rk_post(RkArgs a) {
+    const long end = a.qend > 0 ? a.qend : rk_count(a);
+    for (long q = a.qbeg + blockIdx.x * (long)blockDim.x + threadIdx.x; q < end; q += (long)gridDim.x * blockDim.x)
+        rk_cell(a, q);
+}
 
 } // namespace emix
 

@@ -269,6 +269,7 @@ struct RkArgs {
     const double *xyz;    // coordinates (3 fields), read when imp.on
     const double *clock;  // impeller clock (k_imp_clock), read when imp.on
     const unsigned char *impflag;   // cells the impeller can reach (k_imp_flags)
+    long qbeg, qend;      // single-grid launches: cells [qbeg, qend) only (qend = 0: all)
 };
 
 // Wall cells: z = 0, nz-2, nz-1 (frontera_z), y = 0, ny-1 (frontera_y),

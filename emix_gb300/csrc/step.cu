@@ -289,6 +289,10 @@ void build_plan(emix_ctx *c) {
     }
 }
 
+bool filter_due(const emix_ctx *c) {
+    return c->p.filter_every > 0 && c->step_index % c->p.filter_every == 0;
+}
+
 // Records k and k+1 of a single-grid plan that run as one launch: the
 // gradients' y and z records (1), Smagorinsky and the fluxes that read its
 // viscosity (2); 0 otherwise.  The records stay separate in the plan: the
@@ -352,10 +356,42 @@ int issue_step(emix_ctx *c) {
             EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
             joined = true;
         }
+        if (c->e2e_um && L.kind == LK_RK && L.rk.stage == 3 && !L.rk.faces && k + 1 == np && !filter_due(c)) {
+            // the step's last launch by z-slabs, each slab's um copied back to
+            // the host on the side stream as soon as it is written
+            const long n = c->n, plane = (long)L.rk.nx * L.rk.ny;
+            const int S = emix_ctx::kE2eSlabs;
+            for (int b = 0; b < S; ++b) {
+                const long q0 = plane * (long)(L.rk.nz * b / S), q1 = plane * (long)(L.rk.nz * (b + 1) / S);
+                if (q1 <= q0) continue;
+                RkArgs ra = L.rk;
+                ra.qbeg = q0;
+                ra.qend = q1;
+                k_rk_post<<<cells_grid(q1 - q0), 256, 0, c->stream>>>(ra);
+                EMIX_CUDA_TRY(cudaGetLastError());
+                ++launches;
+                EMIX_CUDA_TRY(cudaEventRecord(c->e2e_ev[1 + b], c->stream));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->e2e_ev[1 + b], 0));
+                for (int m = 0; m < 5; ++m)
+                    EMIX_CUDA_TRY(cudaMemcpyAsync(c->e2e_um + m * n + q0, L.rk.out + m * n + q0,
+                                                  (size_t)(q1 - q0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                                  c->side));
+            }
+            c->e2e_um_done = true;
+            continue;
+        }
         ProfScope ps(c, L.cls);
         int rc = launch_single(L, c->stream);
         if (rc) return rc;
         ++launches;
+        if (c->e2e_phi && L.kind == LK_WENO && L.weno.stage == 3) {
+            // phi is final: copy it back while the substep's flow kernels run
+            EMIX_CUDA_TRY(cudaEventRecord(c->e2e_ev[0], c->stream));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->e2e_ev[0], 0));
+            EMIX_CUDA_TRY(cudaMemcpyAsync(c->e2e_phi, c->phi, (size_t)c->n * sizeof(double),
+                                          cudaMemcpyDeviceToHost, c->side));
+            c->e2e_phi = nullptr;
+        }
     }
     if (fork && !joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
     c->launches = launches;
@@ -395,10 +431,6 @@ void drop_graph(emix_ctx *c) {
     c->graph = nullptr;
     c->fgexec = nullptr;
     c->fgraph = nullptr;
-}
-
-bool filter_due(const emix_ctx *c) {
-    return c->p.filter_every > 0 && c->step_index % c->p.filter_every == 0;
 }
 
 int issue_filter(emix_ctx *c) {
@@ -555,6 +587,9 @@ int emix_ctx_destroy(emix_ctx *c) {
     for (int k = 0; k < 3; ++k) {
         if (c->fork_ev[k]) cudaEventDestroy(c->fork_ev[k]);
         if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+    }
+    for (cudaEvent_t e : c->e2e_ev) {
+        if (e) cudaEventDestroy(e);
     }
     if (c->side) cudaStreamDestroy(c->side);
     cudaFree(c->arena);
@@ -728,12 +763,44 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     if (c->p.level_set)
         EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    int rc = emix_step(c, nsteps, 1);
+    // the last step is issued here, with the copies back overlapping its tail
+    // (needs the side stream, not in use by the level-set overlap)
+    bool tail = nsteps > 0 && c->side && !c->overlap;
+    for (cudaEvent_t &e : c->e2e_ev)
+        if (tail && !e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            e = nullptr;
+            tail = false;
+        }
+    int rc = emix_step(c, tail ? nsteps - 1 : nsteps, 1);
     if (rc) return rc;
-    EMIX_CUDA_TRY(cudaMemcpyAsync(um, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    if (c->p.level_set)
+    bool um_back = false, phi_back = false;
+    if (tail) {
+        // the side stream must not start a copy before the uploads above and
+        // the earlier steps: it waits on the context stream wherever it copies
+        c->e2e_um = um;
+        c->e2e_phi = c->p.level_set ? phi : nullptr;
+        c->e2e_um_done = false;
+        rc = issue_step(c);
+        um_back = c->e2e_um_done;
+        phi_back = c->p.level_set && !c->e2e_phi;
+        c->e2e_um = nullptr;
+        c->e2e_phi = nullptr;
+        c->e2e_um_done = false;
+        if (!rc && filter_due(c)) rc = c->fgexec ? (cudaGraphLaunch(c->fgexec, c->stream) == cudaSuccess ? EMIX_OK : EMIX_ERR_CUDA)
+                                                 : issue_filter(c);
+        if (rc) {
+            cudaStreamSynchronize(c->side);
+            return rc;
+        }
+        ++c->step_index;
+    }
+    if (!um_back)
+        EMIX_CUDA_TRY(cudaMemcpyAsync(um, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (c->p.level_set && !phi_back)
         EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (tail) EMIX_CUDA_TRY(cudaStreamSynchronize(c->side));
     return EMIX_OK;
 }
 

@@ -1,0 +1,82 @@
+"""emix_step_host, the host-buffer entry point (the one the end-to-end figure
+times): the same values as the device-resident steps, bit for bit.  Its last
+step copies phi back after the last level-set stage and um by z-slabs of the
+last RK update, on a second stream, while the step still runs; the cases
+below also cover the forms where it copies after the step instead (the
+level-set overlap on, a filter step last, the impeller's blade-edge
+interpolation after the RK update, no level set) and pageable host buffers."""
+import numpy as np
+import pytest
+
+from emix_gb300 import fields as F
+
+pytestmark = pytest.mark.gpu
+
+
+def _tank(interp=0):
+    w = F.stirred_tank(n=24, impeller=True, impeller_omega=1.3)
+    w.impeller.interp = interp
+    return w
+
+
+def _device(w, nsteps, **kw):
+    from emix_gb300 import ops
+    ctx = ops.Context(w, **kw)
+    ctx.step(nsteps, use_graph=True)
+    um, phi = ctx.download()
+    idx = ctx.step_index
+    ctx.close()
+    return um, phi, idx
+
+
+def _host(w, nsteps, pinned=True, overlap=False, level_set=True, **kw):
+    import torch
+    from emix_gb300 import ops
+    ctx = ops.Context(w, level_set=level_set, **kw)
+    if overlap:
+        ctx.set_overlap(True)
+    um_t = torch.from_numpy(np.ascontiguousarray(w.um))
+    phi_t = torch.from_numpy(np.ascontiguousarray(w.phi))
+    if pinned:
+        um_t, phi_t = um_t.pin_memory(), phi_t.pin_memory()
+    else:
+        um_t, phi_t = um_t.clone(), phi_t.clone()
+    um, phi = um_t.numpy(), phi_t.numpy()
+    ctx.step_host(um, phi if level_set else None, nsteps)
+    idx = ctx.step_index
+    ctx.close()
+    return um.copy(), (phi.copy() if level_set else None), idx
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_matches_device_steps(nsteps, pinned):
+    w = _tank()
+    um, phi, idx = _device(w, nsteps, bc_walls=1)
+    hum, hphi, hidx = _host(w, nsteps, pinned=pinned, bc_walls=1)
+    assert hidx == idx == nsteps
+    assert np.array_equal(hum, um)
+    assert np.array_equal(hphi, phi)
+
+
+@pytest.mark.parametrize("case", ["overlap", "filter_last", "interp", "no_level_set"])
+def test_step_host_forms_without_the_tail_copies(case):
+    kw = {"bc_walls": 1}
+    w = _tank(interp=1 if case == "interp" else 0)
+    nsteps = 3 if case == "filter_last" else 2
+    if case == "filter_last":
+        kw.update(filter_every=2, cfilt=0.2)   # steps 0 and 2 filter: the last one does
+    ls = case != "no_level_set"
+    um, phi, idx = _device(w, nsteps, level_set=ls, **kw)
+    hum, hphi, hidx = _host(w, nsteps, overlap=case == "overlap", level_set=ls, **kw)
+    assert hidx == idx == nsteps
+    assert np.array_equal(hum, um)
+    if ls:
+        assert np.array_equal(hphi, phi)
+
+
+def test_step_host_zero_steps_returns_the_inputs():
+    w = _tank()
+    hum, hphi, idx = _host(w, 0, bc_walls=1)
+    assert idx == 0
+    assert np.array_equal(hum, w.um) and np.array_equal(hphi, w.phi)
