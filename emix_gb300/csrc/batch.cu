@@ -104,23 +104,57 @@ k_batch_deriv_x(const DerivArgs *__restrict__ args, const long *__restrict__ sta
     }
 }
 
+// item vb of a y/z pencil position
+template <int EPI>
+EMIX_DEV void batch_yz_item(const DerivArgs *__restrict__ args, const long *__restrict__ start,
+                            const Shape *__restrict__ shape, int ngrid, long vb) {
+    const int g = find_grid(start, ngrid, vb);
+    const long local = vb - start[g];
+    const Shape sh = shape[g];
+    const DerivArgs &a = args[g];
+    const uint3 bid = make_uint3((unsigned)(local % sh.gx), (unsigned)((local / sh.gx) % sh.gy),
+                                 (unsigned)(local / ((long)sh.gx * sh.gy)));
+    const int nx = a.nx;
+    const int nother = a.axis == 1 ? a.nz : a.ny;
+    const long s = a.axis == 1 ? (long)nx : (long)nx * a.ny;
+    const long os = a.axis == 1 ? (long)nx * a.ny : (long)nx;
+    deriv_yz_body<EPI>(a.T, a.F, nx, nother, s, os, bid, threadIdx.x, blockDim.x);
+}
+
 template <int EPI>
 __global__ void __launch_bounds__(128)
 k_batch_deriv_yz(const DerivArgs *__restrict__ args, const long *__restrict__ start,
                  const Shape *__restrict__ shape, int ngrid) {
     const long total = start[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) batch_yz_item<EPI>(args, start, shape, ngrid, vb);
+}
+
+// two y/z positions (the gradients' y and z) over one work list
+__global__ void __launch_bounds__(128)
+k_batch_deriv_yz_pair(const DerivArgs *__restrict__ aa, const long *__restrict__ sa,
+                      const Shape *__restrict__ ha, const DerivArgs *__restrict__ ab,
+                      const long *__restrict__ sb, const Shape *__restrict__ hb, int ngrid) {
+    const long ta = sa[ngrid], total = ta + sb[ngrid];
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        if (vb < ta) batch_yz_item<EPI_STORE>(aa, sa, ha, ngrid, vb);
+        else batch_yz_item<EPI_STORE>(ab, sb, hb, ngrid, vb - ta);
+    }
+}
+
+// Smagorinsky and the fluxes of a cell from one set of strain pieces, over
+// the fluxes' work list (the same cells as the Smagorinsky position's)
+__global__ void __launch_bounds__(256, 2)
+k_batch_smag_flux(const SmagArgs *__restrict__ sargs, const FluxArgs *__restrict__ fargs,
+                  const long *__restrict__ start, int ngrid, int cpb) {
+    const long total = start[ngrid];
     for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
         const int g = find_grid(start, ngrid, vb);
-        const long local = vb - start[g];
-        const Shape sh = shape[g];
-        const DerivArgs &a = args[g];
-        const uint3 bid = make_uint3((unsigned)(local % sh.gx), (unsigned)((local / sh.gx) % sh.gy),
-                                     (unsigned)(local / ((long)sh.gx * sh.gy)));
-        const int nx = a.nx;
-        const int nother = a.axis == 1 ? a.nz : a.ny;
-        const long s = a.axis == 1 ? (long)nx : (long)nx * a.ny;
-        const long os = a.axis == 1 ? (long)nx * a.ny : (long)nx;
-        deriv_yz_body<EPI>(a.T, a.F, nx, nother, s, os, bid, threadIdx.x, blockDim.x);
+        const FluxArgs &f = fargs[g];
+        const long q0 = (vb - start[g]) * 256L * cpb + threadIdx.x;
+        for (int k = 0; k < cpb; ++k) {
+            const long q = q0 + 256L * k;
+            if (q < f.n) smag_flux_cell(sargs[g], f, q);
+        }
     }
 }
 
@@ -135,6 +169,7 @@ struct BatchTune {
 
 struct BatchPos {
     int kind, cls, epi;
+    int fuse;          // runs with the next position as one launch (plan_fuse_next, every grid)
     void *args;        // device array of ngrid argument structs
     long *start;       // device prefix sums of virtual blocks, ngrid + 1
     Shape *shape;      // device per-grid virtual launch shapes
@@ -302,6 +337,9 @@ int build(emix_batch *b) {
         P.start = reinterpret_cast<long *>(base + off_start[k]);
         P.shape = reinterpret_cast<Shape *>(base + off_shape[k]);
         P.total = totals[k];
+        P.fuse = plan_fuse_next(*plans[0], k);
+        for (int g = 1; g < G && P.fuse; ++g)
+            if (plan_fuse_next(*plans[g], k) != P.fuse) P.fuse = 0;
     }
     b->built = true;
     return EMIX_OK;
@@ -328,7 +366,21 @@ int ctas(const emix_batch *b, long total) {
 int issue(emix_batch *b) {
     const int G = (int)b->grids.size();
     cudaStream_t st = b->stream;
-    for (const BatchPos &P : b->pos) {
+    const size_t npos = b->pos.size();
+    for (size_t k = 0; k < npos; ++k) {
+        const BatchPos &P = b->pos[k];
+        if (P.fuse && k + 1 < npos) {
+            const BatchPos &Q = b->pos[k + 1];
+            if (P.fuse == 1)
+                k_batch_deriv_yz_pair<<<all_items(P.total + Q.total), b->tune.yz_bs, 0, st>>>(
+                    (const DerivArgs *)P.args, P.start, P.shape, (const DerivArgs *)Q.args, Q.start, Q.shape, G);
+            else
+                k_batch_smag_flux<<<ctas(b, Q.total), 256, 0, st>>>((const SmagArgs *)P.args,
+                                                                   (const FluxArgs *)Q.args, Q.start, G,
+                                                                   b->tune.cpb);
+            ++k;
+            continue;
+        }
         const int nb = ctas(b, P.total);
         switch (P.kind) {
         case LK_PRIM: k_batch_cells<PrimOp><<<nb, 256, 0, st>>>((const PrimArgs *)P.args, P.start, G, b->tune.cpb); break;

@@ -13,6 +13,8 @@
 #include "pointwise.cuh"
 #include "weno.cuh"
 
+#include <vector>
+
 namespace emix {
 
 enum LaunchKind {
@@ -55,6 +57,10 @@ struct Launch {
 };
 
 int launch_single(const Launch &L, cudaStream_t st);
+
+// records k and k+1 of a plan that run as one launch (step.cu): 1 the
+// gradients' y and z records, 2 Smagorinsky and the fluxes; 0 none
+int plan_fuse_next(const std::vector<Launch> &P, size_t k);
 
 // compact filter (filter.cu): filtrado on um[5] in place; the tables are
 // prepared on the host before any stream capture

@@ -293,11 +293,14 @@ bool filter_due(const emix_ctx *c) {
     return c->p.filter_every > 0 && c->step_index % c->p.filter_every == 0;
 }
 
-// Records k and k+1 of a single-grid plan that run as one launch: the
-// gradients' y and z records (1), Smagorinsky and the fluxes that read its
-// viscosity (2); 0 otherwise.  The records stay separate in the plan: the
-// batched step and the adjoint's taped step run them one by one.
-int fused_with_next(const std::vector<Launch> &P, size_t k) {
+} // namespace
+
+namespace emix {
+// Records k and k+1 of a plan that run as one launch: the gradients' y and z
+// records (1), Smagorinsky and the fluxes that read its viscosity (2); 0
+// otherwise.  The records stay separate in the plan (the adjoint's taped step
+// runs them one by one).
+int plan_fuse_next(const std::vector<Launch> &P, size_t k) {
     if (k + 1 >= P.size()) return 0;
     const Launch &L = P[k], &M = P[k + 1];
     if (L.kind == LK_DERIV_YZ && L.deriv.pair && M.kind == LK_DERIV_YZ && L.deriv.epi == EPI_STORE &&
@@ -308,6 +311,11 @@ int fused_with_next(const std::vector<Launch> &P, size_t k) {
         return 2;
     return 0;
 }
+} // namespace emix
+
+namespace {
+
+int fused_with_next(const std::vector<Launch> &P, size_t k) { return plan_fuse_next(P, k); }
 
 int issue_step(emix_ctx *c) {
     const bool fork = c->overlap && c->side && !c->prof;
