@@ -400,10 +400,14 @@ int emix_ctx_set_time(emix_ctx *ctx, double t0);
 int emix_ctx_get_time(emix_ctx *ctx, double *t);
 
 /* End-to-end form: copy um/phi from host, advance nsteps, copy back;
- * synchronous. */
+ * synchronous.  The copies back overlap the last step where its results are
+ * final early (phi after the last level-set stage, um by z-slabs of the last
+ * RK update, on a second stream); page-locked host buffers let them run
+ * asynchronously.  The values are those of emix_step, bit for bit. */
 int emix_step_host(emix_ctx *ctx, double *um, double *phi, int nsteps);
 
-/* Number of kernel launches one step issues (for accounting). */
+/* Number of kernel launches one step issues (for accounting; the records
+ * that run as one launch counted once). */
 int emix_ctx_launches_per_step(emix_ctx *ctx);
 
 /* Bytes of device memory the context holds. */
