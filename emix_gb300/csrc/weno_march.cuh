@@ -34,9 +34,11 @@ constexpr int kPR = (kPN + kNT - 1) / kNT;     // tile values each thread loads
 // r change sign, the smoothness terms do not, so the sign goes to the
 // denominator (the right-biased stencil reads its second differences in
 // reverse order with this sign, and needs no negations).
-EMIX_DEV double weno5a(double v3, double a1, double a2, double a3, double a4, double eps4, double c12) {
+// The same with the third differences d1 = a2 - a1, d2 = a3 - a2, d3 = a4 - a3
+// given (from the stage's third-difference tiles): a1 and a4 are not needed.
+EMIX_DEV double weno5d(double v3, double a2, double a3, double d1, double d2, double d3, double eps4,
+                       double c12) {
     constexpr double c13 = 13.0 / 3.0;
-    const double d1 = a2 - a1, d2 = a3 - a2, d3 = a4 - a3;
     const double e1 = fma(2.0, a2, d1);
     const double e2 = -(a2 + a3);
     const double e3 = fma(-2.0, a3, d3);
@@ -52,6 +54,10 @@ EMIX_DEV double weno5a(double v3, double a1, double a2, double a3, double a4, do
     const double num = fma(w1, r1, fma(w2, r2, w3 * r3));
     const double den = c12 * (w1 + w2 + w3);
     return fma(num, rcp_newton(den), v3);
+}
+
+EMIX_DEV double weno5a(double v3, double a1, double a2, double a3, double a4, double eps4, double c12) {
+    return weno5d(v3, a2, a3, a2 - a1, a3 - a2, a4 - a3, eps4, c12);
 }
 
 // z direction of a plane near the z faces: the five differences at the edge
@@ -144,6 +150,8 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
     __shared__ double Ax[kMY][kMX + 4];      // positions x0-1 .. x0+kMX+2
     __shared__ double Dy[kMY + 5][kMX];      // rows y0-2 .. y0+kMY+2
     __shared__ double Ay[kMY + 4][kMX];      // rows y0-1 .. y0+kMY+2
+    __shared__ double Tx[kMY][kMX + 3];      // T(p) = A(p) - A(p-1), positions x0 .. x0+kMX+2
+    __shared__ double Ty[kMY + 3][kMX];      // rows y0 .. y0+kMY+2
 
     const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
     const long sxy = (long)nxg * nyg;
@@ -169,8 +177,9 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
 
     // z window of this column: phi(z), 0 outside the grid
     auto ld = [&](int z) { return (active && z >= 0 && z < nzg) ? phi[col + sxy * z] : 0.0; };
-    // Dz[t] = D(Z - 2 + t), t = 0..5; Az[t] = A(Z - 1 + t), t = 0..4; fz = phi(Z + 3)
-    double Dz[6], Az[5], fz;
+    // Dz[t] = D(Z - 2 + t), t = 0..5; Az[t] = A(Z - 1 + t), t = 0..4;
+    // Tz[t] = T(Z + t) = A(Z + t) - A(Z + t - 1), t = 0..3; fz = phi(Z + 3)
+    double Dz[6], Az[5], Tz[4], fz;
     {
         double f[7];
 #pragma unroll
@@ -179,6 +188,8 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
         for (int t = 0; t < 6; ++t) Dz[t] = (zs - 2 + t == 0) ? ld(1) - ld(0) : f[t + 1] - f[t];
 #pragma unroll
         for (int t = 0; t < 5; ++t) Az[t] = Dz[t + 1] - Dz[t];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) Tz[t] = Az[t + 1] - Az[t];
         fz = f[6];
     }
 
@@ -268,6 +279,16 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
             Ay[j][i] = Dy[j + 1][i] - Dy[j][i];
         }
         __syncthreads();
+        // third differences, once per position instead of three per evaluation
+        for (int t = tid; t < kMY * (kMX + 3); t += kNT) {
+            const int i = t % (kMX + 3), j = t / (kMX + 3);
+            Tx[j][i] = Ax[j][i + 1] - Ax[j][i];
+        }
+        for (int t = tid; t < (kMY + 3) * kMX; t += kNT) {
+            const int i = t % kMX, j = t / kMX;
+            Ty[j][i] = Ay[j + 1][i] - Ay[j][i];
+        }
+        __syncthreads();
 
         if (active) {
             const long id = col + sxy * Z;
@@ -290,30 +311,42 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
                     ex = kWenoEps4 / (jd * jd);
                 }
                 const bool left = __double_as_longlong(u) >= 0;
-                // the five differences as v3 and the second differences a1..a4;
-                // the upwind side is chosen by selects (no divergent WENO5)
+                // the five differences as v3, the second differences a2, a3
+                // and the third differences d1..d3; the upwind side is chosen
+                // by selects (no divergent WENO5)
                 double v3, a1, a2, a3, a4, c12 = left ? 12.0 : -12.0;
+                // right side: its second differences are A(c+3..c) negated
+                // (the sign goes to c12), so its third differences are
+                // -T(c+3), -T(c+2), -T(c+1): the sign by the bit pattern
+                const long long flip = left ? 0LL : (long long)0x8000000000000000ULL;
+                auto neg = [&](double x) { return __longlong_as_double(__double_as_longlong(x) ^ flip); };
+                bool tiled = true;
+                double d1, d2, d3;
                 if ((d == 0 && !wedge_x) || (d == 1 && !wedge_y)) {
-                    // left: v3 = D(c), a = A(c-1..c+2); right: v3 = D(c+1),
-                    // a = -A(c+3..c), given as A(c+3..c) with the sign in c12
-                    // -- tile index of D(c) is t + 2, of A(c) t + 1
-                    const int o = left ? 0 : 4, st = left ? 1 : -1, ov = left ? 2 : 3;
+                    // left: v3 = D(c), a2, a3 = A(c), A(c+1), d = T(c..c+2);
+                    // right: v3 = D(c+1), a2, a3 = A(c+2), A(c+1), d = -T(c+3..c+1)
+                    // -- tile index of D(c) is t + 2, of A(c) t + 1, of T(c) t
+                    const int ov = left ? 2 : 3, oa = left ? 1 : 3, sa = left ? 1 : -1;
+                    const int ot = left ? 0 : 3, st = left ? 1 : -1;
                     if (d == 0) {
-                        const double *ar = &Ax[ty][tx];
                         v3 = Dx[ty][tx + ov];
-                        a1 = ar[o]; a2 = ar[o + st]; a3 = ar[o + 2 * st]; a4 = ar[o + 3 * st];
+                        a2 = Ax[ty][tx + oa]; a3 = Ax[ty][tx + oa + sa];
+                        d1 = Tx[ty][tx + ot]; d2 = Tx[ty][tx + ot + st]; d3 = Tx[ty][tx + ot + 2 * st];
                     } else {
                         v3 = Dy[ty + ov][tx];
-                        a1 = Ay[ty + o][tx]; a2 = Ay[ty + o + st][tx]; a3 = Ay[ty + o + 2 * st][tx];
-                        a4 = Ay[ty + o + 3 * st][tx];
+                        a2 = Ay[ty + oa][tx]; a3 = Ay[ty + oa + sa][tx];
+                        d1 = Ty[ty + ot][tx]; d2 = Ty[ty + ot + st][tx]; d3 = Ty[ty + ot + 2 * st][tx];
                     }
+                    d1 = neg(d1); d2 = neg(d2); d3 = neg(d3);
                 } else if (d == 2 && Z >= 2 && Z <= nzg - 4) {
                     v3 = left ? Dz[2] : Dz[3];
-                    a1 = left ? Az[0] : Az[4];
                     a2 = left ? Az[1] : Az[3];
                     a3 = Az[2];
-                    a4 = left ? Az[3] : Az[1];
+                    d1 = neg(left ? Tz[0] : Tz[3]);
+                    d2 = neg(left ? Tz[1] : Tz[2]);
+                    d3 = neg(left ? Tz[2] : Tz[1]);
                 } else {
+                    tiled = false;
                     // edge rules: the differences at the rule's positions
                     double v[5];
                     if (d == 2) {
@@ -333,7 +366,8 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
                     a1 = v[1] - v[0]; a2 = v[2] - v[1]; a3 = v[3] - v[2]; a4 = v[4] - v[3];
                     c12 = 12.0;
                 }
-                const double W = weno5a(v3, a1, a2, a3, a4, ex, c12);
+                const double W = tiled ? weno5d(v3, a2, a3, d1, d2, d3, ex, c12)
+                                       : weno5a(v3, a1, a2, a3, a4, ex, c12);
                 rs = fma(u, mx * W, rs);
             }
             // TVD-RK3 stage (extrapol.cu:155-212)
@@ -361,6 +395,9 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
 #pragma unroll
         for (int t = 0; t < 4; ++t) Az[t] = Az[t + 1];
         Az[4] = Dz[5] - Dz[4];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) Tz[t] = Tz[t + 1];
+        Tz[3] = Az[4] - Az[3];
         __syncthreads();
     }
     if constexpr (TMA) {
