@@ -60,6 +60,35 @@ EMIX_DEV double weno5a(double v3, double a1, double a2, double a3, double a4, do
     return weno5d(v3, a2, a3, a2 - a1, a3 - a2, a4 - a3, eps4, c12);
 }
 
+// sqrt(13/3), correctly rounded
+constexpr double kSqrt13_3 = 2.0816659994661326;
+
+// The same from the four second differences and the third differences scaled
+// by sqrt(13/3), s_k = sqrt(13/3) d_k (from the stage's scaled tiles), so that
+// the smoothness term c13 d_k^2 + e_k^2 is one FMA: with e1 = 3 a2 - a1,
+// e2 = -(a2 + a3), e3 = a4 - 3 a3 and the candidates halved, r_k / 2 =
+// 2 e1 - a2, a3 - e2, a3 - e3, the halving carried by c6 = c12 / 2.  The
+// sign of s_k does not matter (it enters squared), so the right-biased side
+// reads the tile's values as they are.
+EMIX_DEV double weno5s(double v3, double a1, double a2, double a3, double a4, double s1, double s2,
+                       double s3, double eps4, double c6) {
+    const double e1 = fma(3.0, a2, -a1);
+    const double e2 = -(a2 + a3);
+    const double e3 = fma(-3.0, a3, a4);
+    double t1 = fma(s1, s1, fma(e1, e1, eps4)); t1 *= t1;
+    double t2 = fma(s2, s2, fma(e2, e2, eps4)); t2 *= t2;
+    double t3 = fma(s3, s3, fma(e3, e3, eps4)); t3 *= t3;
+    const double w1 = t2 * t3;
+    const double w2 = (6.0 * t1) * t3;
+    const double w3 = (3.0 * t1) * t2;
+    const double r1 = fma(2.0, e1, -a2);
+    const double r2 = a3 - e2;
+    const double r3 = a3 - e3;
+    const double num = fma(w1, r1, fma(w2, r2, w3 * r3));
+    const double den = c6 * (w1 + w2 + w3);
+    return fma(num, rcp_newton(den), v3);
+}
+
 // z direction of a plane near the z faces: the five differences at the edge
 // rule's positions, read from global memory
 EMIX_DEV void weno_z_general(const double *phi, long id, int Z, int nzg, bool left, bool ztop_bug, long nxg,
@@ -150,7 +179,8 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
     __shared__ double Ax[kMY][kMX + 4];      // positions x0-1 .. x0+kMX+2
     __shared__ double Dy[kMY + 5][kMX];      // rows y0-2 .. y0+kMY+2
     __shared__ double Ay[kMY + 4][kMX];      // rows y0-1 .. y0+kMY+2
-    __shared__ double Tx[kMY][kMX + 3];      // T(p) = A(p) - A(p-1), positions x0 .. x0+kMX+2
+    // scaled third differences S(p) = sqrt(13/3) (A(p) - A(p-1))
+    __shared__ double Tx[kMY][kMX + 3];      // positions x0 .. x0+kMX+2
     __shared__ double Ty[kMY + 3][kMX];      // rows y0 .. y0+kMY+2
 
     const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
@@ -178,7 +208,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
     // z window of this column: phi(z), 0 outside the grid
     auto ld = [&](int z) { return (active && z >= 0 && z < nzg) ? phi[col + sxy * z] : 0.0; };
     // Dz[t] = D(Z - 2 + t), t = 0..5; Az[t] = A(Z - 1 + t), t = 0..4;
-    // Tz[t] = T(Z + t) = A(Z + t) - A(Z + t - 1), t = 0..3; fz = phi(Z + 3)
+    // Tz[t] = S(Z + t) = sqrt(13/3) (A(Z + t) - A(Z + t - 1)), t = 0..3; fz = phi(Z + 3)
     double Dz[6], Az[5], Tz[4], fz;
     {
         double f[7];
@@ -189,7 +219,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
 #pragma unroll
         for (int t = 0; t < 5; ++t) Az[t] = Dz[t + 1] - Dz[t];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) Tz[t] = Az[t + 1] - Az[t];
+        for (int t = 0; t < 4; ++t) Tz[t] = kSqrt13_3 * (Az[t + 1] - Az[t]);
         fz = f[6];
     }
 
@@ -279,14 +309,15 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
             Ay[j][i] = Dy[j + 1][i] - Dy[j][i];
         }
         __syncthreads();
-        // third differences, once per position instead of three per evaluation
+        // scaled third differences, once per position instead of three
+        // differences and three products per evaluation
         for (int t = tid; t < kMY * (kMX + 3); t += kNT) {
             const int i = t % (kMX + 3), j = t / (kMX + 3);
-            Tx[j][i] = Ax[j][i + 1] - Ax[j][i];
+            Tx[j][i] = kSqrt13_3 * (Ax[j][i + 1] - Ax[j][i]);
         }
         for (int t = tid; t < (kMY + 3) * kMX; t += kNT) {
             const int i = t % kMX, j = t / kMX;
-            Ty[j][i] = Ay[j + 1][i] - Ay[j][i];
+            Ty[j][i] = kSqrt13_3 * (Ay[j + 1][i] - Ay[j][i]);
         }
         __syncthreads();
 
@@ -311,40 +342,39 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
                     ex = kWenoEps4 / (jd * jd);
                 }
                 const bool left = __double_as_longlong(u) >= 0;
-                // the five differences as v3, the second differences a2, a3
-                // and the third differences d1..d3; the upwind side is chosen
-                // by selects (no divergent WENO5)
+                // the five differences as v3, the second differences a1..a4
+                // and the scaled third differences s1..s3; the upwind side is
+                // chosen by selects (no divergent WENO5)
                 double v3, a1, a2, a3, a4, c12 = left ? 12.0 : -12.0;
-                // right side: its second differences are A(c+3..c) negated
-                // (the sign goes to c12), so its third differences are
-                // -T(c+3), -T(c+2), -T(c+1): the sign by the bit pattern
-                const long long flip = left ? 0LL : (long long)0x8000000000000000ULL;
-                auto neg = [&](double x) { return __longlong_as_double(__double_as_longlong(x) ^ flip); };
                 bool tiled = true;
-                double d1, d2, d3;
+                double s1, s2, s3;
                 if ((d == 0 && !wedge_x) || (d == 1 && !wedge_y)) {
-                    // left: v3 = D(c), a2, a3 = A(c), A(c+1), d = T(c..c+2);
-                    // right: v3 = D(c+1), a2, a3 = A(c+2), A(c+1), d = -T(c+3..c+1)
-                    // -- tile index of D(c) is t + 2, of A(c) t + 1, of T(c) t
-                    const int ov = left ? 2 : 3, oa = left ? 1 : 3, sa = left ? 1 : -1;
-                    const int ot = left ? 0 : 3, st = left ? 1 : -1;
+                    // left: v3 = D(c), a = A(c-1..c+2), s = S(c..c+2); right:
+                    // v3 = D(c+1), a = -A(c+3..c), given as A(c+3..c) with the
+                    // sign in c12, s = S(c+3..c+1) -- tile index of D(c) is
+                    // t + 2, of A(c) t + 1, of S(c) t
+                    const int o = left ? 0 : 4, st = left ? 1 : -1, ov = left ? 2 : 3, os = left ? 0 : 3;
                     if (d == 0) {
+                        const double *ar = &Ax[ty][tx];
+                        const double *sr = &Tx[ty][tx];
                         v3 = Dx[ty][tx + ov];
-                        a2 = Ax[ty][tx + oa]; a3 = Ax[ty][tx + oa + sa];
-                        d1 = Tx[ty][tx + ot]; d2 = Tx[ty][tx + ot + st]; d3 = Tx[ty][tx + ot + 2 * st];
+                        a1 = ar[o]; a2 = ar[o + st]; a3 = ar[o + 2 * st]; a4 = ar[o + 3 * st];
+                        s1 = sr[os]; s2 = sr[os + st]; s3 = sr[os + 2 * st];
                     } else {
                         v3 = Dy[ty + ov][tx];
-                        a2 = Ay[ty + oa][tx]; a3 = Ay[ty + oa + sa][tx];
-                        d1 = Ty[ty + ot][tx]; d2 = Ty[ty + ot + st][tx]; d3 = Ty[ty + ot + 2 * st][tx];
+                        a1 = Ay[ty + o][tx]; a2 = Ay[ty + o + st][tx]; a3 = Ay[ty + o + 2 * st][tx];
+                        a4 = Ay[ty + o + 3 * st][tx];
+                        s1 = Ty[ty + os][tx]; s2 = Ty[ty + os + st][tx]; s3 = Ty[ty + os + 2 * st][tx];
                     }
-                    d1 = neg(d1); d2 = neg(d2); d3 = neg(d3);
                 } else if (d == 2 && Z >= 2 && Z <= nzg - 4) {
                     v3 = left ? Dz[2] : Dz[3];
+                    a1 = left ? Az[0] : Az[4];
                     a2 = left ? Az[1] : Az[3];
                     a3 = Az[2];
-                    d1 = neg(left ? Tz[0] : Tz[3]);
-                    d2 = neg(left ? Tz[1] : Tz[2]);
-                    d3 = neg(left ? Tz[2] : Tz[1]);
+                    a4 = left ? Az[3] : Az[1];
+                    s1 = left ? Tz[0] : Tz[3];
+                    s2 = left ? Tz[1] : Tz[2];
+                    s3 = left ? Tz[2] : Tz[1];
                 } else {
                     tiled = false;
                     // edge rules: the differences at the rule's positions
@@ -366,7 +396,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
                     a1 = v[1] - v[0]; a2 = v[2] - v[1]; a3 = v[3] - v[2]; a4 = v[4] - v[3];
                     c12 = 12.0;
                 }
-                const double W = tiled ? weno5d(v3, a2, a3, d1, d2, d3, ex, c12)
+                const double W = tiled ? weno5s(v3, a1, a2, a3, a4, s1, s2, s3, ex, left ? 6.0 : -6.0)
                                        : weno5a(v3, a1, a2, a3, a4, ex, c12);
                 rs = fma(u, mx * W, rs);
             }
@@ -397,7 +427,7 @@ EMIX_DEV void weno_march_body_t(const WenoArgs &a, int bx, int by, int bz, int g
         Az[4] = Dz[5] - Dz[4];
 #pragma unroll
         for (int t = 0; t < 3; ++t) Tz[t] = Tz[t + 1];
-        Tz[3] = Az[4] - Az[3];
+        Tz[3] = kSqrt13_3 * (Az[4] - Az[3]);
         __syncthreads();
     }
     if constexpr (TMA) {
