@@ -51,10 +51,13 @@ struct emix_ctx {
     CUtensorMap weno_tmap[3];
     // emix_step_host's last step: the copies of phi and um back to the host
     // start on `side` as soon as each part is final (phi after the last
-    // level-set stage, um by z-slabs of the last RK update)
+    // level-set stage, um by z-slabs of the last RK update); with a single
+    // step, phi's upload runs on `side` under the first substep's flow
+    // kernels (e2e_defer).  Events: [0] phi final, [1..kE2eSlabs] um slabs,
+    // [kE2eSlabs + 1] phi uploaded
     static constexpr int kE2eSlabs = 4;
     double *e2e_um = nullptr, *e2e_phi = nullptr;
-    bool e2e_um_done = false;
+    bool e2e_um_done = false, e2e_defer = false;
     cudaEvent_t e2e_ev[kE2eSlabs + 2] = {};
 };
 

@@ -323,8 +323,32 @@ int issue_step(emix_ctx *c) {
     bool joined = true;
     const size_t np = c->plan.size();
     int launches = 0;
+    // emix_step_host's single step: the level-set padding and first stage wait
+    // for phi's upload on the side stream, so they go after the first
+    // substep's flow kernels (which read neither phi nor anything they write)
+    // and just before its first RK launch (which overwrites the velocity the
+    // stage reads)
+    bool defer = c->e2e_defer && !fork;
+    size_t held[2];
+    int nheld = 0;
     for (size_t k = 0; k < np; ++k) {
         const Launch &L = c->plan[k];
+        if (defer && (L.kind == LK_PAD || L.kind == LK_WENO) && nheld < 2) {
+            held[nheld++] = k;
+            continue;
+        }
+        if (defer && L.kind == LK_RK) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->e2e_ev[emix_ctx::kE2eSlabs + 1], 0));
+            for (int h = 0; h < nheld; ++h) {
+                const Launch &H = c->plan[held[h]];
+                ProfScope ps(c, H.cls);
+                int rc = launch_single(H, c->stream);
+                if (rc) return rc;
+                ++launches;
+            }
+            nheld = 0;
+            defer = false;
+        }
         const int fuse = fused_with_next(c->plan, k);
         if (fuse == 1) {
             // the gradients' y and z records as one launch
@@ -402,6 +426,15 @@ int issue_step(emix_ctx *c) {
         }
     }
     if (fork && !joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
+    if (nheld) {
+        // no RK record followed (not a plan this library builds): issue them last
+        EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->e2e_ev[emix_ctx::kE2eSlabs + 1], 0));
+        for (int h = 0; h < nheld; ++h) {
+            int rc = launch_single(c->plan[held[h]], c->stream);
+            if (rc) return rc;
+            ++launches;
+        }
+    }
     c->launches = launches;
     return EMIX_OK;
 }
@@ -768,9 +801,6 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
     if (!c || !um || nsteps < 0) return EMIX_ERR_ARG;
     if (c->p.level_set && !phi) return EMIX_ERR_ARG;
     const long n = c->n;
-    EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    if (c->p.level_set)
-        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     // the last step is issued here, with the copies back overlapping its tail
     // (needs the side stream, not in use by the level-set overlap)
     bool tail = nsteps > 0 && c->side && !c->overlap;
@@ -780,6 +810,21 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
             e = nullptr;
             tail = false;
         }
+    cudaEvent_t phi_in = tail ? c->e2e_ev[emix_ctx::kE2eSlabs + 1] : nullptr;
+    EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->p.level_set && phi_in) {
+        // phi on the side stream, after whatever the context stream holds
+        EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->stream));
+        EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, phi_in, 0));
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->side));
+        EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->side));
+        // earlier steps of this call wait for it in full
+        if (nsteps > 1) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, phi_in, 0));
+    } else {
+        if (c->p.level_set)
+            EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        if (phi_in) EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->stream));
+    }
     int rc = emix_step(c, tail ? nsteps - 1 : nsteps, 1);
     if (rc) return rc;
     bool um_back = false, phi_back = false;
@@ -789,12 +834,14 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
         c->e2e_um = um;
         c->e2e_phi = c->p.level_set ? phi : nullptr;
         c->e2e_um_done = false;
+        c->e2e_defer = nsteps == 1 && c->p.level_set;
         rc = issue_step(c);
         um_back = c->e2e_um_done;
         phi_back = c->p.level_set && !c->e2e_phi;
         c->e2e_um = nullptr;
         c->e2e_phi = nullptr;
         c->e2e_um_done = false;
+        c->e2e_defer = false;
         if (!rc && filter_due(c)) rc = c->fgexec ? (cudaGraphLaunch(c->fgexec, c->stream) == cudaSuccess ? EMIX_OK : EMIX_ERR_CUDA)
                                                  : issue_filter(c);
         if (rc) {
