@@ -120,7 +120,9 @@ int taped_step(emix_adj *a) {
     int rc = copy(T.um0, c->um0, 5 * n, st);
     if (rc) return rc;
     int s = 0;
-    for (const Launch &L : c->plan) {
+    const std::vector<Launch> &P = c->plan;
+    for (size_t k = 0; k < P.size(); ++k) {
+        const Launch &L = P[k];
         if (L.kind == LK_WENO) {
             ++s;
             if ((rc = copy(T.u[s - 1], c->u, 3 * n, st))) return rc;
@@ -128,12 +130,30 @@ int taped_step(emix_adj *a) {
             if (s >= 2 && (rc = copy(T.umc[s - 1], c->um, 5 * n, st))) return rc;
             if (T.phig[s - 1] && (rc = copy(T.phig[s - 1], L.weno.phi, c->ng, st))) return rc;
         }
-        if ((rc = launch_single(L, st))) return rc;
+        // the records the step runs as one launch run as one here too (the
+        // same values bit for bit); the tape copies follow the pair
+        const int fuse = plan_fuse_next(P, k);
+        const Launch *last = &L;
+        if (fuse == 1) {
+            const DerivArgs &a = L.deriv, &b = P[k + 1].deriv;
+            const double *in[kMaxFields];
+            double *out[kMaxFields];
+            for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
+            for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
+            if ((rc = launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, st))) return rc;
+            last = &P[++k];
+        } else if (fuse == 2) {
+            k_smag_flux<<<cells_grid(P[k + 1].flux.n), 256, 0, st>>>(L.smag, P[k + 1].flux);
+            EMIX_CUDA_TRY(cudaGetLastError());
+            ++k;
+        } else if ((rc = launch_single(L, st))) {
+            return rc;
+        }
         if (L.kind == LK_CLOCK && T.clock && (rc = copy(T.clock, c->clock, kImpClockLen, st))) return rc;
         if (s >= 1) {
-            if (L.cls == CLS_GRADZ && (rc = copy(T.dvel[s - 1], c->dvel, 9 * n, st))) return rc;
+            if (last->cls == CLS_GRADZ && (rc = copy(T.dvel[s - 1], c->dvel, 9 * n, st))) return rc;
             if (L.kind == LK_SMAG && (rc = copy(T.vis[s - 1], c->vis, n, st))) return rc;
-            if (L.cls == CLS_DIVZ && (rc = copy(T.R[s - 1], c->R, 5 * n, st))) return rc;
+            if (last->cls == CLS_DIVZ && (rc = copy(T.R[s - 1], c->R, 5 * n, st))) return rc;
         }
     }
     return s == 3 ? EMIX_OK : EMIX_ERR_ARG;

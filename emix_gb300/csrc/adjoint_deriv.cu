@@ -84,7 +84,10 @@ __global__ void __launch_bounds__(128) k_deriv_t(DerivTTable T, PencilFields F, 
     if (fast) {
         for (; i + 3 >= jbot; --i) {
             advance(i);
-            put(i + 3, fma(T.ta, zq[2] - zq[4], T.tb * (zq[1] - zq[5])));
+            // accumulated: the add folds into the stencil's second FMA
+            const long js = (long)(i + 3) * s;
+            if (ACC) out[js] = fma(T.ta, zq[2] - zq[4], fma(T.tb, zq[1] - zq[5], out[js]));
+            else out[js] = fma(T.ta, zq[2] - zq[4], T.tb * (zq[1] - zq[5]));
         }
     }
     for (; i >= -3; --i) {
