@@ -298,8 +298,9 @@ bool filter_due(const emix_ctx *c) {
 namespace emix {
 // Records k and k+1 of a plan that run as one launch: the gradients' y and z
 // records (1), Smagorinsky and the fluxes that read its viscosity (2); 0
-// otherwise.  The records stay separate in the plan (the adjoint's taped step
-// runs them one by one).
+// otherwise.  The records stay separate in the plan: the fused kernels run
+// the same per-cell functions (the same values bit for bit), and the records
+// keep each operator's arguments for the adjoint's reverse sweep.
 int plan_fuse_next(const std::vector<Launch> &P, size_t k) {
     if (k + 1 >= P.size()) return 0;
     const Launch &L = P[k], &M = P[k + 1];
