@@ -120,6 +120,7 @@ PROTOTYPES = {
     "emix_ctx_state": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "emix_step": (C.c_int, [vp, C.c_int, C.c_int]),
     "emix_ctx_set_overlap": (C.c_int, [vp, C.c_int]),
+    "emix_ctx_set_fusion": (C.c_int, [vp, C.c_int]),
     "emix_ctx_set_tma": (C.c_int, [vp, C.c_int]),
     "emix_ctx_tma_stages": (C.c_int, [vp]),
     "emix_weno_tma_timeouts": (C.c_int, [C.POINTER(C.c_int)]),

@@ -132,7 +132,7 @@ int taped_step(emix_adj *a) {
         }
         // the records the step runs as one launch run as one here too (the
         // same values bit for bit); the tape copies follow the pair
-        const int fuse = plan_fuse_next(P, k);
+        const int fuse = c->fuse ? plan_fuse_next(P, k) : 0;
         const Launch *last = &L;
         if (fuse == 1) {
             const DerivArgs &a = L.deriv, &b = P[k + 1].deriv;

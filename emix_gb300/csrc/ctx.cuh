@@ -45,6 +45,8 @@ struct emix_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
     bool overlap = false;
+    // pairs of records run as one launch (plan_fuse_next; emix_ctx_set_fusion)
+    bool fuse = true;
     // the level-set stages' plane tiles by TMA (emix_ctx_set_tma; on by
     // default where the copy unit's alignment rules hold), one map per stage
     bool tma = true;

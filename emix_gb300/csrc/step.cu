@@ -316,7 +316,7 @@ int plan_fuse_next(const std::vector<Launch> &P, size_t k) {
 
 namespace {
 
-int fused_with_next(const std::vector<Launch> &P, size_t k) { return plan_fuse_next(P, k); }
+int fused_with_next(const emix_ctx *c, size_t k) { return c->fuse ? plan_fuse_next(c->plan, k) : 0; }
 
 int issue_step(emix_ctx *c) {
     const bool fork = c->overlap && c->side && !c->prof;
@@ -350,7 +350,7 @@ int issue_step(emix_ctx *c) {
             nheld = 0;
             defer = false;
         }
-        const int fuse = fused_with_next(c->plan, k);
+        const int fuse = fused_with_next(c, k);
         if (fuse == 1) {
             // the gradients' y and z records as one launch
             const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
@@ -660,6 +660,13 @@ int emix_ctx_set_overlap(emix_ctx *c, int on) {
     return EMIX_OK;
 }
 
+int emix_ctx_set_fusion(emix_ctx *c, int on) {
+    if (!c || (on != 0 && on != 1)) return EMIX_ERR_ARG;
+    c->fuse = on == 1;
+    drop_graph(c);
+    return EMIX_OK;
+}
+
 int emix_ctx_set_stream(emix_ctx *c, void *stream) {
     if (!c) return EMIX_ERR_ARG;
     c->stream = stream ? (cudaStream_t)stream : c->own;
@@ -866,7 +873,7 @@ int emix_ctx_launches_per_step(emix_ctx *c) {
     int k = 0;
     const size_t np = c->plan.size();
     for (size_t q = 0; q < np; ++q) {
-        if (fused_with_next(c->plan, q)) ++q;
+        if (fused_with_next(c, q)) ++q;
         ++k;
     }
     return k;

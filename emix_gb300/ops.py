@@ -445,6 +445,12 @@ class Context:
     def set_overlap(self, on: bool):
         check(self.lib.emix_ctx_set_overlap(self._h, 1 if on else 0), "emix_ctx_set_overlap")
 
+    def set_fusion(self, on: bool):
+        """Run the gradients' y and z passes, and Smagorinsky with the fluxes,
+        as one launch each (default) or every operator alone; the values are
+        bitwise the same."""
+        check(self.lib.emix_ctx_set_fusion(self._h, 1 if on else 0), "emix_ctx_set_fusion")
+
     def set_tma(self, on: bool):
         """Plane tiles of the level-set stages by TMA copies (default) or by
         register-staged loads; the results are bitwise the same."""

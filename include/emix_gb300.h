@@ -351,6 +351,11 @@ int emix_ctx_set_stream(emix_ctx *ctx, void *stream);
  * GB300 both sides are FP64-bound and the overlap gains nothing measurable. */
 int emix_ctx_set_overlap(emix_ctx *ctx, int on);
 
+/* 1 (default): the gradients' y and z passes run as one launch, and so do
+ * the Smagorinsky viscosity and the fluxes; 0: every operator in a launch of
+ * its own.  The values are the same bit for bit (for checks). */
+int emix_ctx_set_fusion(emix_ctx *ctx, int on);
+
 /* 1 (default): the level-set stages bring their phi plane tiles into shared
  * memory with TMA tiled copies (one 3-D tensor map per stage) wherever the
  * copy unit's rules hold (padded x extent even, at least 24 x 22 cells);
