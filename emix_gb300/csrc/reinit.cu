@@ -9,10 +9,10 @@
 //   derivatives (PhiDevPlus/MinusParameterJB, lsTools.cu:587-770).
 //
 // One fused kernel per stage: both WENO5 reconstructions of each direction
-// (away from the padded grid's edges from six shared differences and their
-// second differences, weno5a), the Godunov combination, the speed and the
-// stage update; stages ping-pong between two scratch fields so that stencil
-// reads never meet a write.
+// (away from the padded grid's edges from six shared differences, their
+// second differences and four shared scaled third differences, weno5s), the
+// Godunov combination, the speed and the stage update; stages ping-pong
+// between two scratch fields so that stencil reads never meet a write.
 #include "weno_march.cuh"
 
 namespace emix {
@@ -70,8 +70,11 @@ __global__ void __launch_bounds__(256) k_reinit_stage(ReinitArgs a) {
                 for (int k = 0; k < 6; ++k) v[k] = bd(a.src, base, s3[d], c - 2 + k);
                 const double A0 = v[1] - v[0], A1 = v[2] - v[1], A2 = v[3] - v[2], A3 = v[4] - v[3],
                              A4 = v[5] - v[4];
-                am = C * weno5a(v[2], A0, A1, A2, A3, eps, 12.0);    // phi^-: D(c), A(c-1..c+2)
-                bp = C * weno5a(v[3], A4, A3, A2, A1, eps, -12.0);   // phi^+: D(c+1), -A(c+3..c)
+                // the four third differences both sides share, scaled for weno5s
+                const double S1 = kSqrt13_3 * (A1 - A0), S2 = kSqrt13_3 * (A2 - A1),
+                             S3 = kSqrt13_3 * (A3 - A2), S4 = kSqrt13_3 * (A4 - A3);
+                am = C * weno5s(v[2], A0, A1, A2, A3, S1, S2, S3, eps, 6.0);    // phi^-: D(c), A(c-1..c+2)
+                bp = C * weno5s(v[3], A4, A3, A2, A1, S4, S3, S2, eps, -6.0);   // phi^+: D(c+1), -A(c+3..c)
             } else {
                 int p[5];
                 // left-biased (phi^-)
