@@ -32,7 +32,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 N_GRID = 256
-SAMPLE_N = 128            # CPU sample grid (same generator, fewer cells)
+SINGLE_N = 128           # grid of the single-thread CPU sample (same generator)
 G = 5                    # level-set ghost layers
 
 
@@ -110,6 +110,17 @@ FP64_OPS_PER_CELL = {
 # captures; the bench scales them to the 256^3 launch by its cells.
 DRAM_BYTES_PER_CELL = {"weno_stage": 89.1}
 
+# where the two tables above come from: ncu captures of the named commands,
+# summarised (command, counters, per-kernel figures) in the profiles files
+CONSTANT_SOURCES = {
+    "fp64_ops_per_cell": "ncu --set full (FP64 fma + add + mul thread instructions per cell), "
+                         "python -m emix_gb300.run --n 192 --steps 2 --walls --impeller: "
+                         "profiles/step_kernels_full_stirred_tank_192.txt, "
+                         "profiles/weno_stage_stirred_tank_192.txt",
+    "dram_bytes_per_cell": "ncu --set full (dram__bytes_read.sum + dram__bytes_write.sum per cell of the "
+                           "stage region), same capture: profiles/weno_stage_stirred_tank_192.txt",
+}
+
 
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
@@ -170,41 +181,53 @@ def dist_setup():
     return replicas.world_from_env()
 
 
-def cpu_sample(steps: int, warmup: int):
-    """Oracle (CPU restatement of the reference algorithm) on the SAMPLE_N^3
-    tank, all host threads.  Returns (Mcell-steps/s, seconds, threads)."""
+def cpu_sample(n: int, steps: int, warmup: int, threads: int = 0, w=None):
+    """Oracle (CPU restatement of the reference algorithm) stepping the n^3
+    tank (the headline generator and settings) on `threads` host threads (0:
+    all).  Returns (Mcell-steps/s, seconds, threads)."""
     from emix_gb300 import fields as F
     from oracle import oracle_py as O
-    w = F.stirred_tank(n=SAMPLE_N, impeller=IMPELLER)
-    p = O.step_params(w, bc_walls=WALLS)
-    d, r = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
-    um, phi = w.um, w.phi
-    for _ in range(warmup):
-        um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
-    sec = time.perf_counter() - t0
-    return w.grid.ncell * steps / sec / 1e6, sec, O.get_threads()
+    O.load()
+    before = O.get_threads()
+    if threads:
+        O.set_threads(threads)
+    try:
+        w = w if w is not None else F.stirred_tank(n=n, impeller=IMPELLER)
+        p = O.step_params(w, bc_walls=WALLS)
+        d, r = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
+        um, phi = w.um, w.phi
+        for _ in range(warmup):
+            um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            um, phi = O.step(p, um, phi, w.jbn, w.mask, d, r)
+        sec = time.perf_counter() - t0
+        thr = O.get_threads()
+    finally:
+        O.set_threads(before)
+    return w.grid.ncell * steps / sec / 1e6, sec, thr
 
 
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    v, sec, thr = cpu_sample(args.steps, args.warmup)
+    # the headline workload itself (256^3 tank), every step a full RK3 step of
+    # it; the CPU needs no warm-up beyond its first step
+    warm = min(args.warmup, 1)
+    v, sec, thr = cpu_sample(N_GRID, args.steps, warm)
     line = {
         "impl": "reference", "metric": "Mcell-RK3-steps/s", "value": round(v, 4),
         "unit": "Mcell-RK3-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1e3 * sec / args.steps, 3),
+        "warmup": warm, "ms_per_step": round(1e3 * sec / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": config_dict(None),
         "cpu_baseline": {"value": round(v, 4), "unit": "Mcell-RK3-steps/s", "cores": thr,
                          "kind": "port",
-                         "sample": f"RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator, "
-                                   f"{SAMPLE_N ** 3} cells per step), CPU restatement of the "
-                                   f"reference algorithm, {thr} threads"},
+                         "sample": f"{args.steps} RK3 steps of the {N_GRID}^3 stirred tank (the "
+                                   f"workload of the config, {warm} untimed step first), CPU "
+                                   f"restatement of the reference algorithm, {thr} threads"},
         "e2e": {"value": round(v, 4), "unit": "Mcell-RK3-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -248,6 +271,8 @@ def ensemble_leg(steps: int, warmup: int, stream=None, world: int = 1, rank: int
     ms_b = replicas.max_over_ranks(timed(lambda k: b.step(k, use_graph=True)), world)
     replicas.barrier(world)
     ms_g = replicas.max_over_ranks(timed(lambda k: b.step_per_grid(k, use_graph=True)), world)
+    replicas.barrier(world)
+    ms_e = replicas.max_over_ranks(timed(lambda k: b.step_per_grid(k, use_graph=False)), world)
     # the batched result agrees with the per-grid result (to rounding)
     b.upload(); b.step(1, use_graph=True); a0 = b.download(0)[0]
     b.upload(); b.step_per_grid(1, use_graph=True); a1 = b.download(0)[0]
@@ -259,8 +284,12 @@ def ensemble_leg(steps: int, warmup: int, stream=None, world: int = 1, rank: int
         "cells": total_cells, "steps": steps, "ranks": world,
         "grids_per_rank": len(part), "cells_rank0": ncell,
         "batched": {"value": round(total_cells / (ms_b * 1e-3) / 1e6, 3), "ms_per_step": round(ms_b, 3)},
-        "per_grid": {"value": round(total_cells / (ms_g * 1e-3) / 1e6, 3), "ms_per_step": round(ms_g, 3)},
-        "speedup": round(ms_g / ms_b, 3), "max_rel_diff_vs_per_grid": diff,
+        "per_grid": {"value": round(total_cells / (ms_g * 1e-3) / 1e6, 3), "ms_per_step": round(ms_g, 3),
+                     "form": "each grid's own captured graph, grids one after another"},
+        "per_grid_eager": {"value": round(total_cells / (ms_e * 1e-3) / 1e6, 3), "ms_per_step": round(ms_e, 3),
+                           "form": "each grid's plain kernels launched one by one, no graph"},
+        "speedup": round(ms_g / ms_b, 3), "speedup_vs_eager": round(ms_e / ms_b, 3),
+        "max_rel_diff_vs_per_grid": diff,
         "tuning": {"cells_per_thread": tune[0], "yz_block": tune[1], "ctas_per_sm": tune[2],
                    "autotune_best_ms": round(tuned_ms, 3)},
     }
@@ -299,13 +328,18 @@ def large_leg(steps: int, warmup: int, stream=None):
     }
 
 
-def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=None, fd=True):
+def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=None, fd=True,
+                state_fd=False, reps=3):
     """dJ/d(omega, Cs) of the tank objective after nsteps steps on the n^3 tank
     by the hand-written adjoint, its cost against the forward steps, and the
-    central finite differences (h = 1e-6) it is checked against.  every = 0:
-    every step's tape kept from the forward pass (the tapes of 128^3 x 8 steps
-    fit in HBM, so nothing is recomputed); every >= 1: checkpoints every
-    `every` steps, each step recomputed with its tape in the reverse sweep."""
+    finite differences it is checked against.  every = 0: every step's tape
+    kept from the forward pass (the tapes of 128^3 x 8 steps fit in HBM, so
+    nothing is recomputed); every >= 1: checkpoints every `every` steps, each
+    step recomputed with its tape in the reverse sweep.  fd: central
+    differences with h = 1e-6 and a Richardson pair per parameter (the
+    central ones only where reps > 1, i.e. the smaller workload); state_fd:
+    the directional derivative of J in a seeded direction of the initial um
+    against the adjoint state gradient."""
     import torch
     from emix_gb300 import fields as F
     from emix_gb300 import ops
@@ -313,15 +347,16 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=N
     X, Y, Z = w.grid.coords()
     # free surface with a ripple, inside the box
     w.phi = np.ascontiguousarray(Z - 0.8 * 2.0 + 0.02 * np.sin(3 * X) * np.cos(2 * Y))
+    del X, Y, Z
     r = ops.TankGradient(w, nsteps, every, bc_walls=WALLS)
     s = stream or torch.cuda.Stream()
     r.ctx.set_stream(s.cuda_stream)
     om, cs = w.impeller.omega, w.cs
     r.run(om, cs)                     # warm-up (graph capture, tables)
     r.adj.backward()
-    # forward (with checkpoints) and reverse sweep, three times: the medians
+    # forward (with checkpoints) and reverse sweep, `reps` times: the medians
     fw, bw = [], []
-    for _ in range(3):
+    for _ in range(reps):
         t0 = time.perf_counter()
         J = r.run(om, cs)
         t1 = time.perf_counter()
@@ -330,6 +365,26 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=N
         fw.append(t1 - t0)
         bw.append(t2 - t1)
     t_fw, t_bw = float(np.median(fw)), float(np.median(bw))
+    state = None
+    if state_fd:
+        # <dJ/dum0, d> against (J(um0 + e d) - J(um0 - e d)) / 2e
+        lum, _ = r.adj.state_gradient()
+        um0 = w.um
+        u = F.uniform(93, 0, um0.shape[1:])
+        d = np.stack([(1e-2 * (-1.0) ** m * float(np.abs(um0[m]).max())) * u for m in range(5)])
+        del u
+        pred = float(torch.sum(lum * torch.from_numpy(d).to(lum.device)).item())
+        del lum
+        eps = 1e-4
+        vals = []
+        for sgn in (1.0, -1.0):
+            w.um = np.ascontiguousarray(um0 + sgn * eps * d)
+            vals.append(r.run(om, cs))
+        w.um = um0
+        fdv = (vals[0] - vals[1]) / (2 * eps)
+        state = {"direction": "1e-2 x (-1)^m x max|um_m| x one seeded uniform field, e = 1e-4",
+                 "adjoint": pred, "fd": fdv, "rel_err": abs(pred - fdv) / abs(fdv)}
+        del d
     fds, rich = [], []
 
     def cfd(k, p0, h):
@@ -340,21 +395,23 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=N
     for k, p0 in enumerate((om, cs) if fd else ()):
         # central differences with h = 1e-6 (rounding-limited when dJ is small
         # against J), and a Richardson pair h, h/2 (error O(h^4))
-        fds.append(cfd(k, p0, 1e-6 * max(abs(p0), 1.0)))
+        if reps > 1:
+            fds.append(cfd(k, p0, 1e-6 * max(abs(p0), 1.0)))
         # omega moves the blades: a step small enough that no cell changes side
         h = (1e-3 if k == 0 else 1e-2) * abs(p0)
         rich.append((4.0 * cfd(k, p0, 0.5 * h) - cfd(k, p0, h)) / 3.0)
-    # plain steps without checkpoints, for the cost ratio (median of three)
+    # plain steps without checkpoints, for the cost ratio (median of `reps`)
     r.ctx.upload(w.um, w.phi)
     r.ctx.step(1, use_graph=True)
     torch.cuda.synchronize()
     pl = []
-    for _ in range(3):
+    for _ in range(reps):
         t3 = time.perf_counter()
         r.ctx.step(nsteps, use_graph=True)
         torch.cuda.synchronize()
         pl.append(time.perf_counter() - t3)
     gib = r.adj.device_bytes() / 2**30
+    ctx_gib = r.ctx.device_bytes() / 2**30
     r.close()
     cells = w.grid.ncell
     plain = float(np.median(pl))
@@ -366,7 +423,7 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=N
         r1.run(om, cs)
         r1.adj.backward()
         fw1, bw1 = [], []
-        for _ in range(3):
+        for _ in range(reps):
             t0 = time.perf_counter()
             r1.run(om, cs)
             t1 = time.perf_counter()
@@ -388,14 +445,16 @@ def adjoint_leg(n: int = 128, nsteps: int = 8, every: int = 0, stream=None, nz=N
         "rel_err": [abs(g[0] - fds[0]) / abs(fds[0]), abs(g[1] - fds[1]) / abs(fds[1])] if fds else None,
         "richardson_fd": rich or None,
         "rel_err_richardson": [abs(g[i] - rich[i]) / abs(rich[i]) for i in range(2)] if rich else None,
+        "state_direction": state,
         "forward_s": round(t_fw, 4), "backward_s": round(t_bw, 4), "plain_steps_s": round(plain, 4),
-        "timing": "medians of three runs each",
+        "timing": f"medians of {reps} runs each" if reps > 1 else "one run after a warm-up run",
         "adjoint_over_forward": round(t_bw / plain, 3),
         "gradient_over_forward": round((t_fw + t_bw) / plain, 3),
         "mode": "tapes kept from the forward pass" if every == 0 else f"checkpoints every {every}, recomputed",
         "forward_value": round(cells * nsteps / plain / 1e6, 3),
         "adjoint_value": round(cells * nsteps / t_bw / 1e6, 3),
         "unit": "Mcell-RK3-steps/s", "checkpoint_every": every, "adjoint_gib": round(gib, 2),
+        "context_gib": round(ctx_gib, 2),
         "recompute": recompute,
     }
 
@@ -425,8 +484,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--no-large", action="store_true", help="skip the 512x512x384 leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (gradient) leg")
-    ap.add_argument("--large-adjoint", action="store_true",
-                    help="also run forward + adjoint on 512x512x384 (20 steps, checkpoints every 5)")
+    ap.add_argument("--no-large-adjoint", action="store_true",
+                    help="skip forward + adjoint on 512x512x384 (20 steps, checkpoints every 5)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -529,6 +588,7 @@ def main():
         "kernel": top, "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak,
         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+        "traffic_source": CONSTANT_SOURCES["dram_bytes_per_cell"],
         "binding": "fp64",
         "fp64": {"achieved": round(fp64_ach / 1e9, 2), "peak": round(fp64_peak / 1e9, 2),
                  "unit": "G FP64 lane-ops/s", "frac": round(fp64_ach / fp64_peak, 4),
@@ -547,6 +607,7 @@ def main():
     floor_b = 2064.0
     step_roofline = {
         "fp64_ops_per_cell_step": round(ops_step / n, 1),
+        "fp64_ops_source": CONSTANT_SOURCES["fp64_ops_per_cell"],
         "fp64_achieved_gops": round(ops_step / sec_step / 1e9, 1),
         "fp64_issue_limit_gops": round(issue / 1e9, 1),
         "fp64_frac_of_issue_limit": round(ops_step / sec_step / issue, 4),
@@ -581,14 +642,21 @@ def main():
         line["large"] = large_leg(min(args.steps, 5), 3, stream)
     if world == 1 and not args.no_adjoint:
         line["adjoint"] = adjoint_leg(stream=stream)
-    if world == 1 and args.large_adjoint:
-        line["large_adjoint"] = adjoint_leg(512, 20, 5, stream, nz=384, fd=False)
+    if world == 1 and not args.no_large_adjoint:
+        line["large_adjoint"] = adjoint_leg(512, 20, 5, stream, nz=384, fd=True, state_fd=True, reps=1)
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, sec, thr = cpu_sample(16, 1)
+        # all host threads on the headline workload itself (its fields, two
+        # steps), and one thread (the reference's serial build) on one step of
+        # the 128^3 tank of the same generator
+        v, sec, thr = cpu_sample(N_GRID, 2, 0, w=w)
+        v1, sec1, _ = cpu_sample(SINGLE_N, 1, 0, threads=1)
         line["cpu_baseline"] = {
             "value": round(v, 4), "unit": "Mcell-RK3-steps/s", "cores": thr, "kind": "port",
-            "sample": f"16 RK3 steps of the {SAMPLE_N}^3 stirred tank (same generator), CPU "
-                      f"restatement of the reference algorithm, {sec:.1f} s, {thr} threads"}
+            "sample": f"2 RK3 steps of the {N_GRID}^3 stirred tank (the workload of the config), CPU "
+                      f"restatement of the reference algorithm, {sec:.1f} s, {thr} threads",
+            "single_thread": {"value": round(v1, 4), "unit": "Mcell-RK3-steps/s", "cores": 1,
+                              "sample": f"1 RK3 step of the {SINGLE_N}^3 stirred tank (same generator "
+                                        f"and settings), {sec1:.1f} s, 1 thread"}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

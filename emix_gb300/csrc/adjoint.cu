@@ -59,11 +59,7 @@ struct emix_adj {
 namespace emix {
 namespace {
 
-int grid_n(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 8) b = 152L * 8;
-    return (int)(b < 1 ? 1 : b);
-}
+int grid_n(long n) { return grid_cap(n, 8); }
 
 bool has_clock(const emix_ctx *c) { return c->clock != nullptr; }
 

@@ -189,7 +189,7 @@ struct emix_batch {
     bool built = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    int sms = 152;
+    int sms = 1;       // SMs of the device, set at creation
 };
 
 namespace {
@@ -480,9 +480,7 @@ int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
             return EMIX_ERR_ARG;
     emix_batch *b = new (std::nothrow) emix_batch();
     if (!b) return EMIX_ERR_ALLOC;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    b->sms = device_sms();
     for (int g = 0; g < ngrid; ++g) {
         emix_ctx *c = nullptr;
         int rc = emix_ctx_create(&params[g], &c);

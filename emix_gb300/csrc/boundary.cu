@@ -79,11 +79,7 @@ __global__ void k_metric_invert(double *__restrict__ jbn, long n, int *__restric
     }
 }
 
-int grid1d(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 8) b = 152L * 8;
-    return (int)(b < 1 ? 1 : b);
-}
+int grid1d(long n) { return grid_cap(n, 8); }
 
 } // namespace
 

@@ -30,6 +30,19 @@ void set_last_message(const char *msg);
 
 inline size_t ncell(int nx, int ny, int nz) { return (size_t)nx * (size_t)ny * (size_t)nz; }
 
+// Streaming multiprocessors of the current device (queried once per device
+// ordinal and cached; 1 if the query fails).
+int device_sms();
+
+// Blocks of `bs` threads for a grid-stride loop over n items: one block per
+// bs items, at most `per_sm` blocks per SM of the current device.
+inline int grid_cap(long n, int per_sm, int bs = 256) {
+    long b = (n + bs - 1) / bs;
+    const long cap = (long)device_sms() * per_sm;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
 // Per-axis factor table of one compact first-derivative operator, built on
 // the host by build_deriv_table() and read by the pencil kernels.
 //

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -150,11 +151,7 @@ __global__ void k_scale_jbn11(double *__restrict__ rs, double *__restrict__ rsv,
     }
 }
 
-int grid_for(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 16) b = 152L * 16;
-    return (int)(b < 1 ? 1 : b);
-}
+int grid_for(long n) { return grid_cap(n, 16); }
 
 // grow-only scratch per device for the device-pointer operators
 struct Scratch {
@@ -263,6 +260,25 @@ int ws_get(size_t bytes, double **out, cudaStream_t *st) {
     return EMIX_OK;
 }
 } // namespace
+
+// SM count per device ordinal, queried on first use (0 = not yet known)
+std::atomic<int> g_sms[64];
+
+int device_sms() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = g_sms[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    g_sms[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 
 // One grow-only scratch buffer per device, shared by every call of the
 // device-pointer operators on that device: calls that overlap on the GPU

@@ -16,10 +16,32 @@ __global__ void k_dfma_chain(double *out, double a, double b, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// The library's reciprocal and square-root helpers beside CUDA's own
+// operators, evaluated on the same arguments in the same kernel: out[k*n + q]
+// for k = 0..5 is rcp_fast, 1.0/x, sqrt_fast, sqrt, rsqrt_fast, 1.0/sqrt.
+__global__ void k_math_selftest(const double *__restrict__ x, double *__restrict__ out, long n) {
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double v = x[q];
+        out[q] = rcp_fast(v);
+        out[n + q] = 1.0 / v;
+        out[2 * n + q] = sqrt_fast(v);
+        out[3 * n + q] = sqrt(v);
+        out[4 * n + q] = rsqrt_fast(v);
+        out[5 * n + q] = 1.0 / sqrt(v);
+    }
+}
+
 } // namespace
 } // namespace emix
 
 using namespace emix;
+
+extern "C" int emix_math_selftest_dev(const double *x, double *out, long n, void *stream) {
+    if (!x || !out || n < 1) return EMIX_ERR_ARG;
+    k_math_selftest<<<grid_cap(n, 8), 256, 0, (cudaStream_t)stream>>>(x, out, n);
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
 
 extern "C" int emix_fp64_peak(double *lane_ops_per_s) {
     if (!lane_ops_per_s) return EMIX_ERR_ARG;

@@ -131,11 +131,7 @@ __global__ void __launch_bounds__(kExtBX *kExtBY) k_ext_stage(ExtStageArgs a) {
     a.out[id] = o;
 }
 
-int grid1(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 16) b = 152L * 16;
-    return (int)(b < 1 ? 1 : b);
-}
+int grid1(long n) { return grid_cap(n, 16); }
 
 } // namespace
 

@@ -66,9 +66,7 @@ int emix_impeller_force_dev(double *um, const double *xyz, const emix_impeller *
         ImpClockArgs ca{clk, 0.0, g};
         k_imp_clock<<<1, 32, 0, st>>>(ca);
         const long n = (long)nx * ny * nz;
-        long b = (n + 255) / 256;
-        if (b > 152L * 8) b = 152L * 8;
-        k_impeller_force<<<(int)(b < 1 ? 1 : b), 256, 0, st>>>(um, xyz, g, clk + 2, n, mask);
+        k_impeller_force<<<grid_cap(n, 8), 256, 0, st>>>(um, xyz, g, clk + 2, n, mask);
         e = cudaGetLastError();
     }
     cudaError_t e2 = cudaFreeAsync(clk, st);

@@ -11,48 +11,37 @@
 // compiled into the library instead.
 //
 // Limit: nxg*nyg*nzg <= kNoAllocMaxCells (1,048,576 padded cells, e.g. 101^3);
-// the array holds two such fields, 16 MiB, in every GPU that loads the
-// library, for the life of the process.  The array is shared by all calls: a
+// the array holds two such fields, 16 MiB.  The array is part of this file's
+// device module, which CUDA loads lazily: the first call on a device loads it
+// (reserving the 16 MiB there until the process exits) together with the
+// stage kernels, and so does take device memory once.  Make that first call
+// at set-up, outside any latency-bound loop and before any stream capture;
+// every later call allocates nothing.  The array is shared by all calls: a
 // call overwrites what the previous call left in it, and calls that overlap on
 // the GPU (different streams or threads) race on it.
 #include "weno.cuh"
-
-#include <mutex>
 
 namespace emix {
 namespace {
 
 constexpr long kNoAllocMaxCells = 1L << 20;
-constexpr int kMaxDevices = 64;
 
 // Two padded stage fields.  Host code must not use this name as a device
 // address (in host code it denotes a host-side shadow); the address comes
 // from cudaGetSymbolAddress below.
 static __device__ __align__(256) double g_weno_stage_scratch[2 * kNoAllocMaxCells];
 
-std::mutex g_mu;
-double *g_addr[kMaxDevices] = {nullptr};
-
-// Per-device set-up, run by the first call on each device with that device
-// current.
+// The array's device address on the current device, looked up on every call
+// (a host-side lookup once the module is loaded; a cached address would go
+// stale if the device's context were torn down and created again).
 int scratch_address(double **out) {
-    int dev = 0;
-    EMIX_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_last_message("emix_weno5_advect_dev_noalloc: device ordinal out of range");
-        return EMIX_ERR_ARG;
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_weno_stage_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        set_last_error(e, "cudaGetSymbolAddress(g_weno_stage_scratch)", __FILE__, __LINE__);
+        return EMIX_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_weno_stage_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            set_last_error(e, "cudaGetSymbolAddress(g_weno_stage_scratch)", __FILE__, __LINE__);
-            return EMIX_ERR_CUDA;
-        }
-        g_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_addr[dev];
+    *out = static_cast<double *>(p);
     return EMIX_OK;
 }
 

@@ -14,12 +14,8 @@ namespace emix {
 #define EMIX_FOR_CELLS(q, n) \
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (n); q += (long)gridDim.x * blockDim.x)
 
-inline int cells_grid(long n, int bs = 256) {
-    long b = (n + bs - 1) / bs;
-    const long cap = 152L * 8;   // 8 resident blocks per SM on 152 SMs
-    if (b > cap) b = cap;
-    return (int)(b < 1 ? 1 : b);
-}
+// 8 resident blocks of 256 threads per SM
+inline int cells_grid(long n, int bs = 256) { return grid_cap(n, 8, bs); }
 
 // ---- primitive variables: u = um(2..4)/um(1), pres = um(1)/Mach^2 ------------
 // (varc_to_varnc, src/MSVSingle/herramientas_incomp2.f90:16-27)

@@ -124,11 +124,7 @@ __global__ void k_mirror_inplace(double *f, int g, int nx, int ny, int nz) {
     }
 }
 
-int grid_r(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 8) b = 152L * 8;
-    return (int)(b < 1 ? 1 : b);
-}
+int grid_r(long n) { return grid_cap(n, 8); }
 
 } // namespace
 

@@ -805,9 +805,8 @@ int emix_ctx_set_step_index(emix_ctx *c, long index) {
     return EMIX_OK;
 }
 
-int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
-    if (!c || !um || nsteps < 0) return EMIX_ERR_ARG;
-    if (c->p.level_set && !phi) return EMIX_ERR_ARG;
+// emix_step_host without its check of the level-set stage's bounded waits
+static int step_host_run(emix_ctx *c, double *um, double *phi, int nsteps) {
     const long n = c->n;
     // the last step is issued here, with the copies back overlapping its tail
     // (needs the side stream, not in use by the level-set overlap)
@@ -864,6 +863,33 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
         EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
     if (tail) EMIX_CUDA_TRY(cudaStreamSynchronize(c->side));
+    return EMIX_OK;
+}
+
+int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
+    if (!c || !um || nsteps < 0) return EMIX_ERR_ARG;
+    if (c->p.level_set && !phi) return EMIX_ERR_ARG;
+    // a level-set stage block whose bounded TMA waits ran out leaves its cells
+    // unwritten: the timeout counter is read before and after the steps, and
+    // a rise is returned as an error
+    const bool tma_stages = emix_ctx_tma_stages(c) > 0;
+    int tmo0 = 0;
+    if (tma_stages) {
+        int rc = emix_weno_tma_timeouts(&tmo0);
+        if (rc) return rc;
+    }
+    int rc = step_host_run(c, um, phi, nsteps);
+    if (rc) return rc;
+    if (tma_stages) {
+        int tmo1 = 0;
+        rc = emix_weno_tma_timeouts(&tmo1);
+        if (rc) return rc;
+        if (tmo1 != tmo0) {
+            set_last_message("emix_step_host: level-set stage blocks gave up waiting for their TMA "
+                             "plane copies; phi is incomplete");
+            return EMIX_ERR_TIMEOUT;
+        }
+    }
     return EMIX_OK;
 }
 

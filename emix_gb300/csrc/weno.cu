@@ -43,11 +43,7 @@ int launch_weno_stage(const WenoArgs &a_in, cudaStream_t st, const CUtensorMap *
 }
 
 namespace {
-int pad_grid(long n) {
-    long b = (n + 255) / 256;
-    if (b > 152L * 8) b = 152L * 8;
-    return (int)(b < 1 ? 1 : b);
-}
+int pad_grid(long n) { return grid_cap(n, 8); }
 
 int weno_advect_impl(double *phi, const double *vel, const double *jbn, double hx, double hy,
                      double hz, double dt, int nxg, int nyg, int nzg, int ref_bugs,

@@ -6,6 +6,7 @@
 
 #include <cudaTypedefs.h>   // PFN_cuTensorMapEncodeTiled
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -39,21 +40,28 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// resident blocks per SM x SMs of a stage kernel (queried once per kernel)
+// resident blocks per SM x SMs of a stage kernel on the current device
+// (queried once per kernel and device ordinal)
 template <class K>
-int resident_blocks(K kernel, int &cache) {
-    if (cache == 0) {
-        int dev = 0, sms = 0, per = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kNT, 0) != cudaSuccess) {
-            cudaGetLastError();
-            return 152 * 4;
-        }
-        cache = sms * (per > 0 ? per : 1);
+int resident_blocks(K kernel, std::atomic<int> (&cache)[64]) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return device_sms() * 4;
     }
-    return cache;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kNT, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return device_sms() * 4;
+    }
+    v = device_sms() * (per > 0 ? per : 1);
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
+
+std::atomic<int> g_res_plain[64], g_res_tma[64];
 
 } // namespace
 
@@ -77,8 +85,7 @@ bool weno_tma_map(CUtensorMap *m, const WenoArgs &a) {
 int launch_weno_march(const WenoArgs &a, cudaStream_t st, const CUtensorMap *tmap) {
     const int gx = (a.rn[0] + kMX - 1) / kMX, gy = (a.rn[1] + kMY - 1) / kMY;
     if (gy > 65535) return EMIX_ERR_ARG;
-    static int res_plain = 0, res_tma = 0;
-    const int resident = tmap ? resident_blocks(k_weno_march_tma, res_tma) : resident_blocks(k_weno_march, res_plain);
+    const int resident = tmap ? resident_blocks(k_weno_march_tma, g_res_tma) : resident_blocks(k_weno_march, g_res_plain);
     // z chunks: the count whose block total fills the last wave best, chunks
     // of at least 8 planes, the smaller count on a tie
     const long cols = (long)gx * gy;

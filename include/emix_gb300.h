@@ -151,7 +151,9 @@ int emix_sgs_viscosity_dev(int model, double coef, double c4,
  * (nxg*nyg*nzg, updated in place), vel[3] and jbn[11] (components 0, 4 and 8
  * read) all on the padded grid; hx,hy,hz are the spacings h.  ref_bugs = 1
  * keeps the reference's z-top neighbour index (lsTools.cu:636).  Device
- * pointers; the scratch (three padded fields) is allocated per call. */
+ * pointers; the scratch (two padded stage fields) comes from a grow-only
+ * device buffer of the library, allocated on the first call that needs more;
+ * calls that overlap on the GPU race on it. */
 int emix_weno5_advect_dev(double *phi, const double *vel, const double *jbn,
                           double hx, double hy, double hz, double dt,
                           int nxg, int nyg, int nzg, int ref_bugs, void *stream);
@@ -166,9 +168,13 @@ int emix_weno5_advect(double *phi, const double *vel, const double *jbn,
  * call cudaMalloc (it can block the device, and fails when another allocator
  * already holds the memory).  The two padded stage fields come from a 16 MiB
  * array compiled into the library, so nxg*nyg*nzg must not exceed 1048576
- * (EMIX_ERR_ARG otherwise).  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race on it. */
+ * (EMIX_ERR_ARG otherwise).  CUDA loads the library's device code lazily, so
+ * the first call on a device loads the array's module (reserving its 16 MiB
+ * on that device until the process exits) and the stage kernels: that first
+ * call does take device memory once.  Make it at set-up, outside any
+ * latency-bound loop and before any stream capture; later calls allocate
+ * nothing.  All calls share the array: calls that overlap on the GPU race on
+ * it. */
 int emix_weno5_advect_dev_noalloc(double *phi, const double *vel, const double *jbn,
                                   double hx, double hy, double hz, double dt,
                                   int nxg, int nyg, int nzg, int ref_bugs, void *stream);
@@ -408,7 +414,11 @@ int emix_ctx_get_time(emix_ctx *ctx, double *t);
  * synchronous.  The copies back overlap the last step where its results are
  * final early (phi after the last level-set stage, um by z-slabs of the last
  * RK update, on a second stream); page-locked host buffers let them run
- * asynchronously.  The values are those of emix_step, bit for bit. */
+ * asynchronously.  The values are those of emix_step, bit for bit.  Returns
+ * EMIX_ERR_TIMEOUT when a level-set stage block gave up waiting for its TMA
+ * plane copies during the call (its cells of phi are then unwritten).
+ * emix_step and the other device-pointer forms return before their kernels
+ * finish: their callers poll emix_weno_tma_timeouts instead. */
 int emix_step_host(emix_ctx *ctx, double *um, double *phi, int nsteps);
 
 /* Number of kernel launches one step issues (for accounting; the records
@@ -468,6 +478,14 @@ int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms);
 /* Diagnostic: measured FP64 fused-multiply-add throughput of the current
  * device in lane operations per second (a short dependent-chain kernel). */
 int emix_fp64_peak(double *lane_ops_per_s);
+
+/* Diagnostic with no counterpart in the reference: the kernels' own
+ * reciprocal and square-root routines (third-order steps from
+ * single-precision seeds) beside CUDA's 1.0/x, sqrt(x) and 1.0/sqrt(x) on the
+ * same n arguments x, in one kernel.  out[6*n]: component k = 0..5 holds
+ * rcp_fast, 1.0/x, sqrt_fast, sqrt, rsqrt_fast, 1.0/sqrt.  Device pointers,
+ * asynchronous on stream. */
+int emix_math_selftest_dev(const double *x, double *out, long n, void *stream);
 
 /* ========================================================================
  * Gradient of a tank objective through the RK3 step (hand-written adjoint;

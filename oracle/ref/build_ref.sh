@@ -5,8 +5,16 @@
 # device code and travel to the GPU machine).  Include paths as in
 # solver/mix3d.mk (../include and ../src).  Needs the reference sources, so it
 # runs on the build host, not on the GPU machine.
+# The reference's location is REF (this recipe's default is the read-only
+# mount of the build host); without its sources the recipe does nothing, so
+# it can run anywhere (the GPU machine has no reference and uses the cubins built
+# here).
 set -e
 REF=${REF:-/root/reference}
+if [ ! -f "$REF/solver/cuDeriv.cu" ]; then
+    echo "reference sources not found under REF=$REF: nothing to build"
+    exit 0
+fi
 HERE=$(cd "$(dirname "$0")/.." && pwd)
 OUT="$HERE/_ref"
 NVCC=${NVCC:-nvcc}

@@ -80,8 +80,8 @@ def test_step_with_walls(emix, oracle, sgs):
     d, r = oracle.inisgdm(np.ascontiguousarray(w.grid.coords()))
     rum, rphi = oracle.step(p, w.um, w.phi, w.jbn, w.mask, d, r, nsteps=2)
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
-    assert_close(phi, rphi, tol=1e-11, what="phi")
+        assert_close(um[m], rum[m], what=f"um[{m}]")
+    assert_close(phi, rphi, what="phi")
     ctx.close()
 
 

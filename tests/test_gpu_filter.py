@@ -107,8 +107,8 @@ def test_step_with_filter_matches_oracle(emix, oracle, use_graph):
     assert ctx.step_index == 3
     um, phi = ctx.download()
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
-    assert_close(phi, rphi, tol=1e-11, what="phi")
+        assert_close(um[m], rum[m], what=f"um[{m}]")
+    assert_close(phi, rphi, what="phi")
     ctx.close()
 
 

@@ -75,14 +75,14 @@ def test_step_with_impeller_matches_oracle(emix, oracle, use_graph):
     ctx.step(3, use_graph=use_graph)
     um, phi = ctx.download()
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
-    assert_close(phi, rphi, tol=1e-11, what="phi")
+        assert_close(um[m], rum[m], what=f"um[{m}]")
+    assert_close(phi, rphi, what="phi")
     assert abs(ctx.time - (0.25 + 3 * w.dt)) <= 1e-15
     # restarting the clock repeats the forcing
     ctx.upload(w.um, w.phi)
     ctx.time = 0.25
     ctx.step(3, use_graph=use_graph)
-    assert_close(ctx.download()[0], rum, tol=1e-11, what="after set_time")
+    assert_close(ctx.download()[0], rum, what="after set_time")
     ctx.close()
 
 
@@ -139,6 +139,6 @@ def test_step_with_impeller_interpolation_matches_oracle(emix, oracle, use_graph
     ctx.step(2, use_graph=use_graph)
     um, phi = ctx.download()
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
-    assert_close(phi, rphi, tol=1e-11, what="phi")
+        assert_close(um[m], rum[m], what=f"um[{m}]")
+    assert_close(phi, rphi, what="phi")
     ctx.close()

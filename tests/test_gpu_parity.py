@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from emix_gb300 import fields as F
-from helpers import TOL, assert_close
+from helpers import TOL, assert_close, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -256,9 +256,9 @@ def test_step(emix, oracle, kind, level_set):
     rum, rphi = oracle.step(p, w.um, w.phi if level_set else None, w.jbn, w.mask, dxyz,
                             ratios, nsteps=2)
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
+        assert_close(um[m], rum[m], what=f"um[{m}]")
     if level_set:
-        assert_close(phi, rphi, tol=1e-11, what="phi")
+        assert_close(phi, rphi, what="phi")
     # graph replay gives the same result as direct launches
     ctx.upload(w.um, w.phi if level_set else None)
     ctx.step(2, use_graph=True)
@@ -289,12 +289,26 @@ def test_overlapped_level_set_stream_gives_the_same_bits(emix):
     b.close()
 
 
+def _ulp_nudged(x, seed):
+    """x with every value moved by one ulp up or down (seeded)."""
+    d = np.random.default_rng(seed).integers(0, 2, size=x.shape).astype(bool)
+    return np.where(d, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
+
+
 @pytest.mark.gpu
 def test_taylor_green_64_ten_steps(emix, oracle):
     """The 64^3 periodic Taylor-Green box with the sphere level set, as the
     reference's CPU-runnable configuration is set up (cyclic scheme B,
     Smagorinsky Cs = 0.1, Re = 1000, CFL 0.3), 10 full RK3 steps through the
-    device context against the same 10 steps of the oracle."""
+    device context against the same 10 steps of the oracle.
+
+    Every field is held to 1e-12 unless the problem itself cannot resolve it:
+    the oracle is also run from inputs moved by one ulp, and a field whose own
+    spread under that perturbation exceeds 1e-12 is held to twice that spread.
+    This is the w-momentum, whose largest value is the 1e-3 noise while its
+    equation carries O(1) terms: one ulp of input moves it by about 2e-12
+    after one step and 5e-12 after ten, so no FP64 evaluation order can
+    match another to 1e-12 there."""
     w = F.taylor_green(64)
     ctx = emix.Context(w, level_set=True)
     ctx.step(10, use_graph=True)
@@ -303,9 +317,16 @@ def test_taylor_green_64_ten_steps(emix, oracle):
     p = oracle.step_params(w, level_set=True)
     dxyz, ratios = oracle.inisgdm(np.ascontiguousarray(w.grid.coords()))
     rum, rphi = oracle.step(p, w.um, w.phi, w.jbn, w.mask, dxyz, ratios, nsteps=10)
+    sum_, sphi = oracle.step(p, _ulp_nudged(w.um, 5), _ulp_nudged(w.phi, 6), w.jbn, w.mask, dxyz,
+                             ratios, nsteps=10)
     for m in range(5):
-        assert_close(um[m], rum[m], tol=1e-11, what=f"um[{m}]")
-    assert_close(phi, rphi, tol=1e-11, what="phi")
+        spread = relerr(sum_[m], rum[m])
+        tol = TOL if spread <= TOL else 2.0 * spread
+        if m != 3:
+            assert tol == TOL, f"um[{m}]: spread {spread:.2e} under one ulp of input"
+        assert_close(um[m], rum[m], tol=tol, what=f"um[{m}] (one-ulp spread {spread:.2e})")
+    assert relerr(sphi, rphi) <= TOL
+    assert_close(phi, rphi, what="phi")
 
 
 @pytest.mark.gpu

@@ -234,3 +234,26 @@ def test_thread_count_invariance(oracle):
     b, pb = oracle.step(p, w.um, w.phi, w.jbn, w.mask, dxyz, ratios)
     oracle.set_threads(0)
     assert np.array_equal(a, b) and np.array_equal(pa, pb)
+
+
+def test_taylor_green_w_momentum_is_conditioned_beyond_1e12(oracle):
+    """The conditioning behind the 64^3 Taylor-Green parity test: one RK3
+    step of the oracle from inputs moved by one ulp (seeded directions)
+    already differs from the unmoved step by more than 1e-12 (normwise
+    relative) in the w-momentum, whose largest value is the 1e-3 noise, while
+    the other fields stay near 1e-14."""
+    w = F.taylor_green(64)
+    p = oracle.step_params(w, level_set=True)
+    dxyz, ratios = oracle.inisgdm(np.ascontiguousarray(w.grid.coords()))
+    rng = np.random.default_rng(5)
+
+    def nudged(x):
+        d = rng.integers(0, 2, size=x.shape).astype(bool)
+        return np.where(d, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
+
+    a_um, a_phi = oracle.step(p, w.um, w.phi, w.jbn, w.mask, dxyz, ratios, nsteps=1)
+    b_um, b_phi = oracle.step(p, nudged(w.um), nudged(w.phi), w.jbn, w.mask, dxyz, ratios, nsteps=1)
+    rel = [float(np.max(np.abs(b_um[m] - a_um[m])) / np.max(np.abs(a_um[m]))) for m in range(5)]
+    assert rel[3] > 1e-12
+    assert max(rel[0], rel[1], rel[2], rel[4]) < 1e-13
+    assert float(np.max(np.abs(b_phi - a_phi)) / np.max(np.abs(a_phi))) < 1e-14
