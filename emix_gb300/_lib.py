@@ -136,6 +136,7 @@ PROTOTYPES = {
     "emix_profile_class_count": (C.c_int, []),
     "emix_profile_class_name": (C.c_char_p, [C.c_int]),
     "emix_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "emix_pencil_set_yz_block": (C.c_int, [C.c_int]),
     "emix_math_selftest_dev": (C.c_int, [vp, vp, C.c_long, vp]),
     "emix_bc_walls_dev": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, vp]),
     "emix_cfl_dev": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int,

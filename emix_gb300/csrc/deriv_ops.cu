@@ -37,7 +37,11 @@ const char *last_error() { return t_last_error.c_str(); }
 // Block width of the y/z pencil kernels: the one of 128, 64, 32 threads that
 // leaves the fewest idle lanes in the last block of a row (ties to the wider),
 // e.g. 64 for nx = 192 where 128 would idle a quarter of the threads.
+std::atomic<int> g_yz_block{0};   // emix_pencil_set_yz_block: 0 = by the rule below
+
 int yz_block(int nx) {
+    const int forced = g_yz_block.load(std::memory_order_relaxed);
+    if (forced) return forced;
     int best = 128, waste = ((nx + 127) / 128) * 128 - nx;
     for (int bs : {64, 32}) {
         const int w = ((nx + bs - 1) / bs) * bs - nx;
@@ -299,6 +303,12 @@ extern "C" {
 const char *emix_last_error(void) { return emix::last_error(); }
 
 const char *emix_version(void) { return "emix_gb300 0.1.0 (sm_103a, FP64)"; }
+
+int emix_pencil_set_yz_block(int threads) {
+    if (threads != 0 && threads != 32 && threads != 64 && threads != 128) return EMIX_ERR_ARG;
+    g_yz_block.store(threads, std::memory_order_relaxed);
+    return EMIX_OK;
+}
 
 int emix_set_legacy_scheme(int scheme) {
     if (!scheme_ok(scheme)) return EMIX_ERR_ARG;

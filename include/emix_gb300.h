@@ -479,6 +479,13 @@ int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms);
  * device in lane operations per second (a short dependent-chain kernel). */
 int emix_fp64_peak(double *lane_ops_per_s);
 
+/* Diagnostic with no counterpart in the reference: the block width (32, 64
+ * or 128 threads, one pencil each) of the single-grid y/z pencil launches
+ * issued afterwards; 0 (default) picks the width that idles the fewest lanes
+ * of the last block of a row.  Process-wide; graphs keep the width they were
+ * captured with. */
+int emix_pencil_set_yz_block(int threads);
+
 /* Diagnostic with no counterpart in the reference: the kernels' own
  * reciprocal and square-root routines (third-order steps from
  * single-precision seeds) beside CUDA's 1.0/x, sqrt(x) and 1.0/sqrt(x) on the

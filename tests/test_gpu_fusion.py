@@ -47,3 +47,4 @@ def test_fused_taped_forward_equals_separate_launches():
     assert np.array_equal(u0, u1) and np.array_equal(f0, f1)
     for a, b in zip(g0, g1):
         assert abs(a - b) <= 1e-14 * abs(b), (a, b)
+
