@@ -51,16 +51,12 @@ struct emix_ctx {
     // default where the copy unit's alignment rules hold), one map per stage
     bool tma = true;
     CUtensorMap weno_tmap[3];
-    // emix_step_host's last step: the copies of phi and um back to the host
-    // start on `side` as soon as each part is final (phi after the last
-    // level-set stage, um by z-slabs of the last RK update); with a single
-    // step, phi's upload runs on `side` under the first substep's flow
-    // kernels (e2e_defer).  Events: [0] phi final, [1..kE2eSlabs] um slabs,
-    // [kE2eSlabs + 1] phi uploaded
+    // emix_step_host's own issue of its first and last steps
+    // (issue_step_host, step.cu): the uploads and the copies back on `side`,
+    // overlapped with the step by z-slabs; the events it orders them with
     static constexpr int kE2eSlabs = 4;
-    double *e2e_um = nullptr, *e2e_phi = nullptr;
-    bool e2e_um_done = false, e2e_defer = false;
-    cudaEvent_t e2e_ev[kE2eSlabs + 2] = {};
+    static constexpr int kE2eEvents = 3 + 3 * kE2eSlabs;
+    cudaEvent_t e2e_ev[kE2eEvents] = {};
 };
 
 namespace emix {

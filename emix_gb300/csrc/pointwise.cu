@@ -95,7 +95,11 @@ __global__ void k_sgs_setup(const double *__restrict__ xyz, double *__restrict__
     }
 }
 
-__global__ void k_prim(PrimArgs a) { EMIX_FOR_CELLS(q, a.n) prim_cell(a, q); }
+__global__ void k_prim(PrimArgs a) {
+    const long end = a.qend > 0 ? a.qend : a.n;
+    for (long q = a.qbeg + blockIdx.x * (long)blockDim.x + threadIdx.x; q < end; q += (long)gridDim.x * blockDim.x)
+        prim_cell(a, q);
+}
 __global__ void __launch_bounds__(256, 2) k_flux_all(FluxArgs a) { EMIX_FOR_CELLS(q, a.n) flux_cell(a, q); }
 __global__ void k_sgs_smag(SmagArgs a) { EMIX_FOR_CELLS(q, a.n) smag_cell(a, q); }
 __global__ void __launch_bounds__(256, 2) k_smag_flux(SmagArgs s, FluxArgs f) {

@@ -23,7 +23,8 @@ struct PrimArgs {
     const double *um;
     double *u, *pres;
     double inv_m2;
-    long n;
+    long n;               // cells (the component stride)
+    long qbeg, qend;      // single-grid launches: cells [qbeg, qend) only (qend = 0: all)
 };
 
 EMIX_DEV void prim_cell(const PrimArgs &a, long q) {

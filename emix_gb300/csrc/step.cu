@@ -318,58 +318,37 @@ namespace {
 
 int fused_with_next(const emix_ctx *c, size_t k) { return c->fuse ? plan_fuse_next(c->plan, k) : 0; }
 
+// records k and k+1 as the one launch plan_fuse_next pairs them into
+int launch_fused(emix_ctx *c, size_t k, cudaStream_t st) {
+    const Launch &L = c->plan[k];
+    if (plan_fuse_next(c->plan, k) == 1) {
+        // the gradients' y and z records as one launch
+        const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
+        const double *in[kMaxFields];
+        double *out[kMaxFields];
+        for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
+        for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
+        return launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, st);
+    }
+    const FluxArgs &fa = c->plan[k + 1].flux;
+    k_smag_flux<<<cells_grid(fa.n), 256, 0, st>>>(L.smag, fa);
+    EMIX_CUDA_TRY(cudaGetLastError());
+    return EMIX_OK;
+}
+
 int issue_step(emix_ctx *c) {
     const bool fork = c->overlap && c->side && !c->prof;
     int s = 0;
     bool joined = true;
     const size_t np = c->plan.size();
     int launches = 0;
-    // emix_step_host's single step: the level-set padding and first stage wait
-    // for phi's upload on the side stream, so they go after the first
-    // substep's flow kernels (which read neither phi nor anything they write)
-    // and just before its first RK launch (which overwrites the velocity the
-    // stage reads)
-    bool defer = c->e2e_defer && !fork;
-    size_t held[2];
-    int nheld = 0;
     for (size_t k = 0; k < np; ++k) {
         const Launch &L = c->plan[k];
-        if (defer && (L.kind == LK_PAD || L.kind == LK_WENO) && nheld < 2) {
-            held[nheld++] = k;
-            continue;
-        }
-        if (defer && L.kind == LK_RK) {
-            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->e2e_ev[emix_ctx::kE2eSlabs + 1], 0));
-            for (int h = 0; h < nheld; ++h) {
-                const Launch &H = c->plan[held[h]];
-                ProfScope ps(c, H.cls);
-                int rc = launch_single(H, c->stream);
-                if (rc) return rc;
-                ++launches;
-            }
-            nheld = 0;
-            defer = false;
-        }
         const int fuse = fused_with_next(c, k);
-        if (fuse == 1) {
-            // the gradients' y and z records as one launch
-            const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
-            const double *in[kMaxFields];
-            double *out[kMaxFields];
-            for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
-            for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
-            ProfScope ps(c, CLS_GRADYZ);
-            int rc = launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, c->stream);
+        if (fuse) {
+            ProfScope ps(c, fuse == 1 ? CLS_GRADYZ : CLS_SGSFLUX);
+            int rc = launch_fused(c, k, c->stream);
             if (rc) return rc;
-            ++k;
-            ++launches;
-            continue;
-        }
-        if (fuse == 2) {
-            ProfScope ps(c, CLS_SGSFLUX);
-            const FluxArgs &fa = c->plan[k + 1].flux;
-            k_smag_flux<<<cells_grid(fa.n), 256, 0, c->stream>>>(L.smag, fa);
-            EMIX_CUDA_TRY(cudaGetLastError());
             ++k;
             ++launches;
             continue;
@@ -389,53 +368,12 @@ int issue_step(emix_ctx *c) {
             EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
             joined = true;
         }
-        if (c->e2e_um && L.kind == LK_RK && L.rk.stage == 3 && !L.rk.faces && k + 1 == np && !filter_due(c)) {
-            // the step's last launch by z-slabs, each slab's um copied back to
-            // the host on the side stream as soon as it is written
-            const long n = c->n, plane = (long)L.rk.nx * L.rk.ny;
-            const int S = emix_ctx::kE2eSlabs;
-            for (int b = 0; b < S; ++b) {
-                const long q0 = plane * (long)(L.rk.nz * b / S), q1 = plane * (long)(L.rk.nz * (b + 1) / S);
-                if (q1 <= q0) continue;
-                RkArgs ra = L.rk;
-                ra.qbeg = q0;
-                ra.qend = q1;
-                k_rk_post<<<cells_grid(q1 - q0), 256, 0, c->stream>>>(ra);
-                EMIX_CUDA_TRY(cudaGetLastError());
-                ++launches;
-                EMIX_CUDA_TRY(cudaEventRecord(c->e2e_ev[1 + b], c->stream));
-                EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->e2e_ev[1 + b], 0));
-                for (int m = 0; m < 5; ++m)
-                    EMIX_CUDA_TRY(cudaMemcpyAsync(c->e2e_um + m * n + q0, L.rk.out + m * n + q0,
-                                                  (size_t)(q1 - q0) * sizeof(double), cudaMemcpyDeviceToHost,
-                                                  c->side));
-            }
-            c->e2e_um_done = true;
-            continue;
-        }
         ProfScope ps(c, L.cls);
         int rc = launch_single(L, c->stream);
         if (rc) return rc;
         ++launches;
-        if (c->e2e_phi && L.kind == LK_WENO && L.weno.stage == 3) {
-            // phi is final: copy it back while the substep's flow kernels run
-            EMIX_CUDA_TRY(cudaEventRecord(c->e2e_ev[0], c->stream));
-            EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, c->e2e_ev[0], 0));
-            EMIX_CUDA_TRY(cudaMemcpyAsync(c->e2e_phi, c->phi, (size_t)c->n * sizeof(double),
-                                          cudaMemcpyDeviceToHost, c->side));
-            c->e2e_phi = nullptr;
-        }
     }
     if (fork && !joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[s - 1], 0));
-    if (nheld) {
-        // no RK record followed (not a plan this library builds): issue them last
-        EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->e2e_ev[emix_ctx::kE2eSlabs + 1], 0));
-        for (int h = 0; h < nheld; ++h) {
-            int rc = launch_single(c->plan[held[h]], c->stream);
-            if (rc) return rc;
-            ++launches;
-        }
-    }
     c->launches = launches;
     return EMIX_OK;
 }
@@ -495,6 +433,186 @@ int capture(emix_ctx *c, F issue, cudaGraph_t *g, cudaGraphExec_t *ge) {
         return EMIX_ERR_CUDA;
     }
     *g = gr;
+    return EMIX_OK;
+}
+
+// Plan positions of the records the host-buffer step issues in its own way.
+struct HostPlan {
+    long prim = -1, pad = -1, weno[4] = {-1, -1, -1, -1}, gx1 = -1, gy1 = -1, gz1 = -1, rkf3 = -1, rk3 = -1;
+};
+
+bool find_host_plan(const emix_ctx *c, HostPlan &h) {
+    const std::vector<Launch> &P = c->plan;
+    const long np = (long)P.size();
+    for (long k = 0; k < np; ++k) {
+        const Launch &L = P[k];
+        if (L.kind == LK_PRIM) h.prim = k;
+        else if (L.kind == LK_PAD) h.pad = k;
+        else if (L.kind == LK_WENO && L.weno.stage >= 1 && L.weno.stage <= 3) h.weno[L.weno.stage] = k;
+        else if (L.kind == LK_RK && L.rk.stage == 3) (L.rk.faces ? h.rkf3 : h.rk3) = k;
+    }
+    const long w1 = h.weno[1];
+    if (h.prim < 0 || h.pad != h.prim + 1 || w1 != h.pad + 1 || h.weno[3] < 0 || h.rk3 != np - 1) return false;
+    // substep 1's gradients follow its level-set stage: x, y, z
+    if (w1 + 3 >= np || P[w1 + 1].kind != LK_DERIV_X || P[w1 + 1].cls != CLS_GRADX ||
+        P[w1 + 2].kind != LK_DERIV_YZ || P[w1 + 2].deriv.axis != 1 || P[w1 + 2].cls != CLS_GRADY ||
+        P[w1 + 3].kind != LK_DERIV_YZ || P[w1 + 3].deriv.axis != 2 || P[w1 + 3].cls != CLS_GRADZ)
+        return false;
+    h.gx1 = w1 + 1; h.gy1 = w1 + 2; h.gz1 = w1 + 3;
+    return true;
+}
+
+// The host-buffer step's overlapped form applies: a level-set context with
+// its second stream free, the plan of this library's single-grid step, no
+// blade-edge interpolation after the RK update, planes deep enough for the
+// upload slabs (the ghost planes mirror within ls_ghost planes of a face).
+bool host_pipeline_ok(const emix_ctx *c) {
+    HostPlan h;
+    return c->p.level_set && c->side && !c->overlap && !(c->p.imp.on && c->p.imp.interp) &&
+           c->p.nz / c->p.ls_ghost >= 1 && find_host_plan(c, h);
+}
+
+// One step of emix_step_host, issued directly (not from the graph), with its
+// host copies on the side stream overlapped with it.
+//   um_in, phi_in (uploads): um by z-slabs; as each slab lands, the first
+//     substep's slab-local launches run on it (primitive variables, x and y
+//     gradients, and the level-set stage on the padded planes whose velocity
+//     the slab holds); phi goes after the first slab, before the padding.
+//   um_out, phi_out (copies back): the last level-set stage moves after the
+//     last RK update (it reads the velocity of the substep before, copied
+//     aside first, since the update overwrites it); the update runs by
+//     z-slabs, each slab of um copied back while the rest of the step runs,
+//     then the stage by z-slabs of the interior, each slab of phi copied back.
+// The launches compute exactly what issue_step's do.  A step after which the
+// filter is due copies back after the filter instead.
+int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double *um_out,
+                  double *phi_out) {
+    HostPlan h;
+    if (!find_host_plan(c, h)) return EMIX_ERR_ARG;
+    const emix_params &p = c->p;
+    const long n = c->n, plane = (long)p.nx * p.ny;
+    const int nx = p.nx, ny = p.ny, nz = p.nz, g = p.ls_ghost;
+    const bool up = um_in != nullptr;
+    const bool due = filter_due(c);
+    const bool down = um_out != nullptr && !due;
+    cudaStream_t st = c->stream, sd = c->side;
+    constexpr int S = emix_ctx::kE2eSlabs;
+    cudaEvent_t *ev = c->e2e_ev;   // [0] start, [1, S] um in, S+1 phi in, [S+2, 2S+1] um final, [2S+2, 3S+1] phi final
+    auto zcut = [nz](int b, int parts) { return (int)((long)nz * b / parts); };
+    const size_t db = sizeof(double);
+
+    // the side stream's copies follow whatever the context stream holds
+    EMIX_CUDA_TRY(cudaEventRecord(ev[0], st));
+    EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[0], 0));
+    const int su = up ? (nz / g < S ? nz / g : S) : 0;
+    for (int b = 0; b < su; ++b) {
+        const long q0 = plane * zcut(b, su), q1 = plane * zcut(b + 1, su);
+        for (int m = 0; m < 5; ++m)
+            EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0 + m * n + q0, um_in + m * n + q0, (size_t)(q1 - q0) * db,
+                                          cudaMemcpyHostToDevice, sd));
+        EMIX_CUDA_TRY(cudaEventRecord(ev[1 + b], sd));
+        if (b == 0) {
+            EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi_in, (size_t)n * db, cudaMemcpyHostToDevice, sd));
+            EMIX_CUDA_TRY(cudaEventRecord(ev[S + 1], sd));
+        }
+    }
+
+    int launches = 0;
+    const long np = (long)c->plan.size();
+    for (long k = 0; k < np; ++k) {
+        const Launch &L = c->plan[k];
+        if (up && (k == h.pad || k == h.weno[1] || k == h.gx1 || k == h.gy1 || k == h.gz1)) continue;
+        if (up && k == h.prim) {
+            const Launch &Gx = c->plan[h.gx1], &Gy = c->plan[h.gy1];
+            for (int b = 0; b < su; ++b) {
+                const int z0 = zcut(b, su), z1 = zcut(b + 1, su);
+                const long q0 = plane * z0, q1 = plane * z1;
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[1 + b], 0));
+                Launch Pq = L;
+                Pq.prim.qbeg = q0;
+                Pq.prim.qend = q1;
+                int rc = launch_single(Pq, st);
+                // the slab's x and y gradients (pencils within its planes)
+                const double *in[3];
+                double *out[3];
+                for (int f = 0; f < 3 && !rc; ++f) { in[f] = Gx.deriv.F.in[f] + q0; out[f] = Gx.deriv.F.out[f] + q0; }
+                if (!rc) rc = launch_deriv(Gx.deriv.T, 0, EPI_STORE, 3, in, out, out, nx, ny, z1 - z0, st);
+                for (int f = 0; f < 3 && !rc; ++f) { in[f] = Gy.deriv.F.in[f] + q0; out[f] = Gy.deriv.F.out[f] + q0; }
+                if (!rc) rc = launch_deriv(Gy.deriv.T, 1, EPI_STORE, 3, in, out, out, nx, ny, z1 - z0, st);
+                if (!rc && b == 0) {
+                    EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[S + 1], 0));
+                    rc = launch_single(c->plan[h.pad], st);
+                }
+                // the first level-set stage on the padded planes that mirror
+                // into this slab (with the ghost planes of the end slabs)
+                Launch Wl = c->plan[h.weno[1]];
+                const int za = b == 0 ? 0 : g + z0, zb = b == su - 1 ? nz + 2 * g : g + z1;
+                Wl.weno.r0[2] = za;
+                Wl.weno.rn[2] = zb - za;
+                if (!rc) rc = launch_single(Wl, st);
+                if (rc) return rc;
+                launches += 4 + (b == 0);
+            }
+            int rc = launch_single(c->plan[h.gz1], st);
+            if (rc) return rc;
+            ++launches;
+            continue;
+        }
+        if (down && k == h.weno[3]) continue;   // issued after the last RK update
+        if (down && k == (h.rkf3 >= 0 ? h.rkf3 : h.rk3))
+            // the velocity the last level-set stage reads, kept in W (free
+            // after the last divergence) before the update overwrites it
+            EMIX_CUDA_TRY(cudaMemcpyAsync(c->W, c->u, (size_t)3 * n * db, cudaMemcpyDeviceToDevice, st));
+        if (down && k == h.rk3) {
+            for (int b = 0; b < S; ++b) {
+                const long q0 = plane * zcut(b, S), q1 = plane * zcut(b + 1, S);
+                if (q1 <= q0) continue;
+                RkArgs ra = L.rk;
+                ra.qbeg = q0;
+                ra.qend = q1;
+                k_rk_post<<<cells_grid(q1 - q0), 256, 0, st>>>(ra);
+                EMIX_CUDA_TRY(cudaGetLastError());
+                ++launches;
+                EMIX_CUDA_TRY(cudaEventRecord(ev[S + 2 + b], st));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[S + 2 + b], 0));
+                for (int m = 0; m < 5; ++m)
+                    EMIX_CUDA_TRY(cudaMemcpyAsync(um_out + m * n + q0, L.rk.out + m * n + q0,
+                                                  (size_t)(q1 - q0) * db, cudaMemcpyDeviceToHost, sd));
+            }
+            Launch Wl = c->plan[h.weno[3]];
+            Wl.weno.vel = c->W;
+            for (int b = 0; b < S; ++b) {
+                const int z0 = zcut(b, S), z1 = zcut(b + 1, S);
+                if (z1 <= z0) continue;
+                Wl.weno.r0[2] = g + z0;
+                Wl.weno.rn[2] = z1 - z0;
+                int rc = launch_single(Wl, st);
+                if (rc) return rc;
+                ++launches;
+                EMIX_CUDA_TRY(cudaEventRecord(ev[2 * S + 2 + b], st));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[2 * S + 2 + b], 0));
+                EMIX_CUDA_TRY(cudaMemcpyAsync(phi_out + plane * z0, c->phi + plane * z0,
+                                              (size_t)(z1 - z0) * plane * db, cudaMemcpyDeviceToHost, sd));
+            }
+            continue;
+        }
+        const int fuse = fused_with_next(c, (size_t)k);
+        int rc = fuse ? launch_fused(c, (size_t)k, st) : launch_single(L, st);
+        if (rc) return rc;
+        k += fuse ? 1 : 0;
+        ++launches;
+    }
+    c->launches = launches;
+    if (due) {
+        int rc = c->fgexec ? (cudaGraphLaunch(c->fgexec, st) == cudaSuccess ? EMIX_OK : EMIX_ERR_CUDA)
+                           : issue_filter(c);
+        if (rc) return rc;
+    }
+    ++c->step_index;
+    if (um_out && !down) {
+        EMIX_CUDA_TRY(cudaMemcpyAsync(um_out, c->um0, 5 * n * db, cudaMemcpyDeviceToHost, st));
+        EMIX_CUDA_TRY(cudaMemcpyAsync(phi_out, c->phi, n * db, cudaMemcpyDeviceToHost, st));
+    }
     return EMIX_OK;
 }
 
@@ -808,61 +926,36 @@ int emix_ctx_set_step_index(emix_ctx *c, long index) {
 // emix_step_host without its check of the level-set stage's bounded waits
 static int step_host_run(emix_ctx *c, double *um, double *phi, int nsteps) {
     const long n = c->n;
-    // the last step is issued here, with the copies back overlapping its tail
-    // (needs the side stream, not in use by the level-set overlap)
-    bool tail = nsteps > 0 && c->side && !c->overlap;
-    for (cudaEvent_t &e : c->e2e_ev)
-        if (tail && !e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-            cudaGetLastError();
-            e = nullptr;
-            tail = false;
-        }
-    cudaEvent_t phi_in = tail ? c->e2e_ev[emix_ctx::kE2eSlabs + 1] : nullptr;
-    EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    if (c->p.level_set && phi_in) {
-        // phi on the side stream, after whatever the context stream holds
-        EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->stream));
-        EMIX_CUDA_TRY(cudaStreamWaitEvent(c->side, phi_in, 0));
-        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->side));
-        EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->side));
-        // earlier steps of this call wait for it in full
-        if (nsteps > 1) EMIX_CUDA_TRY(cudaStreamWaitEvent(c->stream, phi_in, 0));
-    } else {
+    if (!host_pipeline_ok(c) || nsteps < 1) {
+        // plain form: upload, steps, copies back, all on the context stream
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, um, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         if (c->p.level_set)
             EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        if (phi_in) EMIX_CUDA_TRY(cudaEventRecord(phi_in, c->stream));
-    }
-    int rc = emix_step(c, tail ? nsteps - 1 : nsteps, 1);
-    if (rc) return rc;
-    bool um_back = false, phi_back = false;
-    if (tail) {
-        // the side stream must not start a copy before the uploads above and
-        // the earlier steps: it waits on the context stream wherever it copies
-        c->e2e_um = um;
-        c->e2e_phi = c->p.level_set ? phi : nullptr;
-        c->e2e_um_done = false;
-        c->e2e_defer = nsteps == 1 && c->p.level_set;
-        rc = issue_step(c);
-        um_back = c->e2e_um_done;
-        phi_back = c->p.level_set && !c->e2e_phi;
-        c->e2e_um = nullptr;
-        c->e2e_phi = nullptr;
-        c->e2e_um_done = false;
-        c->e2e_defer = false;
-        if (!rc && filter_due(c)) rc = c->fgexec ? (cudaGraphLaunch(c->fgexec, c->stream) == cudaSuccess ? EMIX_OK : EMIX_ERR_CUDA)
-                                                 : issue_filter(c);
-        if (rc) {
-            cudaStreamSynchronize(c->side);
-            return rc;
-        }
-        ++c->step_index;
-    }
-    if (!um_back)
+        int rc = emix_step(c, nsteps, 1);
+        if (rc) return rc;
         EMIX_CUDA_TRY(cudaMemcpyAsync(um, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    if (c->p.level_set && !phi_back)
-        EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    if (tail) EMIX_CUDA_TRY(cudaStreamSynchronize(c->side));
+        if (c->p.level_set)
+            EMIX_CUDA_TRY(cudaMemcpyAsync(phi, c->phi, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        EMIX_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        return EMIX_OK;
+    }
+    for (cudaEvent_t &e : c->e2e_ev)
+        if (!e) EMIX_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // the first step takes the uploads, the last the copies back, the steps
+    // between (if any) replay the graph
+    int rc;
+    if (nsteps == 1) {
+        rc = step_host_one(c, um, phi, um, phi);
+    } else {
+        rc = step_host_one(c, um, phi, nullptr, nullptr);
+        if (!rc && nsteps > 2) rc = emix_step(c, nsteps - 2, 1);
+        if (!rc) rc = step_host_one(c, nullptr, nullptr, um, phi);
+    }
+    cudaError_t e1 = cudaStreamSynchronize(c->stream);
+    cudaError_t e2 = cudaStreamSynchronize(c->side);
+    if (rc) return rc;
+    EMIX_CUDA_TRY(e1);
+    EMIX_CUDA_TRY(e2);
     return EMIX_OK;
 }
 

@@ -1,10 +1,14 @@
 """emix_step_host, the host-buffer entry point (the one the end-to-end figure
-times): the same values as the device-resident steps, bit for bit.  Its last
-step copies phi back after the last level-set stage and um by z-slabs of the
-last RK update, on a second stream, while the step still runs; the cases
-below also cover the forms where it copies after the step instead (the
-level-set overlap on, a filter step last, the impeller's blade-edge
-interpolation after the RK update, no level set) and pageable host buffers."""
+times): the same values as the device-resident steps, bit for bit.  Its first
+step uploads um by z-slabs on a second stream and runs the first substep's
+slab-local launches on each slab as it lands; its last step moves the last
+level-set stage after the last RK update, copies um back by z-slabs of that
+update and phi by z-slabs of the stage.  The cases below cover one, two and
+three steps, walls and the periodic box, uneven and shallow z extents (fewer
+upload slabs), the forms that copy plainly instead (the level-set overlap
+on, the impeller's blade-edge interpolation after the RK update, no level
+set), a filter step last (uploads overlapped, copies after the filter) and
+pageable host buffers."""
 import numpy as np
 import pytest
 
@@ -48,7 +52,7 @@ def _host(w, nsteps, pinned=True, overlap=False, level_set=True, **kw):
     return um.copy(), (phi.copy() if level_set else None), idx
 
 
-@pytest.mark.parametrize("nsteps", [1, 3])
+@pytest.mark.parametrize("nsteps", [1, 2, 3])
 @pytest.mark.parametrize("pinned", [True, False])
 def test_step_host_matches_device_steps(nsteps, pinned):
     w = _tank()
@@ -59,11 +63,39 @@ def test_step_host_matches_device_steps(nsteps, pinned):
     assert np.array_equal(hphi, phi)
 
 
+@pytest.mark.parametrize("case", ["nz23", "nz9", "nz14", "periodic", "static_mask"])
+def test_step_host_shapes(case):
+    """Uneven slab cuts (nz = 23), a single upload slab (nz = 9 with 5 ghost
+    layers), two (nz = 14), the periodic box without walls and the tank
+    without the rotating impeller."""
+    kw = {"bc_walls": 1}
+    if case == "periodic":
+        w = F.taylor_green(20)
+        kw = {}
+    elif case == "static_mask":
+        w = F.stirred_tank(n=20, nz=18)
+    else:
+        w = F.stirred_tank(n=18, nz=int(case[2:]), impeller=True, impeller_omega=1.3)
+    for nsteps in (1, 2):
+        um, phi, idx = _device(w, nsteps, **kw)
+        hum, hphi, hidx = _host(w, nsteps, **kw)
+        assert hidx == idx == nsteps
+        assert np.array_equal(hum, um), f"{case}, {nsteps} steps: um"
+        assert np.array_equal(hphi, phi), f"{case}, {nsteps} steps: phi"
+
+
 @pytest.mark.parametrize("case", ["overlap", "filter_last", "interp", "no_level_set"])
 def test_step_host_forms_without_the_tail_copies(case):
     kw = {"bc_walls": 1}
     w = _tank(interp=1 if case == "interp" else 0)
     nsteps = 3 if case == "filter_last" else 2
+    if case == "filter_last":
+        # one step whose filter is due: uploads overlapped, copies after the filter
+        kw1 = dict(kw, filter_every=1, cfilt=0.2)
+        um, phi, idx = _device(w, 1, **kw1)
+        hum, hphi, hidx = _host(w, 1, **kw1)
+        assert hidx == idx == 1
+        assert np.array_equal(hum, um) and np.array_equal(hphi, phi)
     if case == "filter_last":
         kw.update(filter_every=2, cfilt=0.2)   # steps 0 and 2 filter: the last one does
     ls = case != "no_level_set"
