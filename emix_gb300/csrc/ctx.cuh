@@ -54,8 +54,8 @@ struct emix_ctx {
     // emix_step_host's own issue of its first and last steps
     // (issue_step_host, step.cu): the uploads and the copies back on `side`,
     // overlapped with the step by z-slabs; the events it orders them with
-    static constexpr int kE2eSlabs = 4;
-    static constexpr int kE2eEvents = 3 + 3 * kE2eSlabs;
+    static constexpr int kE2eSlabsIn = 8, kE2eSlabs = 4;
+    static constexpr int kE2eEvents = 2 + kE2eSlabsIn + 2 * kE2eSlabs;
     cudaEvent_t e2e_ev[kE2eEvents] = {};
 };
 

@@ -438,7 +438,7 @@ int capture(emix_ctx *c, F issue, cudaGraph_t *g, cudaGraphExec_t *ge) {
 
 // Plan positions of the records the host-buffer step issues in its own way.
 struct HostPlan {
-    long prim = -1, pad = -1, weno[4] = {-1, -1, -1, -1}, gx1 = -1, gy1 = -1, gz1 = -1, rkf3 = -1, rk3 = -1;
+    long prim = -1, pad = -1, weno[4] = {-1, -1, -1, -1}, rkf3 = -1, rk3 = -1;
 };
 
 bool find_host_plan(const emix_ctx *c, HostPlan &h) {
@@ -451,15 +451,9 @@ bool find_host_plan(const emix_ctx *c, HostPlan &h) {
         else if (L.kind == LK_WENO && L.weno.stage >= 1 && L.weno.stage <= 3) h.weno[L.weno.stage] = k;
         else if (L.kind == LK_RK && L.rk.stage == 3) (L.rk.faces ? h.rkf3 : h.rk3) = k;
     }
-    const long w1 = h.weno[1];
-    if (h.prim < 0 || h.pad != h.prim + 1 || w1 != h.pad + 1 || h.weno[3] < 0 || h.rk3 != np - 1) return false;
-    // substep 1's gradients follow its level-set stage: x, y, z
-    if (w1 + 3 >= np || P[w1 + 1].kind != LK_DERIV_X || P[w1 + 1].cls != CLS_GRADX ||
-        P[w1 + 2].kind != LK_DERIV_YZ || P[w1 + 2].deriv.axis != 1 || P[w1 + 2].cls != CLS_GRADY ||
-        P[w1 + 3].kind != LK_DERIV_YZ || P[w1 + 3].deriv.axis != 2 || P[w1 + 3].cls != CLS_GRADZ)
-        return false;
-    h.gx1 = w1 + 1; h.gy1 = w1 + 2; h.gz1 = w1 + 3;
-    return true;
+    // the padding and the first level-set stage directly after the primitive
+    // variables, the last RK update last
+    return h.prim >= 0 && h.pad == h.prim + 1 && h.weno[1] == h.pad + 1 && h.weno[3] >= 0 && h.rk3 == np - 1;
 }
 
 // The host-buffer step's overlapped form applies: a level-set context with
@@ -474,10 +468,10 @@ bool host_pipeline_ok(const emix_ctx *c) {
 
 // One step of emix_step_host, issued directly (not from the graph), with its
 // host copies on the side stream overlapped with it.
-//   um_in, phi_in (uploads): um by z-slabs; as each slab lands, the first
-//     substep's slab-local launches run on it (primitive variables, x and y
-//     gradients, and the level-set stage on the padded planes whose velocity
-//     the slab holds); phi goes after the first slab, before the padding.
+//   um_in, phi_in (uploads): phi first, then um by z-slabs; as each slab
+//     lands, the primitive variables of its cells and the first level-set
+//     stage on the padded planes whose velocity it holds run on it (the
+//     stage fills the GPU even on a slab; pencil launches would not).
 //   um_out, phi_out (copies back): the last level-set stage moves after the
 //     last RK update (it reads the velocity of the substep before, copied
 //     aside first, since the update overwrites it); the update runs by
@@ -491,56 +485,51 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     if (!find_host_plan(c, h)) return EMIX_ERR_ARG;
     const emix_params &p = c->p;
     const long n = c->n, plane = (long)p.nx * p.ny;
-    const int nx = p.nx, ny = p.ny, nz = p.nz, g = p.ls_ghost;
+    const int nz = p.nz, g = p.ls_ghost;
     const bool up = um_in != nullptr;
     const bool due = filter_due(c);
     const bool down = um_out != nullptr && !due;
     cudaStream_t st = c->stream, sd = c->side;
-    constexpr int S = emix_ctx::kE2eSlabs;
-    cudaEvent_t *ev = c->e2e_ev;   // [0] start, [1, S] um in, S+1 phi in, [S+2, 2S+1] um final, [2S+2, 3S+1] phi final
+    constexpr int SI = emix_ctx::kE2eSlabsIn, S = emix_ctx::kE2eSlabs;
+    // events: [0] start, [1] phi in, [2, 2+SI) um slabs in, then S um slabs
+    // final, then S phi slabs final
+    cudaEvent_t *ev = c->e2e_ev, *ev_in = ev + 2, *ev_um = ev + 2 + SI, *ev_phi = ev + 2 + SI + S;
     auto zcut = [nz](int b, int parts) { return (int)((long)nz * b / parts); };
     const size_t db = sizeof(double);
 
     // the side stream's copies follow whatever the context stream holds
     EMIX_CUDA_TRY(cudaEventRecord(ev[0], st));
     EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[0], 0));
-    const int su = up ? (nz / g < S ? nz / g : S) : 0;
+    // upload slabs at least ls_ghost planes deep (the ghost planes mirror
+    // within ls_ghost planes of a face)
+    const int su = up ? (nz / g < SI ? nz / g : SI) : 0;
+    if (up) {
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi_in, (size_t)n * db, cudaMemcpyHostToDevice, sd));
+        EMIX_CUDA_TRY(cudaEventRecord(ev[1], sd));
+    }
     for (int b = 0; b < su; ++b) {
         const long q0 = plane * zcut(b, su), q1 = plane * zcut(b + 1, su);
         for (int m = 0; m < 5; ++m)
             EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0 + m * n + q0, um_in + m * n + q0, (size_t)(q1 - q0) * db,
                                           cudaMemcpyHostToDevice, sd));
-        EMIX_CUDA_TRY(cudaEventRecord(ev[1 + b], sd));
-        if (b == 0) {
-            EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi_in, (size_t)n * db, cudaMemcpyHostToDevice, sd));
-            EMIX_CUDA_TRY(cudaEventRecord(ev[S + 1], sd));
-        }
+        EMIX_CUDA_TRY(cudaEventRecord(ev_in[b], sd));
     }
 
     int launches = 0;
     const long np = (long)c->plan.size();
     for (long k = 0; k < np; ++k) {
         const Launch &L = c->plan[k];
-        if (up && (k == h.pad || k == h.weno[1] || k == h.gx1 || k == h.gy1 || k == h.gz1)) continue;
+        if (up && (k == h.pad || k == h.weno[1])) continue;   // issued with the slabs
         if (up && k == h.prim) {
-            const Launch &Gx = c->plan[h.gx1], &Gy = c->plan[h.gy1];
             for (int b = 0; b < su; ++b) {
                 const int z0 = zcut(b, su), z1 = zcut(b + 1, su);
-                const long q0 = plane * z0, q1 = plane * z1;
-                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[1 + b], 0));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[b], 0));
                 Launch Pq = L;
-                Pq.prim.qbeg = q0;
-                Pq.prim.qend = q1;
+                Pq.prim.qbeg = plane * z0;
+                Pq.prim.qend = plane * z1;
                 int rc = launch_single(Pq, st);
-                // the slab's x and y gradients (pencils within its planes)
-                const double *in[3];
-                double *out[3];
-                for (int f = 0; f < 3 && !rc; ++f) { in[f] = Gx.deriv.F.in[f] + q0; out[f] = Gx.deriv.F.out[f] + q0; }
-                if (!rc) rc = launch_deriv(Gx.deriv.T, 0, EPI_STORE, 3, in, out, out, nx, ny, z1 - z0, st);
-                for (int f = 0; f < 3 && !rc; ++f) { in[f] = Gy.deriv.F.in[f] + q0; out[f] = Gy.deriv.F.out[f] + q0; }
-                if (!rc) rc = launch_deriv(Gy.deriv.T, 1, EPI_STORE, 3, in, out, out, nx, ny, z1 - z0, st);
                 if (!rc && b == 0) {
-                    EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[S + 1], 0));
+                    EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[1], 0));
                     rc = launch_single(c->plan[h.pad], st);
                 }
                 // the first level-set stage on the padded planes that mirror
@@ -551,11 +540,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
                 Wl.weno.rn[2] = zb - za;
                 if (!rc) rc = launch_single(Wl, st);
                 if (rc) return rc;
-                launches += 4 + (b == 0);
+                launches += 2 + (b == 0);
             }
-            int rc = launch_single(c->plan[h.gz1], st);
-            if (rc) return rc;
-            ++launches;
             continue;
         }
         if (down && k == h.weno[3]) continue;   // issued after the last RK update
@@ -573,8 +559,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
                 k_rk_post<<<cells_grid(q1 - q0), 256, 0, st>>>(ra);
                 EMIX_CUDA_TRY(cudaGetLastError());
                 ++launches;
-                EMIX_CUDA_TRY(cudaEventRecord(ev[S + 2 + b], st));
-                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[S + 2 + b], 0));
+                EMIX_CUDA_TRY(cudaEventRecord(ev_um[b], st));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev_um[b], 0));
                 for (int m = 0; m < 5; ++m)
                     EMIX_CUDA_TRY(cudaMemcpyAsync(um_out + m * n + q0, L.rk.out + m * n + q0,
                                                   (size_t)(q1 - q0) * db, cudaMemcpyDeviceToHost, sd));
@@ -589,8 +575,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
                 int rc = launch_single(Wl, st);
                 if (rc) return rc;
                 ++launches;
-                EMIX_CUDA_TRY(cudaEventRecord(ev[2 * S + 2 + b], st));
-                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[2 * S + 2 + b], 0));
+                EMIX_CUDA_TRY(cudaEventRecord(ev_phi[b], st));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev_phi[b], 0));
                 EMIX_CUDA_TRY(cudaMemcpyAsync(phi_out + plane * z0, c->phi + plane * z0,
                                               (size_t)(z1 - z0) * plane * db, cudaMemcpyDeviceToHost, sd));
             }

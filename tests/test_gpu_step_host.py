@@ -1,7 +1,8 @@
 """emix_step_host, the host-buffer entry point (the one the end-to-end figure
 times): the same values as the device-resident steps, bit for bit.  Its first
-step uploads um by z-slabs on a second stream and runs the first substep's
-slab-local launches on each slab as it lands; its last step moves the last
+step uploads phi, then um by z-slabs on a second stream, and runs the
+primitive variables and the first level-set stage on each slab as it lands;
+its last step moves the last
 level-set stage after the last RK update, copies um back by z-slabs of that
 update and phi by z-slabs of the stage.  The cases below cover one, two and
 three steps, walls and the periodic box, uneven and shallow z extents (fewer
