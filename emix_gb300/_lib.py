@@ -65,6 +65,8 @@ PROTOTYPES = {
     "emix_set_legacy_scheme": (C.c_int, [C.c_int]),
     "emix_deriv_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double,
                                  C.c_int, C.c_int, C.c_int, vp]),
+    "emix_deriv_pcr_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double, C.c_int,
+                                     C.c_int, C.c_int, C.c_int, vp]),
     "emix_cudaDeriv": (C.c_int, [i3, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
                                  C.c_int, C.c_int, C.c_int]),
     "emix_cudaDeriv_dev": (C.c_int, [i3, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
@@ -154,6 +156,10 @@ PROTOTYPES = {
     "emix_batch_get_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
     "emix_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+    "emix_batch_set_pcr": (C.c_int, [vp, C.c_int]),
+    "emix_batch_get_pcr": (C.c_int, [vp, C.POINTER(C.c_int)]),
+    "emix_batch_pcr_positions": (C.c_int, [vp, C.POINTER(C.c_int)]),
+    "emix_batch_autotune_pcr_ms": (C.c_int, [vp, C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -10,7 +10,8 @@
 // captured in a CUDA graph.  The work-list granularity (pencils per y/z block,
 // cells per pointwise item, resident CTAs per SM of the persistent kernels)
 // is chosen by a timing autotuner.
-#include "plan.cuh"
+#include "ctx.cuh"
+#include "pcr.cuh"
 #include "weno_march.cuh"
 
 #include <algorithm>
@@ -129,6 +130,31 @@ k_batch_deriv_yz(const DerivArgs *__restrict__ args, const long *__restrict__ st
     for (long vb = blockIdx.x; vb < total; vb += gridDim.x) batch_yz_item<EPI>(args, start, shape, ngrid, vb);
 }
 
+// a y/z position by PCR + Thomas (S steps): item = (x block of
+// pcr_block_x<S>() pencils, other coordinate, field), one warp per 32 / 2^S
+// pencils
+template <int S, int EPI>
+__global__ void __launch_bounds__(128)
+k_batch_deriv_pcr(const DerivArgs *__restrict__ args, const PcrTable *__restrict__ pargs,
+                  const long *__restrict__ start, const Shape *__restrict__ shape, int ngrid) {
+    const long total = start[ngrid];
+    const int warp = threadIdx.x >> 5;
+    for (long vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int g = find_grid(start, ngrid, vb);
+        const long local = vb - start[g];
+        const Shape sh = shape[g];
+        const DerivArgs &a = args[g];
+        const int bx = (int)(local % sh.gx), by = (int)((local / sh.gx) % sh.gy),
+                  bz = (int)(local / ((long)sh.gx * sh.gy));
+        const int nx = a.nx;
+        const int nother = a.axis == 1 ? a.nz : a.ny;
+        const long s = a.axis == 1 ? (long)nx : (long)nx * a.ny;
+        const long os = a.axis == 1 ? (long)nx * a.ny : (long)nx;
+        pcr_yz_warp<S, pcr_rows<S>(), EPI>(pargs[g], a.F, nx, nother, s, os,
+                                           bx * pcr_block_x<S>() + warp * (32 >> S), by, bz);
+    }
+}
+
 // two y/z positions (the gradients' y and z) over one work list
 __global__ void __launch_bounds__(128)
 k_batch_deriv_yz_pair(const DerivArgs *__restrict__ aa, const long *__restrict__ sa,
@@ -165,6 +191,7 @@ struct BatchTune {
     int cpb;       // cells per thread in pointwise items (x 256 per item)
     int yz_bs;     // threads per y/z pencil block
     int ctas_sm;   // resident CTAs per SM for the persistent grids
+    int pcr;       // PCR steps of the y/z positions (0: one Thomas sweep per pencil)
 };
 
 struct BatchPos {
@@ -174,6 +201,8 @@ struct BatchPos {
     long *start;       // device prefix sums of virtual blocks, ngrid + 1
     Shape *shape;      // device per-grid virtual launch shapes
     long total;
+    PcrTable *pcr;     // y/z positions under tune.pcr > 0: device array of ngrid PCR tables
+    int pcr_steps;     // PCR steps of this position (0: Thomas)
 };
 
 } // namespace emix
@@ -185,11 +214,14 @@ struct emix_batch {
     cudaStream_t stream = nullptr, own = nullptr;
     std::vector<BatchPos> pos;
     void *dmem = nullptr;           // one device allocation for all position tables
-    BatchTune tune{4, 64, 4};
+    BatchTune tune{4, 64, 4, 0};
     bool built = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int sms = 1;       // SMs of the device, set at creation
+    // ms per step the last autotune measured: [0] the best Thomas shapes,
+    // [k] the same with k PCR steps in the y/z positions (-1: not measured)
+    double pcr_ms[kPcrMaxSteps + 1] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
 };
 
 namespace {
@@ -258,6 +290,11 @@ Shape shape_of(const Launch &L, const BatchTune &t) {
         const long np = (long)L.deriv.ny * L.deriv.nz;
         s.gx = (int)((np + 127) / 128);
         s.gz = L.deriv.nf;
+    } else if (L.kind == LK_DERIV_YZ && t.pcr > 0) {
+        const int bxp = 4 * (32 >> t.pcr);
+        s.gx = (L.deriv.nx + bxp - 1) / bxp;
+        s.gy = L.deriv.axis == 1 ? L.deriv.nz : L.deriv.ny;
+        s.gz = L.deriv.nf;
     } else if (L.kind == LK_DERIV_YZ) {
         s.gx = (L.deriv.nx + t.yz_bs - 1) / t.yz_bs;
         s.gy = L.deriv.axis == 1 ? L.deriv.nz : L.deriv.ny;
@@ -286,8 +323,9 @@ int build(emix_batch *b) {
     const size_t np = plans[0]->size();
     // host image of every position's tables, laid out back to back
     std::vector<unsigned char> host;
-    std::vector<size_t> off_args(np), off_start(np), off_shape(np);
+    std::vector<size_t> off_args(np), off_start(np), off_shape(np), off_pcr(np, 0);
     std::vector<long> totals(np);
+    std::vector<int> pcr_on(np, 0);
     auto align = [&](size_t a) { host.resize((host.size() + a - 1) / a * a); };
     for (size_t k = 0; k < np; ++k) {
         const Launch &L0 = (*plans[0])[k];
@@ -297,6 +335,18 @@ int build(emix_batch *b) {
         host.resize(host.size() + as * G);
         std::vector<long> start(G + 1, 0);
         std::vector<Shape> sh(G);
+        // y/z positions run by PCR + Thomas when the tuning asks for it and
+        // every grid's pencils fit (at most kPcrMaxN rows)
+        BatchTune tk = b->tune;
+        if (L0.kind == LK_DERIV_YZ && tk.pcr > 0) {
+            for (int g = 0; g < G; ++g) {
+                const Launch &L = (*plans[g])[k];
+                if ((L.deriv.axis == 1 ? L.deriv.ny : L.deriv.nz) > kPcrMaxN) tk.pcr = 0;
+            }
+        } else {
+            tk.pcr = 0;
+        }
+        pcr_on[k] = tk.pcr;
         for (int g = 0; g < G; ++g) {
             const Launch &L = (*plans[g])[k];
             if (L.kind != L0.kind || (L.kind == LK_DERIV_X || L.kind == LK_DERIV_YZ ? L.deriv.epi != L0.deriv.epi : false)) {
@@ -304,7 +354,7 @@ int build(emix_batch *b) {
                 return EMIX_ERR_ARG;
             }
             std::memcpy(host.data() + off_args[k] + as * g, args_ptr(L), as);
-            sh[g] = shape_of(L, b->tune);
+            sh[g] = shape_of(L, tk);
             start[g + 1] = start[g] + (long)sh[g].gx * sh[g].gy * sh[g].gz;
         }
         totals[k] = start[G];
@@ -316,6 +366,21 @@ int build(emix_batch *b) {
         off_shape[k] = host.size();
         host.resize(host.size() + sizeof(Shape) * G);
         std::memcpy(host.data() + off_shape[k], sh.data(), sizeof(Shape) * G);
+        if (pcr_on[k]) {
+            std::vector<PcrTable> pt(G);
+            for (int g = 0; g < G; ++g) {
+                const Launch &L = (*plans[g])[k];
+                const int ax = L.deriv.axis;
+                const emix_params &gp = b->grids[g]->p;
+                int rc = get_pcr_table(gp.scheme[ax], ax == 1 ? L.deriv.ny : L.deriv.nz, gp.h[ax], pcr_on[k],
+                                       &pt[g]);
+                if (rc) return rc;
+            }
+            align(256);
+            off_pcr[k] = host.size();
+            host.resize(host.size() + sizeof(PcrTable) * G);
+            std::memcpy(host.data() + off_pcr[k], pt.data(), sizeof(PcrTable) * G);
+        }
     }
     if (b->dmem) cudaFree(b->dmem);
     b->dmem = nullptr;
@@ -337,10 +402,14 @@ int build(emix_batch *b) {
         P.start = reinterpret_cast<long *>(base + off_start[k]);
         P.shape = reinterpret_cast<Shape *>(base + off_shape[k]);
         P.total = totals[k];
+        P.pcr = pcr_on[k] ? reinterpret_cast<PcrTable *>(base + off_pcr[k]) : nullptr;
         P.fuse = plan_fuse_next(*plans[0], k);
         for (int g = 1; g < G && P.fuse; ++g)
             if (plan_fuse_next(*plans[g], k) != P.fuse) P.fuse = 0;
+        // the gradients' y and z pair runs as one Thomas launch only
+        if (P.fuse == 1 && (pcr_on[k] || (k + 1 < np && pcr_on[k + 1]))) P.fuse = 0;
     }
+    for (size_t k = 0; k < np; ++k) b->pos[k].pcr_steps = pcr_on[k];
     b->built = true;
     return EMIX_OK;
 }
@@ -405,6 +474,27 @@ int issue(emix_batch *b) {
             break;
         }
         case LK_DERIV_YZ:
+            if (P.pcr) {
+                const DerivArgs *da = (const DerivArgs *)P.args;
+                const int nbk = all_items(P.total);
+#define EMIX_PCR_CASE(S)                                                                                 \
+    case S:                                                                                              \
+        if (P.epi == EPI_STORE)                                                                          \
+            k_batch_deriv_pcr<S, EPI_STORE><<<nbk, 128, 0, st>>>(da, P.pcr, P.start, P.shape, G);         \
+        else                                                                                             \
+            k_batch_deriv_pcr<S, EPI_ACCUM><<<nbk, 128, 0, st>>>(da, P.pcr, P.start, P.shape, G);         \
+        break;
+                switch (P.pcr_steps) {
+                    EMIX_PCR_CASE(2)
+                    EMIX_PCR_CASE(3)
+                    EMIX_PCR_CASE(4)
+                    EMIX_PCR_CASE(5)
+                default:
+                    return EMIX_ERR_ARG;
+                }
+#undef EMIX_PCR_CASE
+                break;
+            }
             if (P.epi == EPI_STORE)
                 k_batch_deriv_yz<EPI_STORE><<<all_items(P.total), b->tune.yz_bs, 0, st>>>((const DerivArgs *)P.args, P.start, P.shape, G);
             else
@@ -547,7 +637,7 @@ int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int
     if (!b || cells_per_thread < 1 || cells_per_thread > 64 || ctas_per_sm < 0 || ctas_per_sm > 64 ||
         (yz_block != 32 && yz_block != 64 && yz_block != 128))
         return EMIX_ERR_ARG;
-    b->tune = BatchTune{cells_per_thread, yz_block, ctas_per_sm};
+    b->tune = BatchTune{cells_per_thread, yz_block, ctas_per_sm, b->tune.pcr};
     b->built = false;
     drop_graph(b);
     return EMIX_OK;
@@ -558,6 +648,32 @@ int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, i
     if (cells_per_thread) *cells_per_thread = b->tune.cpb;
     if (yz_block) *yz_block = b->tune.yz_bs;
     if (ctas_per_sm) *ctas_per_sm = b->tune.ctas_sm;
+    return EMIX_OK;
+}
+
+int emix_batch_set_pcr(emix_batch *b, int steps) {
+    if (!b || (steps != 0 && (steps < 2 || steps > kPcrMaxSteps))) return EMIX_ERR_ARG;
+    b->tune.pcr = steps;
+    b->built = false;
+    drop_graph(b);
+    return EMIX_OK;
+}
+
+int emix_batch_get_pcr(emix_batch *b, int *steps) {
+    if (!b || !steps) return EMIX_ERR_ARG;
+    *steps = b->tune.pcr;
+    return EMIX_OK;
+}
+
+int emix_batch_pcr_positions(emix_batch *b, int *count) {
+    if (!b || !count) return EMIX_ERR_ARG;
+    if (!b->built) {
+        int rc = build(b);
+        if (rc) return rc;
+    }
+    int c = 0;
+    for (const BatchPos &P : b->pos) c += P.pcr_steps > 0 ? 1 : 0;
+    *count = c;
     return EMIX_OK;
 }
 
@@ -575,26 +691,53 @@ int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms) {
     EMIX_CUDA_TRY(cudaEventCreate(&e0));
     EMIX_CUDA_TRY(cudaEventCreate(&e1));
     int rc = EMIX_OK;
+    for (double &m : b->pcr_ms) m = -1.0;
+    // ms per step of the current tuning
+    auto timed = [&](float *ms) -> int {
+        int r = step_impl(b, 1, 0);   // build + warm
+        if (r) return r;
+        cudaEventRecord(e0, b->stream);
+        if ((r = step_impl(b, nsteps, 0))) return r;
+        cudaEventRecord(e1, b->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return EMIX_ERR_CUDA;
+        cudaEventElapsedTime(ms, e0, e1);
+        *ms /= nsteps;
+        return EMIX_OK;
+    };
+    // the launch shapes with one Thomas sweep per pencil, then the PCR depth
+    // of the y/z positions on the best of those
+    b->tune.pcr = 0;
     for (int cpb : cpbs)
         for (int bs : bss)
             for (int cs : ctass) {
                 if ((rc = emix_batch_set_tuning(b, cpb, bs, cs))) goto done;
-                if ((rc = step_impl(b, 1, 0))) goto done;   // build + warm
-                cudaEventRecord(e0, b->stream);
-                if ((rc = step_impl(b, nsteps, 0))) goto done;
-                cudaEventRecord(e1, b->stream);
-                if (cudaEventSynchronize(e1) != cudaSuccess) { rc = EMIX_ERR_CUDA; goto done; }
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
+                if ((rc = timed(&ms))) goto done;
                 if (ms < best_t) { best_t = ms; best = b->tune; }
             }
+    b->pcr_ms[0] = best_t;
+    for (int sp = 2; sp <= kPcrMaxSteps; ++sp) {
+        if ((rc = emix_batch_set_tuning(b, best.cpb, best.yz_bs, best.ctas_sm))) goto done;
+        if ((rc = emix_batch_set_pcr(b, sp))) goto done;
+        float ms = 0.f;
+        if ((rc = timed(&ms))) goto done;
+        b->pcr_ms[sp] = ms;
+        if (ms < best_t) { best_t = ms; best = b->tune; }
+    }
 done:
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    b->tune.pcr = best.pcr;
     rc = emix_batch_set_tuning(b, best.cpb, best.yz_bs, best.ctas_sm);
-    if (best_ms) *best_ms = best_t / nsteps;
+    if (best_ms) *best_ms = best_t;
     return rc;
+}
+
+int emix_batch_autotune_pcr_ms(emix_batch *b, double *ms) {
+    if (!b || !ms) return EMIX_ERR_ARG;
+    for (int k = 0; k <= kPcrMaxSteps; ++k) ms[k] = b->pcr_ms[k];
+    return EMIX_OK;
 }
 
 } // extern "C"

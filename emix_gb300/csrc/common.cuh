@@ -166,6 +166,28 @@ struct DerivTable {
     double sm1s;           // sm1 k_{n-1} (periodic)
 };
 
+// Parallel cyclic reduction (PCR) followed by Thomas, for one compact
+// operator: `steps` PCR steps split the system into 2^steps interleaved
+// subsystems (rows i = r (mod 2^steps)), each then solved by Thomas.  The
+// matrix side of every step and the subsystems' factors are precomputed; a
+// pencil costs per row the right-hand-side stencil, two FMAs per PCR step and
+// the three operations of the factored Thomas sweeps.  The cyclic scheme
+// solves the Sherman-Morrison-modified non-cyclic system A' and corrects by
+// zz = A'^{-1} u at the end.
+constexpr int kPcrMaxSteps = 5;
+constexpr int kPcrMaxN = 160;      // pencils of up to 160 rows (5 per lane at 5 steps)
+struct PcrTable {
+    int n, steps, periodic;
+    int nlo, nhi;               // closure rows at each end (non-cyclic schemes)
+    const double *ra, *rb;      // n: interior right-hand side (1/h folded in)
+    const double *cl;           // 4n: closure right-hand side (f_0..f_3 low, f_{n-1}..f_{n-4} high)
+    const double *al, *ga;      // steps x n: d_i += al d_{i-h} + ga d_{i+h}, h = 2^k
+    const double *ib, *mt, *gt; // n: Thomas of the subsystems: w = d ib - mt w_prev, x = w - gt x_next
+    const double *zz;           // n (cyclic): A'^{-1} u
+    double sm1, sm2;            // cyclic: fact = (y_0 + sm1 y_{n-1}) sm2, x = y - fact zz
+};
+int get_pcr_table(int scheme, int n, double h, int steps, PcrTable *out);
+
 // Build the table for (scheme, n, h); rows/u0/zz returned in host vectors.
 // Host arrays: rows[n], clo[kMaxClosure*4], chi[kMaxClosure*4], u0[n], zz[n].
 int build_deriv_table_host(int scheme, int n, double h, DerivTable &t, DerivRow *rows,

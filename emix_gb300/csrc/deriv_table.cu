@@ -279,6 +279,154 @@ int get_table_signed(int scheme, int n, double h, double sign, DerivTable *out) 
     return EMIX_OK;
 }
 
+// ---- PCR + Thomas tables ----------------------------------------------------
+
+namespace {
+
+struct PKey {
+    int dev, scheme, n, steps;
+    double h;
+    bool operator<(const PKey &o) const {
+        return std::tie(dev, scheme, n, steps, h) < std::tie(o.dev, o.scheme, o.n, o.steps, o.h);
+    }
+};
+
+std::mutex g_p_mu;
+std::map<PKey, PcrTable> g_p_tables;   // device buffers live until process exit
+
+} // namespace
+
+int get_pcr_table(int scheme, int n, double h, int steps, PcrTable *out) {
+    if (!(h > 0.0) || steps < 1 || steps > kPcrMaxSteps || n < 6 || n > kPcrMaxN) return EMIX_ERR_ARG;
+    int dev = 0;
+    EMIX_CUDA_TRY(cudaGetDevice(&dev));
+    PKey key{dev, scheme, n, steps, h};
+    std::lock_guard<std::mutex> lock(g_p_mu);
+    auto it = g_p_tables.find(key);
+    if (it != g_p_tables.end()) {
+        *out = it->second;
+        return EMIX_OK;
+    }
+    std::vector<RowDef> R;
+    if (define_rows(scheme, n, R)) return EMIX_ERR_ARG;
+    const bool per = scheme == EMIX_SCHEME_BPER;
+    PcrTable t{};
+    t.n = n; t.steps = steps; t.periodic = per ? 1 : 0;
+    // the non-cyclic matrix A' (the cyclic one with the Sherman-Morrison
+    // corners folded into the diagonal, derivada_incomp.f90:243-250)
+    std::vector<double> a(n), b(n), c(n);
+    for (int i = 0; i < n; ++i) { a[i] = R[i].a; b[i] = R[i].b; c[i] = R[i].c; }
+    double alpha = 0.0, beta = 0.0, gamma = 0.0;
+    if (per) {
+        alpha = R[0].a; beta = R[n - 1].c; gamma = -R[0].b;
+        b[0] = R[0].b - gamma;
+        b[n - 1] = R[n - 1].b - alpha * beta / gamma;
+    }
+    a[0] = 0.0;
+    c[n - 1] = 0.0;
+    // right-hand side, 1/h folded in
+    std::vector<double> ra(n, 0.0), rb(n, 0.0), cl(4 * (size_t)n, 0.0);
+    t.nlo = t.nhi = 0;
+    for (int i = 0; i < n; ++i) {
+        if (R[i].kind == 0) {
+            ra[i] = R[i].ars / h;
+            rb[i] = R[i].brs / h;
+        } else {
+            for (int q = 0; q < 4; ++q) cl[4 * i + q] = R[i].cc[q] / h;
+            if (R[i].kind == 1) ++t.nlo; else ++t.nhi;
+        }
+    }
+    // PCR on the matrix side
+    std::vector<double> al((size_t)steps * n), ga((size_t)steps * n);
+    for (int k = 0; k < steps; ++k) {
+        const int hs = 1 << k;
+        std::vector<double> a2(n), b2(n), c2(n);
+        for (int i = 0; i < n; ++i) {
+            const double am = i - hs >= 0 ? -a[i] / b[i - hs] : 0.0;
+            const double gp = i + hs < n ? -c[i] / b[i + hs] : 0.0;
+            al[(size_t)k * n + i] = am;
+            ga[(size_t)k * n + i] = gp;
+            a2[i] = i - hs >= 0 ? am * a[i - hs] : 0.0;
+            c2[i] = i + hs < n ? gp * c[i + hs] : 0.0;
+            b2[i] = b[i] + (i - hs >= 0 ? am * c[i - hs] : 0.0) + (i + hs < n ? gp * a[i + hs] : 0.0);
+            if (b2[i] == 0.0 || !std::isfinite(b2[i])) return EMIX_ERR_ARG;
+        }
+        a = a2; b = b2; c = c2;
+    }
+    // Thomas factors of each subsystem (rows r, r + H, r + 2H, ...)
+    const int H = 1 << steps;
+    std::vector<double> ib(n), mt(n), gt(n);
+    for (int r = 0; r < H && r < n; ++r) {
+        double bet = 0.0;
+        for (int i = r; i < n; i += H) {
+            if (i == r) {
+                bet = b[i];
+                mt[i] = 0.0;
+            } else {
+                const double gam = c[i - H] / bet;
+                bet = b[i] - a[i] * gam;
+                mt[i] = a[i] / bet;
+            }
+            if (bet == 0.0 || !std::isfinite(bet)) return EMIX_ERR_ARG;
+            ib[i] = 1.0 / bet;
+            gt[i] = c[i] / bet;
+        }
+    }
+    // cyclic correction: zz = A'^{-1} (gamma, 0, ..., 0, alpha) by plain Thomas
+    std::vector<double> zz(n, 0.0);
+    if (per) {
+        std::vector<double> A0(n), B0(n), C0(n), w(n), bet(n), gam(n, 0.0);
+        for (int i = 0; i < n; ++i) { A0[i] = R[i].a; B0[i] = R[i].b; C0[i] = R[i].c; }
+        B0[0] = R[0].b - gamma;
+        B0[n - 1] = R[n - 1].b - alpha * beta / gamma;
+        bet[0] = B0[0];
+        w[0] = gamma / bet[0];
+        for (int i = 1; i < n; ++i) {
+            gam[i] = C0[i - 1] / bet[i - 1];
+            bet[i] = B0[i] - A0[i] * gam[i];
+            const double ri = i == n - 1 ? alpha : 0.0;
+            w[i] = (ri - A0[i] * w[i - 1]) / bet[i];
+        }
+        zz[n - 1] = w[n - 1];
+        for (int i = n - 2; i >= 0; --i) zz[i] = w[i] - gam[i + 1] * zz[i + 1];
+        t.sm1 = beta / gamma;
+        t.sm2 = 1.0 / (1.0 + zz[0] + t.sm1 * zz[n - 1]);
+    }
+    // one allocation: ra | rb | cl | al | ga | ib | mt | gt | zz
+    const size_t nd = (size_t)n * (2 + 4 + 2 * steps + 4);
+    std::vector<double> host;
+    host.reserve(nd);
+    host.insert(host.end(), ra.begin(), ra.end());
+    host.insert(host.end(), rb.begin(), rb.end());
+    host.insert(host.end(), cl.begin(), cl.end());
+    host.insert(host.end(), al.begin(), al.end());
+    host.insert(host.end(), ga.begin(), ga.end());
+    host.insert(host.end(), ib.begin(), ib.end());
+    host.insert(host.end(), mt.begin(), mt.end());
+    host.insert(host.end(), gt.begin(), gt.end());
+    host.insert(host.end(), zz.begin(), zz.end());
+    double *buf = nullptr;
+    if (cudaMalloc(&buf, nd * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_message("cudaMalloc of a PCR table failed");
+        return EMIX_ERR_ALLOC;
+    }
+    EMIX_CUDA_TRY(cudaMemcpy(buf, host.data(), nd * sizeof(double), cudaMemcpyHostToDevice));
+    double *q = buf;
+    t.ra = q; q += n;
+    t.rb = q; q += n;
+    t.cl = q; q += 4 * (size_t)n;
+    t.al = q; q += (size_t)steps * n;
+    t.ga = q; q += (size_t)steps * n;
+    t.ib = q; q += n;
+    t.mt = q; q += n;
+    t.gt = q; q += n;
+    t.zz = q;
+    g_p_tables[key] = t;
+    *out = t;
+    return EMIX_OK;
+}
+
 // ---- transposed operator D^T = B^T A^{-T} (the adjoint's pencil solves) ----
 
 namespace {

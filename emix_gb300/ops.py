@@ -151,6 +151,19 @@ def deriv_dev(x, axis: int, h: float, scheme=SCHEME_C):
     return out
 
 
+def deriv_pcr_dev(x, axis: int, h: float, steps: int, scheme=SCHEME_C):
+    """deriv_dev along y or z by parallel cyclic reduction (steps 2..5) +
+    Thomas (emix_deriv_pcr_dev)."""
+    import torch
+    lib = _lib.load()
+    nx, ny, nz = _dims(x)
+    nf = 1 if x.dim() == 3 else x.shape[0]
+    out = torch.empty_like(x)
+    check(lib.emix_deriv_pcr_dev(scheme, axis, nf, _ptr(out), _ptr(x), h, steps, nx, ny, nz, _stream()),
+          "emix_deriv_pcr_dev")
+    return out
+
+
 def cudaDeriv_dev(vel, temp, h, schemes=SCHEME_C):
     import torch
     lib = _lib.load()
@@ -607,6 +620,26 @@ class Batch:
         check(self.lib.emix_batch_autotune(self._h, nsteps, C.byref(ms)), "emix_batch_autotune")
         self.upload()
         return ms.value
+
+    def set_pcr(self, steps: int):
+        """PCR steps (2..5) of the y/z pencil positions, 0 for Thomas sweeps."""
+        check(self.lib.emix_batch_set_pcr(self._h, steps), "emix_batch_set_pcr")
+
+    def pcr(self) -> int:
+        v = C.c_int()
+        check(self.lib.emix_batch_get_pcr(self._h, C.byref(v)), "emix_batch_get_pcr")
+        return v.value
+
+    def pcr_positions(self) -> int:
+        v = C.c_int()
+        check(self.lib.emix_batch_pcr_positions(self._h, C.byref(v)), "emix_batch_pcr_positions")
+        return v.value
+
+    def autotune_pcr_ms(self):
+        """{steps: ms per step} the last autotune measured (0: Thomas)."""
+        ms = (C.c_double * 6)()
+        check(self.lib.emix_batch_autotune_pcr_ms(self._h, ms), "emix_batch_autotune_pcr_ms")
+        return {k: ms[k] for k in (0, 2, 3, 4, 5) if ms[k] >= 0}
 
     def close(self):
         if self._h:

@@ -93,6 +93,16 @@ int emix_set_legacy_scheme(int scheme);
 int emix_deriv_dev(int scheme, int axis, int nf, double *out, const double *in,
                    double h, int nx, int ny, int nz, void *stream);
 
+/* emix_deriv_dev along y (axis 1) or z (axis 2) by parallel cyclic
+ * reduction + Thomas instead of one serial Thomas sweep per pencil
+ * (src/Schemes/derivCompact.cu:146-215 solves each pencil serially): steps =
+ * 2..5 PCR steps split each pencil over 2^steps lanes of a warp (partners
+ * exchanged by warp shuffles), each lane then solving its 2^-steps share by
+ * Thomas.  Pencils of at most 160 rows (EMIX_ERR_ARG otherwise).  The same
+ * operator as emix_deriv_dev to rounding.  Device pointers. */
+int emix_deriv_pcr_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                       int steps, int nx, int ny, int nz, void *stream);
+
 /* cudaDeriv with status, explicit per-axis schemes, host pointers. */
 int emix_cudaDeriv(const int schemes[3], double *dVel, double *dTemp,
                    const double *vel, const double *temp,
@@ -470,10 +480,27 @@ int emix_batch_step_per_grid(emix_batch *b, int nsteps, int use_graph);
 int emix_batch_set_tuning(emix_batch *b, int cells_per_thread, int yz_block, int ctas_per_sm);
 int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, int *ctas_per_sm);
 
-/* Autotuner: times every candidate tuning over nsteps batched steps and keeps
- * the fastest (advances the state; re-upload it afterwards).  best_ms may be
- * NULL. */
+/* y/z pencil positions of the batched step by parallel cyclic reduction +
+ * Thomas (emix_deriv_pcr_dev) with steps = 2..5 PCR steps, or 0 (default)
+ * by one Thomas sweep per pencil.  A position whose pencils exceed 160 rows
+ * in any grid keeps the Thomas sweep; emix_batch_pcr_positions counts the
+ * positions that run by PCR.  The gradients' y and z positions then run as
+ * two launches. */
+int emix_batch_set_pcr(emix_batch *b, int steps);
+int emix_batch_get_pcr(emix_batch *b, int *steps);
+int emix_batch_pcr_positions(emix_batch *b, int *count);
+
+/* Autotuner: times every candidate launch shape (cells per pointwise item,
+ * y/z block width, resident CTAs per SM) over nsteps batched steps with one
+ * Thomas sweep per pencil, then the best of them with 2..5 PCR steps in the
+ * y/z positions, and keeps the fastest (advances the state; re-upload it
+ * afterwards).  best_ms (may be NULL) receives the best ms per step. */
 int emix_batch_autotune(emix_batch *b, int nsteps, double *best_ms);
+
+/* ms per step the last emix_batch_autotune measured: ms[0] the best shape
+ * with Thomas sweeps, ms[k] (k = 2..5) the same shape with k PCR steps; -1
+ * where not measured.  ms holds 6 values. */
+int emix_batch_autotune_pcr_ms(emix_batch *b, double *ms);
 
 /* Diagnostic: measured FP64 fused-multiply-add throughput of the current
  * device in lane operations per second (a short dependent-chain kernel). */

@@ -64,3 +64,56 @@ def test_autotune_keeps_results(emix):
     for g in range(len(ws)):
         assert_close(b.download(g)[0], ref[g][0], tol=1e-13, what=f"grid {g}")
     b.close()
+
+
+@pytest.mark.parametrize("steps", [2, 3, 4, 5])
+def test_batched_pcr_matches_per_grid_and_oracle(emix, oracle, steps):
+    """The batched step with its y/z positions by PCR + Thomas: every y/z
+    position runs by PCR (the grids' pencils are at most 160 rows), the
+    result agrees with the per-grid Thomas steps to rounding (1e-12) and
+    with the oracle at 1e-12; a grid with longer pencils keeps Thomas."""
+    ws = F.ensemble(ngrids=4, seed=13, sizes=(16, 40, 48))
+    b = emix.Batch(ws)
+    b.step_per_grid(2)
+    ref = [b.download(g) for g in range(len(ws))]
+    b.upload()
+    b.set_pcr(steps)
+    assert b.pcr() == steps
+    assert b.pcr_positions() == 12   # per substep: gradients y, z; divergence y, z
+    for use_graph in (False, True):
+        b.upload()
+        b.step(2, use_graph=use_graph)
+        for g in range(len(ws)):
+            um, phi = b.download(g)
+            assert_close(um, ref[g][0], what=f"grid {g} um, {steps} PCR steps")
+            assert_close(phi, ref[g][1], what=f"grid {g} phi, {steps} PCR steps")
+    w = ws[0]
+    p = oracle.step_params(w)
+    d, r = oracle.inisgdm(np.ascontiguousarray(w.grid.coords()))
+    rum, rphi = oracle.step(p, w.um, w.phi, w.jbn, w.mask, d, r, nsteps=2)
+    um, phi = b.download(0)
+    # per field, except the w-momentum: its largest value is the 1e-3 noise of
+    # this Taylor-Green family, where one ulp of input already moves it by
+    # ~2e-12 after a step (tests/test_oracle_pins.py); all five fields together
+    assert_close(um, rum, what="um against the oracle")
+    for m in (0, 1, 2, 4):
+        assert_close(um[m], rum[m], what=f"um[{m}] against the oracle")
+    assert_close(phi, rphi, what="phi against the oracle")
+    b.close()
+    long = F.ensemble(ngrids=2, seed=13, sizes=(16,)) + [F.random_box(16, 168, 16, seed=3, periodic=True)]
+    for w in long:
+        w.sgs_model = 1
+    b = emix.Batch(long)
+    b.set_pcr(steps)
+    assert b.pcr_positions() == 6    # the y positions keep Thomas (168 rows)
+    b.close()
+
+
+def test_autotune_measures_pcr_depths(emix):
+    ws = _grids(1)
+    b = emix.Batch(ws)
+    b.autotune(nsteps=1)
+    ms = b.autotune_pcr_ms()
+    assert sorted(ms) == [0, 2, 3, 4, 5] and all(v > 0 for v in ms.values())
+    assert b.pcr() in (0, 2, 3, 4, 5)
+    b.close()
