@@ -37,14 +37,19 @@ struct emix_ctx {
     cudaEvent_t prof_ev[2 * 64] = {};
     int prof_cls[64] = {};
     std::vector<emix::Launch> plan;   // one RK3 step
-    // optionally (emix_ctx_set_overlap) the level-set stages run on a second
-    // stream, concurrently with the flow's kernels of the same substep (fork
-    // before the stage, join before the RK update that overwrites the velocity
-    // the stage reads).  Off by default: both sides are FP64-bound and fill
-    // the GPU, and the overlap measured no gain.
+    // the level-set stages run on a second stream, concurrently with the
+    // flow's kernels of the same substep (fork before the stage, join before
+    // the RK update that overwrites the velocity the stage reads), and so do
+    // the x gradients beside the y and z gradients: both fill the launch tails
+    // of the other stream's FP64-bound kernels (emix_ctx_set_overlap; on by
+    // default for level-set contexts)
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
-    bool overlap = false;
+    // bit 1: the level-set stages on `side`; bit 2: each substep's x
+    // gradients on `side`, concurrent with its y and z gradients (joined
+    // before the first launch that reads them)
+    int overlap = 0;
+    cudaEvent_t gfork_ev[3] = {}, gjoin_ev[3] = {};
     // pairs of records run as one launch (plan_fuse_next; emix_ctx_set_fusion)
     bool fuse = true;
     // the level-set stages' plane tiles by TMA (emix_ctx_set_tma; on by

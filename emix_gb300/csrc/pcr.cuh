@@ -49,6 +49,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
     const int x = x0 + (lane >> S);
     const bool live = x < nx && o < nother;
     const int n = P.n;
+    const int m = (n + H - 1) >> S;   // slots in use (<= M; the same in every lane)
     const long off = (long)(live ? x : 0) + (long)(live ? o : 0) * os;
     const double *__restrict__ in = pick(F.in, fi) + off;
     double *out = pick(F.out, fi) + off;
@@ -57,7 +58,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
 #pragma unroll
     for (int t = 0; t < M; ++t) {
         const int i = r + H * t;
-        d[t] = (live && i < n) ? pcr_rhs(P, in, s, i) : 0.0;
+        d[t] = (t < m && live && i < n) ? pcr_rhs(P, in, s, i) : 0.0;
     }
     // PCR: d_i += al_i d_{i-h} + ga_i d_{i+h}, h = 2^k.  Row i - h lives in
     // lane r - h (slot t) or, for r < h, lane r - h + H (slot t - 1); row
@@ -73,6 +74,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
         double prev = 0.0;
 #pragma unroll
         for (int t = 0; t < M; ++t) {
+            if (t >= m) break;
             const int i = r + H * t;
             const double nxt = t + 1 < M ? d[t + 1] : 0.0;
             const double a0 = __shfl_sync(0xffffffffu, d[t], lo);
@@ -89,6 +91,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
     double w = 0.0;
 #pragma unroll
     for (int t = 0; t < M; ++t) {
+        if (t >= m) break;
         const int i = r + H * t;
         if (i < n) {
             w = fma(-P.mt[i], w, d[t] * P.ib[i]);
@@ -99,7 +102,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
 #pragma unroll
     for (int t = M - 1; t >= 0; --t) {
         const int i = r + H * t;
-        if (i < n) {
+        if (t < m && i < n) {
             xv = d[t] - P.gt[i] * xv;
             d[t] = xv;
         }
@@ -116,6 +119,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
         const double fact = (y0 + P.sm1 * yn) * P.sm2;
 #pragma unroll
         for (int t = 0; t < M; ++t) {
+            if (t >= m) break;
             const int i = r + H * t;
             if (i < n) d[t] -= fact * P.zz[i];
         }
@@ -123,6 +127,7 @@ EMIX_DEV void pcr_yz_warp(const PcrTable &P, const PencilFields &F, int nx, int 
     if (!live) return;
 #pragma unroll
     for (int t = 0; t < M; ++t) {
+        if (t >= m) break;
         const int i = r + H * t;
         if (i < n) {
             double v = d[t];

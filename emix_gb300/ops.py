@@ -455,8 +455,11 @@ class Context:
     def step(self, nsteps=1, use_graph=False):
         check(self.lib.emix_step(self._h, nsteps, 1 if use_graph else 0), "emix_step")
 
-    def set_overlap(self, on: bool):
-        check(self.lib.emix_ctx_set_overlap(self._h, 1 if on else 0), "emix_ctx_set_overlap")
+    def set_overlap(self, on):
+        """Concurrency inside a step: False/0 one stream; True/1 the level-set
+        stages on a second stream; 2 the x gradients on it; 3 both."""
+        mode = int(on) if not isinstance(on, bool) else (1 if on else 0)
+        check(self.lib.emix_ctx_set_overlap(self._h, mode), "emix_ctx_set_overlap")
 
     def set_fusion(self, on: bool):
         """Run the gradients' y and z passes, and Smagorinsky with the fluxes,

@@ -358,13 +358,19 @@ typedef struct emix_ctx emix_ctx;
 int emix_ctx_create(const emix_params *p, emix_ctx **out);
 int emix_ctx_destroy(emix_ctx *ctx);
 
-/* Stream the context launches on (NULL = the legacy default stream). */
+/* Stream the context launches on (NULL = the context's own stream). */
 int emix_ctx_set_stream(emix_ctx *ctx, void *stream);
 
-/* 1: each level-set stage runs on a second stream of the context,
- * concurrently with the flow's kernels of its substep (joined before the RK
- * update); 0 (default): one stream.  Results are the same either way; on a
- * GB300 both sides are FP64-bound and the overlap gains nothing measurable. */
+/* Concurrency inside a step, a bit mask (0 = one stream; 3, both bits, is
+ * the default of level-set contexts, 0 of the others):
+ * bit 1 (value 1): each level-set stage runs on a second stream of the
+ * context, concurrently with the flow's kernels of its substep (joined before
+ * the RK update); bit 2 (value 2): each substep's x gradients run on the
+ * second stream concurrently with its y and z gradients (joined before the
+ * first launch that reads them).  Results are the same bit for bit in every
+ * mode (only level-set contexts have the second stream).  On the 256^3 tank
+ * both bits together gain 1% (the concurrent launches fill each other's last
+ * waves). */
 int emix_ctx_set_overlap(emix_ctx *ctx, int on);
 
 /* 1 (default): the gradients' y and z passes run as one launch, and so do

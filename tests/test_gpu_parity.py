@@ -270,13 +270,16 @@ def test_step(emix, oracle, kind, level_set):
 
 
 @pytest.mark.gpu
-def test_overlapped_level_set_stream_gives_the_same_bits(emix):
-    """The level-set stages on a second stream and on the context's one
-    stream (the default) give identical results."""
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_overlapped_streams_give_the_same_bits(emix, mode):
+    """The level-set stages (mode 1), the x gradients (mode 2) or both on a
+    second stream, and the context's one stream (the default), give
+    identical results."""
     w = F.stirred_tank(n=24, impeller=True)
     a = emix.Context(w, bc_walls=1)
     b = emix.Context(w, bc_walls=1)
-    a.set_overlap(True)
+    a.set_overlap(mode)
+    b.set_overlap(0)
     for use_graph in (False, True):
         a.upload(w.um, w.phi); a.time = 0.0
         b.upload(w.um, w.phi); b.time = 0.0

@@ -6,10 +6,11 @@ its last step moves the last
 level-set stage after the last RK update, copies um back by z-slabs of that
 update and phi by z-slabs of the stage.  The cases below cover one, two and
 three steps, walls and the periodic box, uneven and shallow z extents (fewer
-upload slabs), the forms that copy plainly instead (the level-set overlap
-on, the impeller's blade-edge interpolation after the RK update, no level
-set), a filter step last (uploads overlapped, copies after the filter) and
-pageable host buffers."""
+upload slabs), the context's steps on one stream and with the level-set
+stages alone on the second, the forms that copy plainly instead (the
+impeller's blade-edge interpolation after the RK update, no level set), a
+filter step last (uploads overlapped, copies after the filter) and pageable
+host buffers."""
 import numpy as np
 import pytest
 
@@ -34,12 +35,12 @@ def _device(w, nsteps, **kw):
     return um, phi, idx
 
 
-def _host(w, nsteps, pinned=True, overlap=False, level_set=True, **kw):
+def _host(w, nsteps, pinned=True, overlap=None, level_set=True, **kw):
     import torch
     from emix_gb300 import ops
     ctx = ops.Context(w, level_set=level_set, **kw)
-    if overlap:
-        ctx.set_overlap(True)
+    if overlap is not None:
+        ctx.set_overlap(overlap)
     um_t = torch.from_numpy(np.ascontiguousarray(w.um))
     phi_t = torch.from_numpy(np.ascontiguousarray(w.phi))
     if pinned:
@@ -85,8 +86,8 @@ def test_step_host_shapes(case):
         assert np.array_equal(hphi, phi), f"{case}, {nsteps} steps: phi"
 
 
-@pytest.mark.parametrize("case", ["overlap", "filter_last", "interp", "no_level_set"])
-def test_step_host_forms_without_the_tail_copies(case):
+@pytest.mark.parametrize("case", ["one_stream", "stages_only", "filter_last", "interp", "no_level_set"])
+def test_step_host_forms(case):
     kw = {"bc_walls": 1}
     w = _tank(interp=1 if case == "interp" else 0)
     nsteps = 3 if case == "filter_last" else 2
@@ -101,7 +102,8 @@ def test_step_host_forms_without_the_tail_copies(case):
         kw.update(filter_every=2, cfilt=0.2)   # steps 0 and 2 filter: the last one does
     ls = case != "no_level_set"
     um, phi, idx = _device(w, nsteps, level_set=ls, **kw)
-    hum, hphi, hidx = _host(w, nsteps, overlap=case == "overlap", level_set=ls, **kw)
+    ov = {"one_stream": 0, "stages_only": 1}.get(case)
+    hum, hphi, hidx = _host(w, nsteps, overlap=ov, level_set=ls, **kw)
     assert hidx == idx == nsteps
     assert np.array_equal(hum, um)
     if ls:
