@@ -12,6 +12,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libemix_gb300.so"
 
 EMIX_OK = 0
+EMIX_ERR_ALLOC = 3
 STATUS_NAMES = {0: "EMIX_OK", 1: "EMIX_ERR_ARG", 2: "EMIX_ERR_CUDA", 3: "EMIX_ERR_ALLOC",
                 4: "EMIX_ERR_UNSUPPORTED", 5: "EMIX_ERR_TIMEOUT"}
 

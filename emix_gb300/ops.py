@@ -724,7 +724,12 @@ class TankGradient:
     def __init__(self, workload, nsteps, every=1, objective=None, **ctx_kw):
         self.workload = workload
         self.ctx = Context(workload, **ctx_kw)
-        self.adj = Adjoint(self.ctx, nsteps, every, objective or tank_objective(workload))
+        try:
+            self.adj = Adjoint(self.ctx, nsteps, every, objective or tank_objective(workload))
+        except Exception:
+            # the adjoint's arena did not fit: release the context's before raising
+            self.ctx.close()
+            raise
 
     def run(self, omega: float, cs: float) -> float:
         w = self.workload

@@ -96,8 +96,12 @@ def operators(n: int, passes: int = 2) -> None:
     velg = torch.stack([ops.ghost_pad_dev(u[d].contiguous(), g) for d in range(3)]).contiguous()
     jbng = torch.stack([ops.ghost_pad_dev(jbn[c].contiguous(), g) for c in range(11)]).contiguous()
     dmins = torch.full_like(phig, min(hs))
+    # the PCR form takes pencils of at most 160 rows: y and z cut to 160
+    m = min(n, 160)
+    us = u[:, :m, :m, :].contiguous()
     for _ in range(passes):
         ops.deriv_dev(u, 0, hs[0], F.SCHEME_B)
+        ops.deriv_pcr_dev(us, 1, hs[1], 3, F.SCHEME_B)
         ops.deriv_t_dev(u, 1, hs[1], F.SCHEME_B)
         dvel, dtemp = ops.cudaDeriv_dev(u, um[4].contiguous(), hs, F.SCHEME_C)
         dxyz, ratios = ops.sgs_setup_dev(xyz)
