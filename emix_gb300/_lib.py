@@ -128,6 +128,10 @@ PROTOTYPES = {
     "emix_ctx_tma_stages": (C.c_int, [vp]),
     "emix_weno_tma_timeouts": (C.c_int, [C.POINTER(C.c_int)]),
     "emix_weno_tma_test_drop": (C.c_int, [C.c_int]),
+    "emix_ctx_set_pencil_tma": (C.c_int, [vp, C.c_int]),
+    "emix_ctx_pencil_tma_launches": (C.c_int, [vp]),
+    "emix_pencil_tma_timeouts": (C.c_int, [C.POINTER(C.c_int)]),
+    "emix_pencil_tma_test_drop": (C.c_int, [C.c_int]),
     "emix_ctx_get_step_index": (C.c_int, [vp, C.POINTER(C.c_long)]),
     "emix_ctx_set_step_index": (C.c_int, [vp, C.c_long]),
     "emix_ctx_set_time": (C.c_int, [vp, C.c_double]),

@@ -10,6 +10,7 @@
 
 #include "boundary.cuh"
 #include "deriv.cuh"
+#include "deriv_tma.cuh"
 #include "pointwise.cuh"
 #include "weno.cuh"
 
@@ -54,6 +55,7 @@ struct Launch {
         ImpInterpArgs interp;
     };
     const CUtensorMap *tmap;   // LK_WENO: plane tiles by TMA (null: register-staged loads)
+    const PencilMaps *pmaps;   // LK_DERIV_YZ accumulating: rows by TMA (null: loads)
 };
 
 int launch_single(const Launch &L, cudaStream_t st);

@@ -48,6 +48,9 @@ int launch_single(const Launch &L, cudaStream_t st) {
         return launch_weno_stage(L.weno, st, L.tmap);
     case LK_DERIV_X:
     case LK_DERIV_YZ:
+        if (L.pmaps)
+            return launch_deriv_yz_tma(L.deriv.T, *L.pmaps, L.deriv.axis, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
+                                       L.deriv.F.out, L.deriv.nx, L.deriv.ny, L.deriv.nz, st);
         return launch_deriv(L.deriv.T, L.deriv.axis, L.deriv.epi, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
                             L.deriv.F.out, L.deriv.nx, L.deriv.ny, L.deriv.nz, st);
     case LK_SMAG:
@@ -242,10 +245,15 @@ void build_plan(emix_ctx *c) {
                 out[m] = c->R + m * n;
                 wb[m] = c->W + m * n;
             }
-            if (ax == 0)
+            if (ax == 0) {
                 P.push_back(deriv_launch(c->T[ax], ax, EPI_STORE, 5, in, out, out, nx, ny, nz, CLS_DIVX));
-            else
+            } else {
                 P.push_back(deriv_launch(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, CLS_DIVX + ax));
+                // rows by TMA where the copy unit's rules hold (closed tables)
+                PencilMaps *pm = &c->pmaps[2 * (s - 1) + (ax - 1)];
+                if (c->pencil_tma && !c->T[ax].periodic && pencil_tma_maps(pm, ax, 5, in, wb, out, nx, ny, nz))
+                    P.back().pmaps = pm;
+            }
         }
         // RK update and conversions; with walls the boundary conditions go
         // between the RK combination and the conversions (rungek_ico.f90:98-104):
@@ -781,6 +789,20 @@ int emix_ctx_tma_stages(emix_ctx *c) {
     return k;
 }
 
+int emix_ctx_set_pencil_tma(emix_ctx *c, int on) {
+    if (!c || (on != 0 && on != 1)) return EMIX_ERR_ARG;
+    c->pencil_tma = on == 1;
+    ctx_rebuild_plan(c);
+    return EMIX_OK;
+}
+
+int emix_ctx_pencil_tma_launches(emix_ctx *c) {
+    if (!c) return -1;
+    int k = 0;
+    for (const Launch &L : c->plan) k += (L.kind == LK_DERIV_YZ && L.pmaps) ? 1 : 0;
+    return k;
+}
+
 int emix_ctx_set_overlap(emix_ctx *c, int on) {
     if (!c || on < 0 || on > 3) return EMIX_ERR_ARG;
     c->overlap = on;
@@ -972,13 +994,19 @@ static int step_host_run(emix_ctx *c, double *um, double *phi, int nsteps) {
 int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
     if (!c || !um || nsteps < 0) return EMIX_ERR_ARG;
     if (c->p.level_set && !phi) return EMIX_ERR_ARG;
-    // a level-set stage block whose bounded TMA waits ran out leaves its cells
-    // unwritten: the timeout counter is read before and after the steps, and
-    // a rise is returned as an error
+    // a block whose bounded TMA waits ran out (a level-set stage block, or a
+    // divergence pencil block) leaves its cells unwritten: the timeout
+    // counters are read before and after the steps, and a rise is returned as
+    // an error
     const bool tma_stages = emix_ctx_tma_stages(c) > 0;
-    int tmo0 = 0;
+    const bool tma_pencils = emix_ctx_pencil_tma_launches(c) > 0;
+    int tmo0 = 0, pto0 = 0;
     if (tma_stages) {
         int rc = emix_weno_tma_timeouts(&tmo0);
+        if (rc) return rc;
+    }
+    if (tma_pencils) {
+        int rc = emix_pencil_tma_timeouts(&pto0);
         if (rc) return rc;
     }
     int rc = step_host_run(c, um, phi, nsteps);
@@ -990,6 +1018,16 @@ int emix_step_host(emix_ctx *c, double *um, double *phi, int nsteps) {
         if (tmo1 != tmo0) {
             set_last_message("emix_step_host: level-set stage blocks gave up waiting for their TMA "
                              "plane copies; phi is incomplete");
+            return EMIX_ERR_TIMEOUT;
+        }
+    }
+    if (tma_pencils) {
+        int pto1 = 0;
+        rc = emix_pencil_tma_timeouts(&pto1);
+        if (rc) return rc;
+        if (pto1 != pto0) {
+            set_last_message("emix_step_host: divergence pencil blocks gave up waiting for their TMA "
+                             "row copies; um is incomplete");
             return EMIX_ERR_TIMEOUT;
         }
     }

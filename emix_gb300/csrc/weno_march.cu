@@ -4,7 +4,6 @@
 // by register-staged loads otherwise.
 #include "weno_march.cuh"
 
-#include <cudaTypedefs.h>   // PFN_cuTensorMapEncodeTiled
 
 #include <atomic>
 #include <cstring>
@@ -23,22 +22,6 @@ __global__ void __launch_bounds__(kNT, 4) k_weno_march_tma(const __grid_constant
     weno_march_body_t<true>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.z, &tmap);
 }
 
-// cuTensorMapEncodeTiled from the driver, fetched once through the runtime
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            cudaGetLastError();
-    });
-    return fn;
-}
 
 // resident blocks per SM x SMs of a stage kernel on the current device
 // (queried once per kernel and device ordinal)
@@ -65,11 +48,27 @@ std::atomic<int> g_res_plain[64], g_res_tma[64];
 
 } // namespace
 
+PFN_cuTensorMapEncodeTiled_v12000 tma_encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
 bool weno_tma_map(CUtensorMap *m, const WenoArgs &a) {
     const int nxg = a.nxg, nyg = a.nyg, nzg = a.nzg;
     if ((reinterpret_cast<uintptr_t>(a.phi) & 15) != 0 || (nxg & 1) != 0 || nxg < kTW || nyg < kTY)
         return false;
-    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tma_encode_fn();
     if (!fn) return false;
     const cuuint64_t dim[3] = {(cuuint64_t)nxg, (cuuint64_t)nyg, (cuuint64_t)nzg};
     const cuuint64_t stride[2] = {(cuuint64_t)nxg * 8, (cuuint64_t)nxg * nyg * 8};

@@ -17,6 +17,7 @@
 //     planes near the z faces read them from global memory (weno_z_general).
 #pragma once
 
+#include "tma.cuh"
 #include "weno.cuh"
 
 namespace emix {
@@ -133,24 +134,6 @@ EMIX_DEV void load_plane(const double *__restrict__ phi, int x0, int y0, int Z, 
 constexpr int kTW = kPX + 2;                        // 24 doubles: 192 bytes per row
 constexpr int kTY = kPY;                            // 22 rows
 constexpr unsigned kTileBytes = kTW * kTY * 8;      // 4224
-constexpr long kTmaWaitLimit = 1L << 22;            // polls (with 64 ns pauses) before giving up
-
-EMIX_DEV unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-// bounded wait for phase `parity` of the mbarrier at shared address bar:
-// non-blocking tests with 64 ns pauses, about 0.3 s in all before giving up
-EMIX_DEV bool mbar_wait(unsigned bar, unsigned parity) {
-    for (long it = 0; it < kTmaWaitLimit; ++it) {
-        unsigned done;
-        asm volatile("{\n\t.reg .pred p;\n\t"
-                     "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-        if (done) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
 
 // one thread: expect the tile's bytes on bar, then copy the box at (x, y, z)
 EMIX_DEV void tma_plane(const void *tmap, unsigned dst, unsigned bar, int x, int y, int z) {

@@ -383,6 +383,13 @@ def ghost_unpad_dev(ghost, g):
     return out
 
 
+def pencil_tma_timeouts() -> int:
+    """Pencil blocks that gave up waiting for a TMA row copy (0 in a correct run)."""
+    out = C.c_int()
+    check(_lib.load().emix_pencil_tma_timeouts(C.byref(out)), "emix_pencil_tma_timeouts")
+    return out.value
+
+
 def weno_tma_timeouts() -> int:
     """Level-set stage blocks that gave up waiting for a TMA plane copy (0 in a correct run)."""
     out = C.c_int()
@@ -474,6 +481,13 @@ class Context:
 
     def tma_stages(self) -> int:
         return int(self.lib.emix_ctx_tma_stages(self._h))
+
+    def set_pencil_tma(self, on: bool):
+        """The divergence's y/z passes with their rows staged by TMA (same values)."""
+        check(self.lib.emix_ctx_set_pencil_tma(self._h, 1 if on else 0), "emix_ctx_set_pencil_tma")
+
+    def pencil_tma_launches(self) -> int:
+        return int(self.lib.emix_ctx_pencil_tma_launches(self._h))
 
     @property
     def time(self) -> float:

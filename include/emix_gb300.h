@@ -391,6 +391,28 @@ int emix_ctx_tma_stages(emix_ctx *ctx);
  * unwritten; 0 in every correct run. */
 int emix_weno_tma_timeouts(int *count);
 
+/* 1: the flux divergence's y and z passes (the accumulating pencil sweeps)
+ * bring the rows they read into shared memory by TMA tiled copies (4 rows x
+ * 128 pencils per copy, a ring of three), where the copy unit's rules hold
+ * (closed schemes, nx even, 16-byte aligned fields); 0: the threads load
+ * them.  The values are the same either way.  emix_ctx_pencil_tma_launches
+ * gives how many of the step's launches use the copies.  The reference
+ * transposes each field and walks each pencil serially
+ * (src/Schemes/derivCompact.cu:8-37,146-215). */
+int emix_ctx_set_pencil_tma(emix_ctx *ctx, int on);
+int emix_ctx_pencil_tma_launches(emix_ctx *ctx);
+
+/* Pencil blocks (since the library was loaded, on the current device) that
+ * gave up waiting for a row copy after about 0.3 s and left their pencils
+ * unwritten; 0 in every correct run. */
+int emix_pencil_tma_timeouts(int *count);
+
+/* Test hook for those bounded waits: 1 makes the TMA pencil launches issue
+ * no copies (current device), so every block gives up after its wait, counts
+ * itself and leaves its pencils; 0 restores normal operation.  Never set in a
+ * production run. */
+int emix_pencil_tma_test_drop(int on);
+
 /* Test hook for the bounded waits: 1 makes the TMA level-set stages issue no
  * plane copies (current device), so every stage block gives up after its
  * waits (about a second), counts itself and leaves its cells unwritten; the

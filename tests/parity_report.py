@@ -1,9 +1,10 @@
 """Per-output parity of the CUDA library: the normwise relative L-inf error of
 every output against the CPU oracle (and, for the operators the reference
 also has in CUDA, against the reference kernels' own recorded outputs in
-tests/golden/reference_cuda.npz).  The tests assert the bar (1e-12, 1e-11
-after several nonlinear steps); this prints the errors themselves as a
-markdown table.  Needs a GPU:
+tests/golden/reference_cuda.npz).  The tests assert the bar (1e-12; for the
+Taylor-Green w-momentum, twice the oracle's own spread under one ulp of input
+perturbation); this prints the errors themselves as a markdown table.  Needs
+a GPU:
 
     python tests/parity_report.py
 """
@@ -127,6 +128,51 @@ def main() -> int:
     row("step x3, tank 24^3 walls + impeller: um (5 fields, max)", "oracle",
         max(relerr(got_um[m], rum[m]) for m in range(5)))
     row("step x3, tank 24^3 walls + impeller: phi", "oracle", relerr(got_phi, rphi))
+    # the Taylor-Green box per field, beside the oracle's own spread when its
+    # inputs move by one ulp (seeded directions)
+    w = F.taylor_green(64)
+    ctx = E.Context(w, level_set=True)
+    ctx.step(10, use_graph=True)
+    got_um, got_phi = ctx.download()
+    ctx.close()
+    p = O.step_params(w, level_set=True)
+    dx, rt = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
+    rum, rphi = O.step(p, w.um, w.phi, w.jbn, w.mask, dx, rt, nsteps=10)
+
+    def nudged(x, seed):
+        d = np.random.default_rng(seed).integers(0, 2, size=x.shape).astype(bool)
+        return np.where(d, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
+
+    sum_, _ = O.step(p, nudged(w.um, 5), nudged(w.phi, 6), w.jbn, w.mask, dx, rt, nsteps=10)
+    for m in range(5):
+        row(f"step x10, Taylor-Green 64^3: um[{m}]", "oracle", relerr(got_um[m], rum[m]))
+        row(f"step x10, Taylor-Green 64^3: um[{m}]", "oracle with inputs moved by one ulp", relerr(sum_[m], rum[m]))
+    # the benchmark's own sizes: the 256^3 tank one step through the host-buffer
+    # entry point, the 128^3 tank 8 steps through the device context
+    for n, nsteps in ((256, 1), (128, 8)):
+        w = F.stirred_tank(n=n, impeller=True)
+        ctx = E.Context(w, level_set=True, ls_ghost=5, bc_walls=1)
+        if nsteps == 1:
+            got_um = np.ascontiguousarray(w.um.copy())
+            got_phi = np.ascontiguousarray(w.phi.copy())
+            ctx.step_host(got_um, got_phi, 1)
+        else:
+            ctx.step(nsteps, use_graph=True)
+            got_um, got_phi = ctx.download()
+        ctx.close()
+        p = O.step_params(w, level_set=True, bc_walls=1)
+        dx, rt = O.inisgdm(np.ascontiguousarray(w.grid.coords()))
+        rum, rphi = O.step(p, w.um, w.phi, w.jbn, w.mask, dx, rt, nsteps=nsteps)
+        for m in range(5):
+            row(f"step x{nsteps}, tank {n}^3 walls + impeller: um[{m}]", "oracle", relerr(got_um[m], rum[m]))
+        row(f"step x{nsteps}, tank {n}^3 walls + impeller: phi", "oracle", relerr(got_phi, rphi))
+    # the y/z derivative by PCR + Thomas
+    w = F.random_box(24, 48, 40, seed=31)
+    f = np.ascontiguousarray(w.um[1:4])
+    for steps in (2, 3, 4, 5):
+        got = host(E.deriv_pcr_dev(dev(f), 1, w.grid.h(1), steps, F.SCHEME_B))
+        e = max(relerr(got[c], O.deriv3d(F.SCHEME_B, 1, f[c], w.grid.h(1))) for c in range(3))
+        row(f"D by PCR ({steps} steps) + Thomas, scheme B, axis y (24x48x40, 3 fields)", "oracle", e)
     # against the reference's own CUDA kernels
     gold_path = HERE / "golden" / "reference_cuda.npz"
     spec = importlib.util.spec_from_file_location("mg", HERE / "golden" / "make_reference_golden.py")
