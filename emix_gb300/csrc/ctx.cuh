@@ -56,10 +56,11 @@ struct emix_ctx {
     // default where the copy unit's alignment rules hold), one map per stage
     bool tma = true;
     CUtensorMap weno_tmap[3];
-    // the divergence's y and z passes with their rows by TMA
-    // (emix_ctx_set_pencil_tma), one set of maps per substep and axis
-    bool pencil_tma = false;
-    emix::PencilMaps pmaps[6];
+    // the divergence's y and z passes and the gradients' fused y + z launch
+    // with their rows by TMA (emix_ctx_set_pencil_tma): maps per substep,
+    // [2s + a] the divergence along axis a + 1, [6 + s] the gradients
+    bool pencil_tma = true;
+    emix::PencilMaps pmaps[9];
     // emix_step_host's own issue of its first and last steps
     // (issue_step_host, step.cu): the uploads and the copies back on `side`,
     // overlapped with the step by z-slabs; the events it orders them with

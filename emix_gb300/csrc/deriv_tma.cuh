@@ -1,15 +1,16 @@
 // deriv_tma.cuh -- y/z pencil sweeps with their rows staged by TMA
 // (deriv_tma.cu).
 //
-// The accumulating y/z derivative (out += D f, the flux divergence's y and z
-// passes) of deriv_yz_accum with the same arithmetic, but every row the
-// sweeps read comes through shared memory: a block of 32, 64 or 128 pencils
-// (lanes along x) has one thread issue 3-D tiled copies of 4 rows x the
-// block's pencils (4 KB at 128) into a ring of three buffers, completion on
-// an mbarrier per buffer; the forward sweep reads f from the ring, the
-// backward sweep w and the accumulation target.  Every wait is bounded: a block whose copy does not
-// arrive counts itself (emix_pencil_tma_timeouts), waits (bounded) for the
-// copies it still has in flight and leaves its pencils unwritten.
+// The y/z derivative (out += D f, the flux divergence's y and z passes, or
+// out = D f, the velocity gradients' y and z passes as one launch) of the
+// load kernels with the same arithmetic, but every row the sweeps read comes
+// through shared memory: a block of 32, 64 or 128 pencils (lanes along x)
+// has one thread issue 3-D tiled copies of 4 rows x the block's pencils
+// (4 KB at 128) into a ring of three buffers, completion on an mbarrier per
+// buffer; the forward sweep reads f from the ring, the backward sweep w (and
+// the accumulation target).  Every wait is bounded: a block whose copy does
+// not arrive counts itself (emix_pencil_tma_timeouts), waits (bounded) for
+// the copies it still has in flight and leaves its pencils unwritten.
 #pragma once
 
 #include "deriv.cuh"
@@ -27,17 +28,22 @@ constexpr int kPtS = 3;     // buffers in the ring
 // 128, the block's threads) is the one that idles the fewest lanes of a row
 struct PencilMaps {
     CUtensorMap in[kMaxFields], w[kMaxFields], out[kMaxFields];
+    int axis[kMaxFields];   // 1 (y) or 2 (z) per field
     int width;
 };
 
-// Encodes the maps; false where the copy unit's rules do not hold (nx odd, a
-// field not 16-byte aligned) or the driver lacks the encoder.
-bool pencil_tma_maps(PencilMaps *M, int axis, int nf, const double *const *in, double *const *w,
+// Encodes the maps of nf fields, field f along axis[f]; false where the copy
+// unit's rules do not hold (nx odd, a field not 16-byte aligned) or the
+// driver lacks the encoder.
+bool pencil_tma_maps(PencilMaps *M, const int *axis, int nf, const double *const *in, double *const *w,
                      double *const *out, int nx, int ny, int nz);
 
-// out += D in along axis 1 or 2 for a closed (non-cyclic) table, rows staged
-// by TMA through the maps M (fields as in launch_deriv).
-int launch_deriv_yz_tma(const DerivTable &T, const PencilMaps &M, int axis, int nf, const double *const *in,
-                        double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st);
+// D in along each field's axis for closed (non-cyclic) tables, rows staged
+// by TMA through the maps M: out += D in (EPI_ACCUM) or out = D in
+// (EPI_STORE, w = out); fields [0, nfa) with table Ta, the rest with Tb
+// (fields as in launch_deriv).
+int launch_deriv_yz_tma(const DerivTable &Ta, const DerivTable &Tb, const PencilMaps &M, int epi, int nfa, int nf,
+                        const double *const *in, double *const *w, double *const *out, int nx, int ny, int nz,
+                        cudaStream_t st);
 
 } // namespace emix

@@ -56,6 +56,7 @@ struct Launch {
     };
     const CUtensorMap *tmap;   // LK_WENO: plane tiles by TMA (null: register-staged loads)
     const PencilMaps *pmaps;   // LK_DERIV_YZ accumulating: rows by TMA (null: loads)
+    const PencilMaps *pair_pmaps;   // the gradients' y record: the fused y + z launch by TMA
 };
 
 int launch_single(const Launch &L, cudaStream_t st);

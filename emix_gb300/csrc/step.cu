@@ -49,8 +49,9 @@ int launch_single(const Launch &L, cudaStream_t st) {
     case LK_DERIV_X:
     case LK_DERIV_YZ:
         if (L.pmaps)
-            return launch_deriv_yz_tma(L.deriv.T, *L.pmaps, L.deriv.axis, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
-                                       L.deriv.F.out, L.deriv.nx, L.deriv.ny, L.deriv.nz, st);
+            return launch_deriv_yz_tma(L.deriv.T, L.deriv.T, *L.pmaps, L.deriv.epi, L.deriv.nf, L.deriv.nf,
+                                       L.deriv.F.in, L.deriv.F.w, L.deriv.F.out, L.deriv.nx, L.deriv.ny,
+                                       L.deriv.nz, st);
         return launch_deriv(L.deriv.T, L.deriv.axis, L.deriv.epi, L.deriv.nf, L.deriv.F.in, L.deriv.F.w,
                             L.deriv.F.out, L.deriv.nx, L.deriv.ny, L.deriv.nz, st);
     case LK_SMAG:
@@ -211,6 +212,18 @@ void build_plan(emix_ctx *c) {
             P.push_back(deriv_launch(c->T[ax], ax, EPI_STORE, 3, in, out, out, nx, ny, nz, CLS_GRADX + ax));
             if (ax == 1) P.back().deriv.pair = 1;
         }
+        {
+            // the y and z records as one launch with its rows by TMA, where
+            // the copy unit's rules hold (closed tables)
+            const double *in[6] = {c->u, c->u + n, c->u + 2 * n, c->u, c->u + n, c->u + 2 * n};
+            double *out[6] = {c->dvel + 3 * n, c->dvel + 4 * n, c->dvel + 5 * n,
+                              c->dvel + 6 * n, c->dvel + 7 * n, c->dvel + 8 * n};
+            const int axes[6] = {1, 1, 1, 2, 2, 2};
+            PencilMaps *pm = &c->pmaps[6 + (s - 1)];
+            if (c->pencil_tma && !c->T[1].periodic && !c->T[2].periodic &&
+                pencil_tma_maps(pm, axes, 6, in, out, out, nx, ny, nz))
+                P[P.size() - 2].pair_pmaps = pm;
+        }
         // SGS viscosity
         if (p.sgs_model == EMIX_SGS_STRUCTURE) {
             const double cutoff = cos(20.0 * atan(1.0) / 45.0);
@@ -251,7 +264,8 @@ void build_plan(emix_ctx *c) {
                 P.push_back(deriv_launch(c->T[ax], ax, EPI_ACCUM, 5, in, wb, out, nx, ny, nz, CLS_DIVX + ax));
                 // rows by TMA where the copy unit's rules hold (closed tables)
                 PencilMaps *pm = &c->pmaps[2 * (s - 1) + (ax - 1)];
-                if (c->pencil_tma && !c->T[ax].periodic && pencil_tma_maps(pm, ax, 5, in, wb, out, nx, ny, nz))
+                const int axes[5] = {ax, ax, ax, ax, ax};
+                if (c->pencil_tma && !c->T[ax].periodic && pencil_tma_maps(pm, axes, 5, in, wb, out, nx, ny, nz))
                     P.back().pmaps = pm;
             }
         }
@@ -336,6 +350,9 @@ int launch_fused(emix_ctx *c, size_t k, cudaStream_t st) {
         double *out[kMaxFields];
         for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
         for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
+        if (L.pair_pmaps)
+            return launch_deriv_yz_tma(a.T, b.T, *L.pair_pmaps, EPI_STORE, a.nf, a.nf + b.nf, in, out, out, a.nx,
+                                       a.ny, a.nz, st);
         return launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, st);
     }
     const FluxArgs &fa = c->plan[k + 1].flux;
@@ -799,7 +816,13 @@ int emix_ctx_set_pencil_tma(emix_ctx *c, int on) {
 int emix_ctx_pencil_tma_launches(emix_ctx *c) {
     if (!c) return -1;
     int k = 0;
-    for (const Launch &L : c->plan) k += (L.kind == LK_DERIV_YZ && L.pmaps) ? 1 : 0;
+    const size_t np = c->plan.size();
+    for (size_t q = 0; q < np; ++q) {
+        const Launch &L = c->plan[q];
+        if (L.kind != LK_DERIV_YZ) continue;
+        if (L.pmaps) ++k;
+        if (L.pair_pmaps && fused_with_next(c, q) == 1) ++k;
+    }
     return k;
 }
 

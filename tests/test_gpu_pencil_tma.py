@@ -1,5 +1,7 @@
-"""The flux divergence's y and z passes with their rows staged by TMA tiled
-copies (emix_ctx_set_pencil_tma) against the same passes with loads: the
+"""The flux divergence's y and z passes and the velocity gradients' fused y
+and z launch with their rows staged by TMA tiled copies
+(emix_ctx_set_pencil_tma, on by default) against the same passes with
+loads: the
 same values bit for bit (the same arithmetic in the same order) in the
 graph-replayed and eager steps, the host-buffer step and the taped forward;
 the fall-back where the copy unit's rules do not hold; and the bounded waits
@@ -28,7 +30,8 @@ def test_tma_rows_give_the_same_bits(emix, shape):
     timeouts = emix.pencil_tma_timeouts()
     w = F.stirred_tank(n=n, nz=nz, impeller=True)
     a, b = _pair(w, bc_walls=1)
-    assert a.pencil_tma_launches() == 6 and b.pencil_tma_launches() == 0
+    # per substep: divergence y, divergence z, gradients y + z
+    assert a.pencil_tma_launches() == 9 and b.pencil_tma_launches() == 0
     for use_graph in (True, False):
         for c in (a, b):
             c.upload(w.um, w.phi)
