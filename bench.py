@@ -579,6 +579,22 @@ def main():
     ms_e2e = max_over_ranks(f0.elapsed_time(f1))
     e2e_value = world * n * args.steps / (ms_e2e * 1e-3) / 1e6
     assert np.isfinite(um_np).all() and np.isfinite(phi_np).all()
+    # the host link this box gives: um's pinned buffer to and from the device
+    dev_um = torch.empty(um_h.shape, dtype=um_h.dtype, device="cuda")
+    link = {}
+    for name, dst, src in (("h2d_gbs", dev_um, um_h), ("d2h_gbs", um_h, dev_um)):
+        best = 1e30
+        for _ in range(3):
+            l0 = torch.cuda.Event(enable_timing=True)
+            l1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                l0.record(stream)
+                dst.copy_(src, non_blocking=True)
+                l1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, l0.elapsed_time(l1))
+        link[name] = round(um_h.numel() * 8 / (best * 1e-3) / 1e9, 1)
+    del dev_um
 
     # ---- per-kernel times (CUDA events around every launch) ----
     prof = ctx.profile(nsteps=max(3, min(args.steps, 10)))
@@ -640,7 +656,8 @@ def main():
         "config": config_dict(w),
         "e2e": {"value": round(e2e_value, 3), "unit": "Mcell-RK3-steps/s",
                 "h2d_bytes_per_step": int(6 * n * 8), "d2h_bytes_per_step": int(6 * n * 8),
-                "api": "emix_step_host (pinned host buffers, H2D um+phi, one step, D2H um+phi)"},
+                "api": "emix_step_host (pinned host buffers, H2D um+phi, one step, D2H um+phi)",
+                "host_link": link},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline,
         "step_roofline": step_roofline,
