@@ -84,9 +84,12 @@ PROTOTYPES = {
                                           C.c_int, C.c_int, vp, vp]),
     "emix_deriv_t_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int,
                                    C.c_int, C.c_int, vp]),
+    "emix_deriv_t_tma_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, vp]),
     "emix_adj_create": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(EmixObjective), C.POINTER(vp)]),
     "emix_adj_destroy": (C.c_int, [vp]),
     "emix_adj_device_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+    "emix_adj_set_overlap": (C.c_int, [vp, C.c_int]),
     "emix_adj_forward": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "emix_adj_backward": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "emix_adj_state_gradient": (C.c_int, [vp, vp, vp]),

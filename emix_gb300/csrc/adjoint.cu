@@ -51,9 +51,20 @@ struct emix_adj {
     // adjoint fields
     double *Lum0, *LA, *LB, *LU0, *LU1, *LP0, *LP1, *LR, *LF, *Ldvel, *Lvis, *T5, *W;
     double *Lphi, *Lphi_prev, *Lphig0, *LphiA, *LphiB, *LD;
+    double *LuW;                     // the level-set stage's velocity adjoint (second stream)
     double *red;                     // [0] dJ/domega, [1] dJ/dCs, [2] J
     emix::DerivTTable TT[3];
     double J = 0.0;
+    // tensor maps of the reverse sweep's y/z D^T passes (rows by TMA while the
+    // context's pencil_tma is on): the divergence's per axis, the gradients'
+    // per axis and target (LU0, LU1); ok where the copy unit's rules hold
+    emix::PencilMaps tdiv[2], tgrad[2][2];
+    bool tdiv_ok[2] = {false, false}, tgrad_ok[2][2] = {{false, false}, {false, false}};
+    // the taped forward's second-stream work (emix_adj_set_overlap)
+    int overlap = 1;
+    cudaEvent_t ev_fork = nullptr, ev_a = nullptr, ev_b = nullptr;
+    // the reverse sweep's level-set adjoints on the second stream
+    cudaEvent_t ev_wfork = nullptr, ev_wdone = nullptr, ev_wfree = nullptr;
 };
 
 namespace emix {
@@ -107,51 +118,84 @@ namespace emix {
 namespace {
 
 // one step with its tape (the launches of the plan, eager, with copies of
-// each substep's inputs)
+// each substep's inputs).  With the context's second stream (a->overlap) the
+// tape copies and the level-set stages run there, overlapped with the flow's
+// kernels: each copy forks after the record that produced its source; the
+// substep's inputs (um0, u, pres, um, the stage's padded phi) and its
+// level-set stage join before its RK update, which overwrites u, pres and um;
+// the gradients, viscosity and divergence join before the next substep's
+// gradients, which overwrite the first of them, or at the step's end.
 int taped_step(emix_adj *a) {
     emix_ctx *c = a->c;
     const long n = c->n;
     cudaStream_t st = c->stream;
+    const bool two = a->overlap && c->side && a->ev_fork;
+    cudaStream_t sd = two ? c->side : st;
+    bool pend_a = false, pend_b = false;
+    // fork the second stream after what the compute stream has issued so far
+    auto fork = [&]() -> int {
+        if (two) {
+            EMIX_CUDA_TRY(cudaEventRecord(a->ev_fork, st));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, a->ev_fork, 0));
+        }
+        return EMIX_OK;
+    };
+    auto done = [&](cudaEvent_t ev, bool &pend) -> int {
+        if (two) {
+            EMIX_CUDA_TRY(cudaEventRecord(ev, sd));
+            pend = true;
+        }
+        return EMIX_OK;
+    };
+    auto join = [&](cudaEvent_t ev, bool &pend) -> int {
+        if (pend) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev, 0));
+            pend = false;
+        }
+        return EMIX_OK;
+    };
     Tape &T = *a->tape;
-    int rc = copy(T.um0, c->um0, 5 * n, st);
-    if (rc) return rc;
+    int rc;
+    if ((rc = fork()) || (rc = copy(T.um0, c->um0, 5 * n, sd)) || (rc = done(a->ev_a, pend_a))) return rc;
     int s = 0;
     const std::vector<Launch> &P = c->plan;
     for (size_t k = 0; k < P.size(); ++k) {
         const Launch &L = P[k];
+        if (L.kind == LK_RK && (rc = join(a->ev_a, pend_a))) return rc;
+        if (L.kind == LK_DERIV_X && L.cls == CLS_GRADX && (rc = join(a->ev_b, pend_b))) return rc;
         if (L.kind == LK_WENO) {
             ++s;
-            if ((rc = copy(T.u[s - 1], c->u, 3 * n, st))) return rc;
-            if ((rc = copy(T.p[s - 1], c->pres, n, st))) return rc;
-            if (s >= 2 && (rc = copy(T.umc[s - 1], c->um, 5 * n, st))) return rc;
-            if (T.phig[s - 1] && (rc = copy(T.phig[s - 1], L.weno.phi, c->ng, st))) return rc;
+            if ((rc = fork())) return rc;
+            if ((rc = copy(T.u[s - 1], c->u, 3 * n, sd))) return rc;
+            if ((rc = copy(T.p[s - 1], c->pres, n, sd))) return rc;
+            if (s >= 2 && (rc = copy(T.umc[s - 1], c->um, 5 * n, sd))) return rc;
+            if (T.phig[s - 1] && (rc = copy(T.phig[s - 1], L.weno.phi, c->ng, sd))) return rc;
+            if ((rc = launch_single(L, sd)) || (rc = done(a->ev_a, pend_a))) return rc;
+            continue;
         }
         // the records the step runs as one launch run as one here too (the
         // same values bit for bit); the tape copies follow the pair
         const int fuse = c->fuse ? plan_fuse_next(P, k) : 0;
         const Launch *last = &L;
-        if (fuse == 1) {
-            const DerivArgs &a = L.deriv, &b = P[k + 1].deriv;
-            const double *in[kMaxFields];
-            double *out[kMaxFields];
-            for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
-            for (int f = 0; f < b.nf; ++f) { in[a.nf + f] = b.F.in[f]; out[a.nf + f] = b.F.out[f]; }
-            if ((rc = launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, st))) return rc;
+        if (fuse) {
+            if ((rc = launch_fused_pair(P, k, st))) return rc;
             last = &P[++k];
-        } else if (fuse == 2) {
-            k_smag_flux<<<cells_grid(P[k + 1].flux.n), 256, 0, st>>>(L.smag, P[k + 1].flux);
-            EMIX_CUDA_TRY(cudaGetLastError());
-            ++k;
         } else if ((rc = launch_single(L, st))) {
             return rc;
         }
         if (L.kind == LK_CLOCK && T.clock && (rc = copy(T.clock, c->clock, kImpClockLen, st))) return rc;
         if (s >= 1) {
-            if (last->cls == CLS_GRADZ && (rc = copy(T.dvel[s - 1], c->dvel, 9 * n, st))) return rc;
-            if (L.kind == LK_SMAG && (rc = copy(T.vis[s - 1], c->vis, n, st))) return rc;
-            if (last->cls == CLS_DIVZ && (rc = copy(T.R[s - 1], c->R, 5 * n, st))) return rc;
+            double *dst = nullptr;
+            const double *src = nullptr;
+            long cnt = 0;
+            if (last->cls == CLS_GRADZ) { dst = T.dvel[s - 1]; src = c->dvel; cnt = 9 * n; }
+            if (L.kind == LK_SMAG) { dst = T.vis[s - 1]; src = c->vis; cnt = n; }
+            if (last->cls == CLS_DIVZ) { dst = T.R[s - 1]; src = c->R; cnt = 5 * n; }
+            if (dst && ((rc = fork()) || (rc = copy(dst, src, cnt, sd)) || (rc = done(a->ev_b, pend_b))))
+                return rc;
         }
     }
+    if ((rc = join(a->ev_a, pend_a)) || (rc = join(a->ev_b, pend_b))) return rc;
     return s == 3 ? EMIX_OK : EMIX_ERR_ARG;
 }
 
@@ -171,6 +215,17 @@ const Launch *plan_weno(emix_ctx *c, int s) {
     return nullptr;
 }
 
+// D^T along y or z of nf fields with rows by TMA: while the context's
+// pencil_tma is on and the pass has fewer pencils than about one resident
+// wave of the device (1024 per SM): there the one-thread-per-pencil loads
+// leave too few warps to hide their latency and the staged rows win; at
+// larger sizes the loads are as fast and the ring's waits cost more.
+bool tma_rows(const emix_adj *a, int ax, int nf) {
+    const emix_params &p = a->c->p;
+    const long np = (long)p.nx * (ax == 1 ? p.nz : p.ny);
+    return a->c->pencil_tma && np * nf < 1024L * device_sms();
+}
+
 // adjoint of the taped step: in a->LA (um0 of the next step) and a->Lphi
 // (phi of the next step); out a->Lum0 and a->Lphi_prev (this step's start)
 int step_adjoint(emix_adj *a) {
@@ -183,6 +238,17 @@ int step_adjoint(emix_adj *a) {
     if ((rc = zero(a->Lum0, 5 * n, st)) || (rc = zero(a->Lphig0, ng, st)) ||
         (rc = zero(a->LphiA, ng, st)) || (rc = zero(a->LphiB, ng, st)))
         return rc;
+    // With the context's second stream (a->overlap) the level-set stages'
+    // adjoints run there, concurrently with the flow's: they chain only
+    // through the phi adjoints and the tape, and stage s's velocity adjoint
+    // goes to LuW, added to the substep's LuIn on the compute stream once both
+    // are done (the next stage waits for that add before reusing LuW).
+    const bool two = a->overlap && c->side && a->ev_wfork;
+    cudaStream_t sw = two ? c->side : st;
+    if (two) {
+        EMIX_CUDA_TRY(cudaEventRecord(a->ev_wfork, st));
+        EMIX_CUDA_TRY(cudaStreamWaitEvent(sw, a->ev_wfork, 0));
+    }
     double *Lo = a->LA, *Lnext = a->LB;          // adjoint of the substep's um output / input
     double *LuOut = nullptr, *LpOut = nullptr;   // adjoint of its u / pres outputs
     double *LuIn = a->LU0, *LpIn = a->LP0;
@@ -191,6 +257,31 @@ int step_adjoint(emix_adj *a) {
         const Launch *Lrk = plan_rk(c, s), *Lw = plan_weno(c, s);
         if (!Lrk || !Lw) return EMIX_ERR_ARG;
         const double *umc = s == 1 ? T.um0 : T.umc[s - 1];
+        // level-set stage s's adjoint: on sw before the flow's (two streams),
+        // else after it on the compute stream, where the flux adjoint has
+        // stored LuIn and the gradients' D^T have accumulated into it
+        auto level_set_stage = [&]() -> int {
+            if (two && s < 3) EMIX_CUDA_TRY(cudaStreamWaitEvent(sw, a->ev_wfree, 0));
+            int r;
+            if ((r = zero(a->LD, 3 * ng, sw))) return r;
+            if (two && (r = zero(a->LuW, 3 * n, sw))) return r;
+            const WenoArgs &wa = Lw->weno;
+            WenoAdjArgs G{};
+            G.phi = T.phig[s - 1] ? T.phig[s - 1] : wa.phi;
+            G.lout = s == 3 ? a->Lphi : (s == 2 ? a->LphiB : a->LphiA);
+            G.lphi0 = a->Lphig0;
+            G.lphiin = s == 1 ? a->Lphig0 : (s == 2 ? a->LphiA : a->LphiB);
+            G.lD = a->LD; G.lu = two ? a->LuW : LuIn; G.vel = T.u[s - 1]; G.wce = wa.wce;
+            G.nxg = wa.nxg; G.nyg = wa.nyg; G.nzg = wa.nzg; G.g = wa.g;
+            for (int d = 0; d < 3; ++d) { G.r0[d] = wa.r0[d]; G.rn[d] = wa.rn[d]; }
+            G.dt = wa.dt; G.stage = s;
+            k_adj_weno<<<grid_n((long)wa.rn[0] * wa.rn[1] * wa.rn[2]), 256, 0, sw>>>(G);
+            k_adj_weno_dphi<<<grid_n(ng), 256, 0, sw>>>(a->LD, G.lphiin, wa.nxg, wa.nyg, wa.nzg);
+            EMIX_CUDA_TRY(cudaGetLastError());
+            if (two) EMIX_CUDA_TRY(cudaEventRecord(a->ev_wdone, sw));
+            return EMIX_OK;
+        };
+        if (two && (rc = level_set_stage())) return rc;
         // RK update
         RkAdjArgs A{};
         A.a = Lrk->rk;
@@ -216,7 +307,8 @@ int step_adjoint(emix_adj *a) {
                 w[m] = a->W + m * n;
                 out[m] = a->LF + (3 * m + ax) * n;
             }
-            if ((rc = launch_deriv_t(a->TT[ax], ax, 0, 5, in, w, out, nx, ny, nz, st))) return rc;
+            const PencilMaps *pm = ax && tma_rows(a, ax, 5) && a->tdiv_ok[ax - 1] ? &a->tdiv[ax - 1] : nullptr;
+            if ((rc = launch_deriv_t(a->TT[ax], ax, 0, 5, in, w, out, nx, ny, nz, st, pm))) return rc;
         }
         // fluxes
         FluxAdjArgs F{};
@@ -239,22 +331,19 @@ int step_adjoint(emix_adj *a) {
                 w[q] = a->W + q * n;
                 out[q] = LuIn + q * n;
             }
-            if ((rc = launch_deriv_t(a->TT[ax], ax, 1, 3, in, w, out, nx, ny, nz, st))) return rc;
+            const int v = LuIn == a->LU0 ? 0 : 1;
+            const PencilMaps *pm =
+                ax && tma_rows(a, ax, 3) && a->tgrad_ok[ax - 1][v] ? &a->tgrad[ax - 1][v] : nullptr;
+            if ((rc = launch_deriv_t(a->TT[ax], ax, 1, 3, in, w, out, nx, ny, nz, st, pm))) return rc;
         }
-        // level-set stage s
-        if ((rc = zero(a->LD, 3 * ng, st))) return rc;
-        const WenoArgs &wa = Lw->weno;
-        WenoAdjArgs G{};
-        G.phi = T.phig[s - 1] ? T.phig[s - 1] : wa.phi;
-        G.lout = s == 3 ? a->Lphi : (s == 2 ? a->LphiB : a->LphiA);
-        G.lphi0 = a->Lphig0;
-        G.lphiin = s == 1 ? a->Lphig0 : (s == 2 ? a->LphiA : a->LphiB);
-        G.lD = a->LD; G.lu = LuIn; G.vel = T.u[s - 1]; G.wce = wa.wce;
-        G.nxg = wa.nxg; G.nyg = wa.nyg; G.nzg = wa.nzg; G.g = wa.g;
-        for (int d = 0; d < 3; ++d) { G.r0[d] = wa.r0[d]; G.rn[d] = wa.rn[d]; }
-        G.dt = wa.dt; G.stage = s;
-        k_adj_weno<<<grid_n((long)wa.rn[0] * wa.rn[1] * wa.rn[2]), 256, 0, st>>>(G);
-        k_adj_weno_dphi<<<grid_n(ng), 256, 0, st>>>(a->LD, G.lphiin, wa.nxg, wa.nyg, wa.nzg);
+        if (!two && (rc = level_set_stage())) return rc;
+        if (two) {
+            // the level-set stage's adjoint has run beside this substep's
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, a->ev_wdone, 0));
+            k_add_into<<<grid_n(3 * n), 256, 0, st>>>(LuIn, a->LuW, 3 * n);
+            EMIX_CUDA_TRY(cudaGetLastError());
+            EMIX_CUDA_TRY(cudaEventRecord(a->ev_wfree, st));
+        }
         // hand over to substep s-1
         LuOut = LuIn; LpOut = LpIn;
         LuIn = LuIn == a->LU0 ? a->LU1 : a->LU0;
@@ -306,6 +395,13 @@ double *take(double *&q, long cnt) {
     double *r = q;
     q += cnt;
     return r;
+}
+
+void destroy_events(emix_adj *a) {
+    for (cudaEvent_t *e : {&a->ev_fork, &a->ev_a, &a->ev_b, &a->ev_wfork, &a->ev_wdone, &a->ev_wfree}) {
+        if (*e) cudaEventDestroy(*e);
+        *e = nullptr;
+    }
 }
 
 // forward steps of one segment: from state `from` (clock clk), storing the
@@ -361,7 +457,7 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     const long cnt = (long)ncp * 6 * n + (long)nseg * 6 * n + 6 * n        // checkpoints, segment, final
                      + (long)ntape * tape_cnt + (keep ? kImpClockLen : 0)  // tapes, final clock
                      + 5 * n * 3 + 3 * n * 2 + n * 2 + 5 * n + 15 * n + 9 * n + n + 5 * n + 6 * n
-                     + 2 * n + 3 * ng + 3 * ng + 8 + 2048;
+                     + 2 * n + 3 * ng + 3 * ng + 3 * n + 8 + 2048;
     a->bytes = (size_t)cnt * sizeof(double);
     if (cudaMalloc(&a->arena, a->bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -399,9 +495,42 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     a->Lphi = take(q, n); a->Lphi_prev = take(q, n);
     a->Lphig0 = take(q, ng); a->LphiA = take(q, ng); a->LphiB = take(q, ng);
     a->LD = take(q, 3 * ng);
+    a->LuW = take(q, 3 * n);
     a->red = take(q, 8 + 2048);   // [0] dJ/domega, [1] dJ/dCs, [2] J, then J's block partials
     a->cp_clock.assign(2 * (size_t)ncp, 0.0);
     a->seg_clock.assign(2 * (size_t)nseg, 0.0);
+    for (int ax = 1; ax <= 2; ++ax) {
+        const int axes[5] = {ax, ax, ax, ax, ax};
+        if (a->TT[ax].periodic) continue;
+        const double *in[5];
+        double *w[5], *o[5];
+        for (int m = 0; m < 5; ++m) {
+            in[m] = a->LR + m * n;
+            w[m] = a->W + m * n;
+            o[m] = a->LF + (3 * m + ax) * n;
+        }
+        a->tdiv_ok[ax - 1] = pencil_tma_maps(&a->tdiv[ax - 1], axes, 5, in, w, o, p.nx, p.ny, p.nz);
+        for (int v = 0; v < 2; ++v) {
+            double *lu = v == 0 ? a->LU0 : a->LU1;
+            for (int q = 0; q < 3; ++q) {
+                in[q] = a->Ldvel + (3 * ax + q) * n;
+                w[q] = a->W + q * n;
+                o[q] = lu + q * n;
+            }
+            a->tgrad_ok[ax - 1][v] = pencil_tma_maps(&a->tgrad[ax - 1][v], axes, 3, in, w, o, p.nx, p.ny, p.nz);
+        }
+    }
+    if (c->side &&
+        (cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&a->ev_a, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&a->ev_b, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&a->ev_wfork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&a->ev_wdone, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&a->ev_wfree, cudaEventDisableTiming) != cudaSuccess)) {
+        // without the events both passes run on the compute stream alone
+        cudaGetLastError();
+        destroy_events(a);
+    }
     *out = a;
     return EMIX_OK;
 }
@@ -409,8 +538,15 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
 int emix_adj_destroy(emix_adj *a) {
     if (!a) return EMIX_ERR_ARG;
     cudaStreamSynchronize(a->c->stream);
+    destroy_events(a);
     cudaFree(a->arena);
     delete a;
+    return EMIX_OK;
+}
+
+int emix_adj_set_overlap(emix_adj *a, int on) {
+    if (!a || on < 0 || on > 1) return EMIX_ERR_ARG;
+    a->overlap = on;
     return EMIX_OK;
 }
 

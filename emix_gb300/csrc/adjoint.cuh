@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "deriv.cuh"
+#include "deriv_tma.cuh"
 #include "impeller.cuh"
 #include "pointwise.cuh"
 #include "weno.cuh"
@@ -18,8 +19,10 @@
 namespace emix {
 
 // out = D^T in (acc = 0) or out += D^T in (acc = 1) along `axis`, for nf <= 6
-// fields; w is scratch of the size of in.
+// fields; w is scratch of the size of in.  With maps (y or z, a closed
+// table) the rows come by TMA through them, the same values bit for bit.
 int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double *const *in,
-                   double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st);
+                   double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st,
+                   const PencilMaps *maps = nullptr);
 
 } // namespace emix

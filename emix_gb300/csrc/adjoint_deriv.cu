@@ -7,7 +7,9 @@
 // from which out_j = sum_k B^T[j][k] z_{j+k-3} is finished as soon as its last
 // z is known (4 operations on the interior rows, where B^T is the
 // antisymmetric 5-point stencil).  The cyclic scheme is anti-self-adjoint (D^T = -D) and uses the
-// forward kernels with a negated table.
+// forward kernels with a negated table.  Given tensor maps, the y and z
+// passes run k_deriv_t_yz_tma (deriv_tma.cu), the same arithmetic on rows
+// staged by TMA.
 #include "adjoint.cuh"
 
 namespace emix {
@@ -208,8 +210,11 @@ __global__ void __launch_bounds__(128) k_deriv_t_x(DerivTTable T, PencilFields F
 } // namespace
 
 int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double *const *in,
-                   double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st) {
+                   double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st,
+                   const PencilMaps *maps) {
     if (nf < 1 || nf > kMaxFields || axis < 0 || axis > 2) return EMIX_ERR_ARG;
+    if (maps && axis != 0 && !T.periodic)
+        return launch_deriv_t_yz_tma(T, *maps, acc, nf, in, w, out, nx, ny, nz, st);
     if (T.periodic) {
         if (!acc) return launch_deriv(T.neg, axis, EPI_STORE, nf, in, w, out, nx, ny, nz, st);
         return launch_deriv(T.neg, axis, EPI_ACCUM, nf, in, w, out, nx, ny, nz, st);
@@ -242,8 +247,10 @@ using namespace emix;
 
 extern "C" {
 
-int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
-                     int nx, int ny, int nz, int accumulate, void *stream) {
+namespace {
+
+int deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h, int nx, int ny, int nz,
+                int accumulate, void *stream, bool tma) {
     const int dims[3] = {nx, ny, nz};
     if (axis < 0 || axis > 2 || nf < 1 || nf > kMaxFields || !out || !in || !(h > 0) || nx < 1 ||
         ny < 1 || nz < 1 || (accumulate != 0 && accumulate != 1))
@@ -251,18 +258,36 @@ int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in
     DerivTTable T;
     int rc = get_deriv_t_table(scheme, dims[axis], h, &T);
     if (rc) return rc;
+    if (tma && (axis == 0 || T.periodic)) return EMIX_ERR_ARG;
     const long n = (long)nx * ny * nz;
     double *scr;
     rc = device_scratch((size_t)nf * n * sizeof(double), &scr);
     if (rc) return rc;
     const double *ins[kMaxFields];
     double *ws[kMaxFields], *outs[kMaxFields];
+    int axes[kMaxFields];
     for (int f = 0; f < nf; ++f) {
         ins[f] = in + f * n;
         ws[f] = scr + f * n;
         outs[f] = out + f * n;
+        axes[f] = axis;
     }
-    return launch_deriv_t(T, axis, accumulate, nf, ins, ws, outs, nx, ny, nz, (cudaStream_t)stream);
+    PencilMaps M;
+    if (tma && !pencil_tma_maps(&M, axes, nf, ins, ws, outs, nx, ny, nz)) return EMIX_ERR_ARG;
+    return launch_deriv_t(T, axis, accumulate, nf, ins, ws, outs, nx, ny, nz, (cudaStream_t)stream,
+                          tma ? &M : nullptr);
+}
+
+} // namespace
+
+int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                     int nx, int ny, int nz, int accumulate, void *stream) {
+    return deriv_t_dev(scheme, axis, nf, out, in, h, nx, ny, nz, accumulate, stream, false);
+}
+
+int emix_deriv_t_tma_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                         int nx, int ny, int nz, int accumulate, void *stream) {
+    return deriv_t_dev(scheme, axis, nf, out, in, h, nx, ny, nz, accumulate, stream, true);
 }
 
 } // extern "C"

@@ -200,6 +200,11 @@ __global__ void __launch_bounds__(256) k_adj_smag(SmagAdjArgs A) {
     block_sum_add(lcs, A.red + 1);
 }
 
+// dst += src over cnt values
+__global__ void k_add_into(double *dst, const double *src, long cnt) {
+    EMIX_FOR_CELLS(q, cnt) dst[q] += src[q];
+}
+
 // ---- primitive variables at the start of the step -----------------------------
 __global__ void k_adj_prim(const double *um0, const double *lu, const double *lp, double inv_m2,
                            double *lum0, long n) {

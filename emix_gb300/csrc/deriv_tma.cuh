@@ -2,8 +2,9 @@
 // (deriv_tma.cu).
 //
 // The y/z derivative (out += D f, the flux divergence's y and z passes, or
-// out = D f, the velocity gradients' y and z passes as one launch) of the
-// load kernels with the same arithmetic, but every row the sweeps read comes
+// out = D f, the velocity gradients' y and z passes as one launch) and its
+// transpose (the adjoint's D^T passes) of the load kernels with the same
+// arithmetic, but every row the sweeps read comes
 // through shared memory: a block of 32, 64 or 128 pencils (lanes along x)
 // has one thread issue 3-D tiled copies of 4 rows x the block's pencils
 // (4 KB at 128) into a ring of three buffers, completion on an mbarrier per
@@ -45,5 +46,12 @@ bool pencil_tma_maps(PencilMaps *M, const int *axis, int nf, const double *const
 int launch_deriv_yz_tma(const DerivTable &Ta, const DerivTable &Tb, const PencilMaps &M, int epi, int nfa, int nf,
                         const double *const *in, double *const *w, double *const *out, int nx, int ny, int nz,
                         cudaStream_t st);
+
+// D^T in along each field's axis (a closed table T), rows staged by TMA
+// through the maps M: out = D^T in (acc = 0) or out += D^T in (acc = 1), with
+// w the forward sweep's buffer; the same values bit for bit as the load
+// kernel of launch_deriv_t.
+int launch_deriv_t_yz_tma(const DerivTTable &T, const PencilMaps &M, int acc, int nf, const double *const *in,
+                          double *const *w, double *const *out, int nx, int ny, int nz, cudaStream_t st);
 
 } // namespace emix

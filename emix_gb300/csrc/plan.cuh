@@ -65,6 +65,10 @@ int launch_single(const Launch &L, cudaStream_t st);
 // gradients' y and z records, 2 Smagorinsky and the fluxes; 0 none
 int plan_fuse_next(const std::vector<Launch> &P, size_t k);
 
+// records k and k+1 as the one launch plan_fuse_next pairs them into (the
+// gradient pair by TMA rows where the y record carries its maps)
+int launch_fused_pair(const std::vector<Launch> &P, size_t k, cudaStream_t st);
+
 // compact filter (filter.cu): filtrado on um[5] in place; the tables are
 // prepared on the host before any stream capture
 int launch_filtrado(double *um, const double *jbn, double cfilt, int nx, int ny, int nz,

@@ -334,18 +334,12 @@ int plan_fuse_next(const std::vector<Launch> &P, size_t k) {
         return 2;
     return 0;
 }
-} // namespace emix
 
-namespace {
-
-int fused_with_next(const emix_ctx *c, size_t k) { return c->fuse ? plan_fuse_next(c->plan, k) : 0; }
-
-// records k and k+1 as the one launch plan_fuse_next pairs them into
-int launch_fused(emix_ctx *c, size_t k, cudaStream_t st) {
-    const Launch &L = c->plan[k];
-    if (plan_fuse_next(c->plan, k) == 1) {
+int launch_fused_pair(const std::vector<Launch> &P, size_t k, cudaStream_t st) {
+    const Launch &L = P[k];
+    if (plan_fuse_next(P, k) == 1) {
         // the gradients' y and z records as one launch
-        const DerivArgs &a = L.deriv, &b = c->plan[k + 1].deriv;
+        const DerivArgs &a = L.deriv, &b = P[k + 1].deriv;
         const double *in[kMaxFields];
         double *out[kMaxFields];
         for (int f = 0; f < a.nf; ++f) { in[f] = a.F.in[f]; out[f] = a.F.out[f]; }
@@ -355,11 +349,18 @@ int launch_fused(emix_ctx *c, size_t k, cudaStream_t st) {
                                        a.ny, a.nz, st);
         return launch_deriv_yz_pair(a.T, b.T, a.nf, b.nf, in, out, a.nx, a.ny, a.nz, st);
     }
-    const FluxArgs &fa = c->plan[k + 1].flux;
+    const FluxArgs &fa = P[k + 1].flux;
     k_smag_flux<<<cells_grid(fa.n), 256, 0, st>>>(L.smag, fa);
     EMIX_CUDA_TRY(cudaGetLastError());
     return EMIX_OK;
 }
+} // namespace emix
+
+namespace {
+
+int fused_with_next(const emix_ctx *c, size_t k) { return c->fuse ? plan_fuse_next(c->plan, k) : 0; }
+
+int launch_fused(emix_ctx *c, size_t k, cudaStream_t st) { return launch_fused_pair(c->plan, k, st); }
 
 int issue_step(emix_ctx *c) {
     const bool fork = (c->overlap & 1) && c->side && !c->prof;

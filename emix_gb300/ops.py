@@ -251,8 +251,9 @@ def impeller_force_dev(um, xyz, imp, t):
     return mask
 
 
-def deriv_t_dev(y, axis: int, h: float, scheme=SCHEME_C, out=None):
-    """D^T y along `axis` (the transpose of deriv_dev); out += D^T y when out is given."""
+def deriv_t_dev(y, axis: int, h: float, scheme=SCHEME_C, out=None, tma=False):
+    """D^T y along `axis` (the transpose of deriv_dev); out += D^T y when out
+    is given.  tma: the y/z form with its rows staged by TMA (the adjoint's)."""
     import torch
     lib = _lib.load()
     nx, ny, nz = _dims(y)
@@ -260,8 +261,9 @@ def deriv_t_dev(y, axis: int, h: float, scheme=SCHEME_C, out=None):
     acc = out is not None
     if out is None:
         out = torch.empty_like(y)
-    check(lib.emix_deriv_t_dev(scheme, axis, nf, _ptr(out), _ptr(y), h, nx, ny, nz, int(acc),
-                               _stream()), "emix_deriv_t_dev")
+    fn, name = ((lib.emix_deriv_t_tma_dev, "emix_deriv_t_tma_dev") if tma
+                else (lib.emix_deriv_t_dev, "emix_deriv_t_dev"))
+    check(fn(scheme, axis, nf, _ptr(out), _ptr(y), h, nx, ny, nz, int(acc), _stream()), name)
     return out
 
 
@@ -717,6 +719,11 @@ class Adjoint:
         check(self.lib.emix_adj_state_gradient(self._h, _ptr(lum), _ptr(lphi)),
               "emix_adj_state_gradient")
         return lum, lphi
+
+    def set_overlap(self, on: bool):
+        """Tape copies and level-set stages of the taped forward on the
+        context's second stream (default) or on the compute stream."""
+        check(self.lib.emix_adj_set_overlap(self._h, int(bool(on))), "emix_adj_set_overlap")
 
     def device_bytes(self) -> int:
         b = C.c_size_t()

@@ -244,6 +244,13 @@ int emix_extrapolate_dev(double *ext, const double *phiS, const double *jbn,
 int emix_deriv_t_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
                      int nx, int ny, int nz, int accumulate, void *stream);
 
+/* emix_deriv_t_dev along y or z (axis 1, 2) with the rows staged by TMA
+ * tiled copies, as the adjoint's reverse sweep runs it: the same values bit
+ * for bit.  EMIX_ERR_ARG where the copy unit's rules do not hold (axis 0,
+ * the cyclic scheme, nx odd, a pointer not 16-byte aligned). */
+int emix_deriv_t_tma_dev(int scheme, int axis, int nf, double *out, const double *in, double h,
+                         int nx, int ny, int nz, int accumulate, void *stream);
+
 /* Sussman reinitialisation of a padded level set: the device form of
  * cuReinitLsJB (src/LevelSet/lsTransportEc.cu:420-676, with
  * reini_RS_WENOJB, src/LevelSet/lsTools.cu:824-902).  phi (in/out), jbn
@@ -577,6 +584,12 @@ int emix_adj_create(emix_ctx *ctx, int nsteps, int every, const emix_objective *
                     emix_adj **adj);
 int emix_adj_destroy(emix_adj *adj);
 int emix_adj_device_bytes(emix_adj *adj, size_t *bytes);
+
+/* 1 (default): the taped forward steps copy their tapes and run the
+ * level-set stages on the context's second stream, overlapped with the
+ * flow's kernels; 0: everything on the compute stream.  The same values bit
+ * for bit either way. */
+int emix_adj_set_overlap(emix_adj *adj, int on);
 
 /* Run nsteps from the context's current state, keeping checkpoints; J out. */
 int emix_adj_forward(emix_adj *adj, double *J);

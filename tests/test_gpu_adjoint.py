@@ -146,6 +146,33 @@ def test_kept_tapes_give_the_recomputed_gradient(emix):
     torch.cuda.synchronize()
 
 
+@pytest.mark.parametrize("every", [0, 1])
+def test_taped_forward_overlap_is_neutral(emix, every):
+    """The taped forward with its tape copies and level-set stages on the
+    second stream (the default) against everything on the compute stream:
+    bit for bit the same J and final state, and the same dJ/d(omega, Cs) and
+    initial-state adjoint to the rounding of the reverse sweep's atomic
+    scatters (a tape copy joined too late, or a stage read before it was
+    written, would show far above that)."""
+    w = _tank_case(n=36)
+    out = []
+    for on in (1, 0):
+        r = _runner(emix, w, 3, every)
+        r.adj.set_overlap(on)
+        J = r.run(1.3, 0.1)
+        g = r.adj.backward()
+        lum, lphi = r.adj.state_gradient()
+        um, phi = r.ctx.download()
+        out.append((J, g, lum.cpu().numpy(), lphi.cpu().numpy(), um, phi))
+        r.close()
+    (J0, g0, l0, p0, u0, f0), (J1, g1, l1, p1, u1, f1) = out
+    assert J0 == J1
+    assert np.array_equal(u0, u1) and np.array_equal(f0, f1)
+    assert abs(g0[0] - g1[0]) <= 1e-14 * abs(g1[0]) and abs(g0[1] - g1[1]) <= 1e-14 * abs(g1[1])
+    assert_close(l0, l1, tol=1e-13, what="lum")
+    assert_close(p0, p1, tol=1e-13, what="lphi")
+
+
 def test_state_gradient_matches_directional_derivative(emix):
     import torch
     w = _tank_case(18)

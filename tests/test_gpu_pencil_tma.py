@@ -1,12 +1,13 @@
 """The flux divergence's y and z passes and the velocity gradients' fused y
 and z launch with their rows staged by TMA tiled copies
 (emix_ctx_set_pencil_tma, on by default) against the same passes with
-loads: the
-same values bit for bit (the same arithmetic in the same order) in the
-graph-replayed and eager steps, the host-buffer step and the taped forward;
-the fall-back where the copy unit's rules do not hold; and the bounded waits
-(copies dropped by a test hook: every block gives up, counts itself, the
-host-buffer step reports EMIX_ERR_TIMEOUT, and the context recovers)."""
+loads: the same values bit for bit (the same arithmetic in the same order) in
+the graph-replayed and eager steps, the host-buffer step and the taped
+forward; the transposed passes of the adjoint's reverse sweep
+(emix_deriv_t_tma_dev) against their load kernel, bit for bit; the fall-back
+where the copy unit's rules do not hold; and the bounded waits (copies
+dropped by a test hook: every block gives up, counts itself, the host-buffer
+step reports EMIX_ERR_TIMEOUT, and the context recovers)."""
 import numpy as np
 import pytest
 
@@ -106,3 +107,67 @@ def test_dropped_row_copies_time_out_and_the_context_recovers(emix):
     assert emix.pencil_tma_timeouts() == after
     a.close()
     b.close()
+
+
+# (nf, nz, ny, nx): pencils of 26 and 9 rows (a partial last chunk, whose
+# accumulation box runs past the end), 130 and 64 rows; blocks of 64, 32, 32, 128
+@pytest.mark.parametrize("shape", [(5, 9, 26, 40), (3, 130, 13, 20), (2, 64, 6, 128), (1, 10, 9, 24)])
+@pytest.mark.parametrize("scheme", [F.SCHEME_A, F.SCHEME_B, F.SCHEME_C])
+def test_transposed_passes_with_tma_rows_give_the_same_bits(emix, shape, scheme):
+    """D^T along y and z (the adjoint's reverse-sweep passes) with rows staged
+    by TMA against the load kernel: the same values bit for bit, storing and
+    accumulating."""
+    import torch
+    timeouts = emix.pencil_tma_timeouts()
+    nf, nz, ny, nx = shape
+    for axis in (1, 2):
+        n = (nx, ny, nz)[axis]
+        h = 1.0 / (n - 1)
+        y = torch.from_numpy(F.uniform(97, axis, shape)).cuda()
+        x = torch.from_numpy(F.uniform(98, axis, shape)).cuda()
+        a = emix.deriv_t_dev(y, axis, h, scheme, tma=True)
+        b = emix.deriv_t_dev(y, axis, h, scheme)
+        assert torch.equal(a, b), (axis, "store")
+        a = x.clone()
+        b = x.clone()
+        emix.deriv_t_dev(y, axis, h, scheme, out=a, tma=True)
+        emix.deriv_t_dev(y, axis, h, scheme, out=b)
+        assert torch.equal(a, b), (axis, "accumulate")
+    torch.cuda.synchronize()
+    assert emix.pencil_tma_timeouts() == timeouts
+
+
+def test_transposed_passes_refuse_where_the_rules_do_not_hold(emix):
+    import torch
+    from emix_gb300 import _lib
+    y = torch.zeros((4, 6, 7), dtype=torch.float64, device="cuda")    # nx = 7: rows not 16-byte aligned
+    with pytest.raises(_lib.EmixError):
+        emix.deriv_t_dev(y, 1, 0.1, F.SCHEME_C, tma=True)
+    y = torch.zeros((4, 6, 8), dtype=torch.float64, device="cuda")
+    with pytest.raises(_lib.EmixError):
+        emix.deriv_t_dev(y, 0, 0.1, F.SCHEME_C, tma=True)                # x pencils: the load kernel's
+    with pytest.raises(_lib.EmixError):
+        emix.deriv_t_dev(y, 1, 1.0 / 6, F.SCHEME_BPER, tma=True)        # the cyclic scheme: D^T = -D
+
+
+def test_transposed_pass_with_dropped_copies_times_out(emix):
+    """Copies left out by the test hook: every block gives up after its
+    bounded wait, counts itself and writes nothing; the next pass is exact."""
+    import torch
+    from emix_gb300 import _lib
+    lib = _lib.load()
+    y = torch.from_numpy(F.uniform(99, 1, (12, 20, 32))).cuda()
+    before = emix.pencil_tma_timeouts()
+    out = torch.full_like(y, 7.0)
+    _lib.check(lib.emix_pencil_tma_test_drop(1), "emix_pencil_tma_test_drop")
+    try:
+        emix.deriv_t_dev(y, 1, 0.05, F.SCHEME_C, out=out, tma=True)
+        torch.cuda.synchronize()
+    finally:
+        _lib.check(lib.emix_pencil_tma_test_drop(0), "emix_pencil_tma_test_drop")
+    assert emix.pencil_tma_timeouts() == before + 12     # one block of 32 pencils per z plane
+    assert bool((out == 7.0).all())
+    a = emix.deriv_t_dev(y, 1, 0.05, F.SCHEME_C, tma=True)
+    b = emix.deriv_t_dev(y, 1, 0.05, F.SCHEME_C)
+    assert torch.equal(a, b)
+    assert emix.pencil_tma_timeouts() == before + 12
