@@ -42,7 +42,7 @@ int launch_single(const Launch &L, cudaStream_t st) {
         k_prim<<<cells_grid(L.prim.n), 256, 0, st>>>(L.prim);
         break;
     case LK_PAD:
-        k_ghost_pad<<<cells_grid(L.pad.ng), 256, 0, st>>>(L.pad);
+        k_ghost_pad<<<cells_grid(L.pad.qend > 0 ? L.pad.qend - L.pad.qbeg : L.pad.ng), 256, 0, st>>>(L.pad);
         break;
     case LK_WENO:
         return launch_weno_stage(L.weno, st, L.tmap);
@@ -534,8 +534,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     const bool down = um_out != nullptr && !due;
     cudaStream_t st = c->stream, sd = c->side;
     constexpr int SI = emix_ctx::kE2eSlabsIn, S = emix_ctx::kE2eSlabs;
-    // events: [0] start, [1] phi in, [2, 2+SI) um slabs in, then S um slabs
-    // final, then S phi slabs final
+    // events: [0] start, [1] unused, [2, 2+SI) phi and um slabs in, then S
+    // um slabs final, then S phi slabs final
     cudaEvent_t *ev = c->e2e_ev, *ev_in = ev + 2, *ev_um = ev + 2 + SI, *ev_phi = ev + 2 + SI + S;
     auto zcut = [nz](int b, int parts) { return (int)((long)nz * b / parts); };
     const size_t db = sizeof(double);
@@ -543,15 +543,12 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     // the side stream's copies follow whatever the context stream holds
     EMIX_CUDA_TRY(cudaEventRecord(ev[0], st));
     EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[0], 0));
-    // upload slabs at least ls_ghost planes deep (the ghost planes mirror
-    // within ls_ghost planes of a face)
+    // upload slabs (phi, then um) at least ls_ghost planes deep (the ghost
+    // planes mirror within ls_ghost planes of a face)
     const int su = up ? (nz / g < SI ? nz / g : SI) : 0;
-    if (up) {
-        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, phi_in, (size_t)n * db, cudaMemcpyHostToDevice, sd));
-        EMIX_CUDA_TRY(cudaEventRecord(ev[1], sd));
-    }
     for (int b = 0; b < su; ++b) {
         const long q0 = plane * zcut(b, su), q1 = plane * zcut(b + 1, su);
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi + q0, phi_in + q0, (size_t)(q1 - q0) * db, cudaMemcpyHostToDevice, sd));
         for (int m = 0; m < 5; ++m)
             EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0 + m * n + q0, um_in + m * n + q0, (size_t)(q1 - q0) * db,
                                           cudaMemcpyHostToDevice, sd));
@@ -564,27 +561,41 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
         const Launch &L = c->plan[k];
         if (up && (k == h.pad || k == h.weno[1])) continue;   // issued with the slabs
         if (up && k == h.prim) {
-            for (int b = 0; b < su; ++b) {
-                const int z0 = zcut(b, su), z1 = zcut(b + 1, su);
-                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[b], 0));
-                Launch Pq = L;
-                Pq.prim.qbeg = plane * z0;
-                Pq.prim.qend = plane * z1;
-                int rc = launch_single(Pq, st);
-                if (!rc && b == 0) {
-                    EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev[1], 0));
-                    rc = launch_single(c->plan[h.pad], st);
-                }
-                // the first level-set stage on the padded planes that mirror
-                // into this slab (with the ghost planes of the end slabs)
+            // per slab: the primitive variables, the padded planes that mirror
+            // into the slab (with the ghost planes of the end slabs), and the
+            // first level-set stage on the previous slab's padded planes,
+            // whose WENO5 reach (3 planes) ends within this slab's
+            const long pg = (long)(p.nx + 2 * g) * (p.ny + 2 * g);
+            auto padded = [&](int b, int &za, int &zb) {
+                za = b == 0 ? 0 : g + zcut(b, su);
+                zb = b == su - 1 ? nz + 2 * g : g + zcut(b + 1, su);
+            };
+            auto stage1 = [&](int b) {
                 Launch Wl = c->plan[h.weno[1]];
-                const int za = b == 0 ? 0 : g + z0, zb = b == su - 1 ? nz + 2 * g : g + z1;
+                int za, zb;
+                padded(b, za, zb);
                 Wl.weno.r0[2] = za;
                 Wl.weno.rn[2] = zb - za;
-                if (!rc) rc = launch_single(Wl, st);
+                return launch_single(Wl, st);
+            };
+            for (int b = 0; b < su; ++b) {
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[b], 0));
+                Launch Pq = L;
+                Pq.prim.qbeg = plane * zcut(b, su);
+                Pq.prim.qend = plane * zcut(b + 1, su);
+                int rc = launch_single(Pq, st);
+                Launch Pd = c->plan[h.pad];
+                int za, zb;
+                padded(b, za, zb);
+                Pd.pad.qbeg = pg * za;
+                Pd.pad.qend = pg * zb;
+                if (!rc) rc = launch_single(Pd, st);
+                if (!rc && b >= 1) rc = stage1(b - 1);
                 if (rc) return rc;
-                launches += 2 + (b == 0);
+                launches += 2 + (b >= 1);
             }
+            if (int rc = stage1(su - 1)) return rc;
+            ++launches;
             continue;
         }
         if (down && k == h.weno[3]) continue;   // issued after the last RK update

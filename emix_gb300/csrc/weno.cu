@@ -16,7 +16,8 @@ __global__ void k_weno_scales(const double *__restrict__ jbn, double *__restrict
 }
 
 __global__ void k_ghost_pad(PadArgs a) {
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < a.ng; q += (long)gridDim.x * blockDim.x)
+    const long end = a.qend > 0 ? a.qend : a.ng;
+    for (long q = a.qbeg + blockIdx.x * (long)blockDim.x + threadIdx.x; q < end; q += (long)gridDim.x * blockDim.x)
         pad_cell(a, q);
 }
 

@@ -53,6 +53,7 @@ struct PadArgs {
     double dir;
     int nx, ny, nz;
     long ng;
+    long qbeg, qend;   // k_ghost_pad: padded cells [qbeg, qend) only (qend = 0: all)
 };
 __global__ void k_ghost_pad(PadArgs a);
 __global__ void k_ghost_unpad(double *__restrict__ val, const double *__restrict__ ghost, int g,
