@@ -22,6 +22,7 @@ def main(argv=None):
                     help="run each standalone device operator once (after a warm-up pass)")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--grids", type=int, default=48, help="ensemble: the first N grids of the 48-grid draw")
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--no-level-set", action="store_true")
     ap.add_argument("--walls", action="store_true", help="frontera wall conditions every substep")
@@ -37,7 +38,7 @@ def main(argv=None):
         operators(a.n)
         return 0
     if a.workload == "ensemble":
-        b = ops.Batch(F.ensemble(ngrids=48, seed=7))
+        b = ops.Batch(F.ensemble(ngrids=a.grids, seed=7))
         b.upload()
         t0 = time.perf_counter()
         b.step(a.steps, use_graph=a.graph)
@@ -45,7 +46,7 @@ def main(argv=None):
         sec = time.perf_counter() - t0
         um = b.download(0)[0]
         ok = bool(np.isfinite(um).all())
-        print(f"ensemble of 48 grids ({b.ncell} cells): {a.steps} batched steps in {sec:.3f} s, "
+        print(f"ensemble of {a.grids} grids ({b.ncell} cells): {a.steps} batched steps in {sec:.3f} s, "
               f"finite={ok}")
         b.close()
         return 0 if ok else 1
