@@ -195,13 +195,30 @@ __global__ void __launch_bounds__(128) k_deriv_t_x(DerivTTable T, PencilFields F
         __syncwarp();
         // out rows [c0 + 3, c0 + cl + 3) (from row 0 in the last chunk), below n
         const int js = c0 == 0 ? 0 : c0 + 3, je = min(c0 + cl + 3, n);
-        for (int q = 0; q < npw; ++q) {
-            for (int j = js + lane; j < je; j += 32) {
-                double v = tile[q * kXLd + j - c0];
-                double *o = out + (long)q * n + j;
-                if (ACC) v += *o;
-                *o = v;
+        if (ACC) {
+            // the targets of eight pencils loaded before any is stored, so
+            // their loads are in flight together
+            const int j = js + lane;
+            const bool in1 = j < je;
+            for (int q0 = 0; q0 < npw; q0 += 8) {
+                double old[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    old[k] = in1 && q0 + k < npw ? out[(long)(q0 + k) * n + j] : 0.0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (in1 && q0 + k < npw)
+                        out[(long)(q0 + k) * n + j] = tile[(q0 + k) * kXLd + j - c0] + old[k];
             }
+            // the last chunk's rows past the first 32 of its range
+            for (int q = 0; q < npw; ++q)
+                for (int jj = j + 32; jj < je; jj += 32) {
+                    double *o = out + (long)q * n + jj;
+                    *o = tile[q * kXLd + jj - c0] + *o;
+                }
+        } else {
+            for (int q = 0; q < npw; ++q)
+                for (int j = js + lane; j < je; j += 32) out[(long)q * n + j] = tile[q * kXLd + j - c0];
         }
         __syncwarp();
     }

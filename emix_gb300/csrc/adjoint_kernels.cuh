@@ -186,15 +186,17 @@ __global__ void __launch_bounds__(256) k_adj_smag(SmagAdjArgs A) {
     for (long q0 = blockIdx.x * (long)blockDim.x; q0 < n; q0 += (long)gridDim.x * blockDim.x) {
         const long q = q0 + threadIdx.x;
         if (q < n) {
-            double dv[9], ldv[9];
+            // the targets loaded with the inputs, not after the arithmetic
+            double dv[9], ldv[9], old[9];
             for (int c = 0; c < 9; ++c) {
                 dv[c] = A.dvel[c * n + q];
+                old[c] = A.ldvel[c * n + q];
                 ldv[c] = 0.0;
             }
             lcs += smag_adj(dv, A.jbn[q], A.jbn[4 * n + q], A.jbn[8 * n + q], A.cs, A.dxyz[q], A.lvis[q],
                             ldv);
             for (int c = 0; c < 9; ++c)
-                if (ldv[c] != 0.0) A.ldvel[c * n + q] += ldv[c];
+                if (ldv[c] != 0.0) A.ldvel[c * n + q] = old[c] + ldv[c];
         }
     }
     block_sum_add(lcs, A.red + 1);
