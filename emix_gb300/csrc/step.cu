@@ -544,10 +544,12 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     EMIX_CUDA_TRY(cudaEventRecord(ev[0], st));
     EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, ev[0], 0));
     // upload slabs (phi, then um) at least ls_ghost planes deep (the ghost
-    // planes mirror within ls_ghost planes of a face)
-    const int su = up ? (nz / g < SI ? nz / g : SI) : 0;
+    // planes mirror within ls_ghost planes of a face); the first half as deep
+    // as the others, since nothing computes before it lands
+    const int su = up ? ((nz / g + 1) / 2 < SI ? (nz / g + 1) / 2 : SI) : 0;
+    auto zin = [nz, su](int b) { return b == 0 ? 0 : (int)((long)nz * (2 * b - 1) / (2 * su - 1)); };
     for (int b = 0; b < su; ++b) {
-        const long q0 = plane * zcut(b, su), q1 = plane * zcut(b + 1, su);
+        const long q0 = plane * zin(b), q1 = plane * zin(b + 1);
         EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi + q0, phi_in + q0, (size_t)(q1 - q0) * db, cudaMemcpyHostToDevice, sd));
         for (int m = 0; m < 5; ++m)
             EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0 + m * n + q0, um_in + m * n + q0, (size_t)(q1 - q0) * db,
@@ -567,8 +569,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
             // whose WENO5 reach (3 planes) ends within this slab's
             const long pg = (long)(p.nx + 2 * g) * (p.ny + 2 * g);
             auto padded = [&](int b, int &za, int &zb) {
-                za = b == 0 ? 0 : g + zcut(b, su);
-                zb = b == su - 1 ? nz + 2 * g : g + zcut(b + 1, su);
+                za = b == 0 ? 0 : g + zin(b);
+                zb = b == su - 1 ? nz + 2 * g : g + zin(b + 1);
             };
             auto stage1 = [&](int b) {
                 Launch Wl = c->plan[h.weno[1]];
@@ -581,8 +583,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
             for (int b = 0; b < su; ++b) {
                 EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[b], 0));
                 Launch Pq = L;
-                Pq.prim.qbeg = plane * zcut(b, su);
-                Pq.prim.qend = plane * zcut(b + 1, su);
+                Pq.prim.qbeg = plane * zin(b);
+                Pq.prim.qend = plane * zin(b + 1);
                 int rc = launch_single(Pq, st);
                 Launch Pd = c->plan[h.pad];
                 int za, zb;
