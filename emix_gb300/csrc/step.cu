@@ -558,6 +558,9 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     }
 
     int launches = 0;
+    const bool fork = (c->overlap & 1) && !c->prof, gfork = (c->overlap & 2) && !c->prof;
+    int fs = 0, gs = 0;
+    bool joined = true, gjoined = true;
     const long np = (long)c->plan.size();
     for (long k = 0; k < np; ++k) {
         const Launch &L = c->plan[k];
@@ -601,6 +604,38 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
             continue;
         }
         if (down && k == h.weno[3]) continue;   // issued after the last RK update
+        // the graph-replayed step's concurrency (issue_step) for the records
+        // issued here one by one: the x gradients and the level-set stages
+        // not sliced with the copies run on the second stream, joined before
+        // the records that overwrite what they read
+        if (gfork && L.kind == LK_DERIV_X && L.cls == CLS_GRADX && gs < 3) {
+            EMIX_CUDA_TRY(cudaEventRecord(c->gfork_ev[gs], st));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, c->gfork_ev[gs], 0));
+            if (int rc = launch_single(L, sd)) return rc;
+            EMIX_CUDA_TRY(cudaEventRecord(c->gjoin_ev[gs], sd));
+            gjoined = false;
+            ++gs;
+            ++launches;
+            continue;
+        }
+        if (!gjoined && L.cls != CLS_GRADY && L.cls != CLS_GRADZ) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, c->gjoin_ev[gs - 1], 0));
+            gjoined = true;
+        }
+        if (fork && L.kind == LK_WENO && fs < 3) {
+            EMIX_CUDA_TRY(cudaEventRecord(c->fork_ev[fs], st));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(sd, c->fork_ev[fs], 0));
+            if (int rc = launch_single(L, sd)) return rc;
+            EMIX_CUDA_TRY(cudaEventRecord(c->join_ev[fs], sd));
+            joined = false;
+            ++fs;
+            ++launches;
+            continue;
+        }
+        if (!joined && L.kind == LK_RK) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, c->join_ev[fs - 1], 0));
+            joined = true;
+        }
         if (down && k == (h.rkf3 >= 0 ? h.rkf3 : h.rk3))
             // the velocity the last level-set stage reads, kept in W (free
             // after the last divergence) before the update overwrites it
@@ -644,6 +679,8 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
         k += fuse ? 1 : 0;
         ++launches;
     }
+    if (!joined) EMIX_CUDA_TRY(cudaStreamWaitEvent(st, c->join_ev[fs - 1], 0));
+    if (!gjoined) EMIX_CUDA_TRY(cudaStreamWaitEvent(st, c->gjoin_ev[gs - 1], 0));
     c->launches = launches;
     if (due) {
         int rc = c->fgexec ? (cudaGraphLaunch(c->fgexec, st) == cudaSuccess ? EMIX_OK : EMIX_ERR_CUDA)
