@@ -165,6 +165,7 @@ PROTOTYPES = {
                                          C.POINTER(C.c_int)]),
     "emix_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
     "emix_batch_set_pcr": (C.c_int, [vp, C.c_int]),
+    "emix_batch_set_overlap": (C.c_int, [vp, C.c_int]),
     "emix_batch_get_pcr": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "emix_batch_pcr_positions": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "emix_batch_autotune_pcr_ms": (C.c_int, [vp, C.POINTER(C.c_double)]),

@@ -219,6 +219,11 @@ struct emix_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int sms = 1;       // SMs of the device, set at creation
+    // concurrency inside a step (emix_batch_set_overlap): bit 0 the level-set
+    // positions, bit 1 the x-gradient positions on the second stream
+    int overlap = 3;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev[6] = {}, join_ev[6] = {};
     // ms per step the last autotune measured: [0] the best Thomas shapes,
     // [k] the same with k PCR steps in the y/z positions (-1: not measured)
     double pcr_ms[kPcrMaxSteps + 1] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
@@ -432,11 +437,13 @@ int ctas(const emix_batch *b, long total) {
     return (int)(c < 1 ? 1 : c);
 }
 
-int issue(emix_batch *b) {
+// position k on stream st (with the next one where they run as one launch);
+// *used: the positions it covered
+int launch_pos(emix_batch *b, size_t k, cudaStream_t st, size_t *used) {
     const int G = (int)b->grids.size();
-    cudaStream_t st = b->stream;
     const size_t npos = b->pos.size();
-    for (size_t k = 0; k < npos; ++k) {
+    *used = 1;
+    {
         const BatchPos &P = b->pos[k];
         if (P.fuse && k + 1 < npos) {
             const BatchPos &Q = b->pos[k + 1];
@@ -447,8 +454,9 @@ int issue(emix_batch *b) {
                 k_batch_smag_flux<<<ctas(b, Q.total), 256, 0, st>>>((const SmagArgs *)P.args,
                                                                    (const FluxArgs *)Q.args, Q.start, G,
                                                                    b->tune.cpb);
-            ++k;
-            continue;
+            *used = 2;
+            EMIX_CUDA_TRY(cudaGetLastError());
+            return EMIX_OK;
         }
         const int nb = ctas(b, P.total);
         switch (P.kind) {
@@ -508,11 +516,59 @@ int issue(emix_batch *b) {
     return EMIX_OK;
 }
 
+// one step: the positions in order on the batch's stream; with the second
+// stream, the level-set positions there joined before the next RK update
+// (which overwrites the velocity they read), the x-gradient positions joined
+// before the first position after the gradients' y and z
+int issue(emix_batch *b) {
+    cudaStream_t st = b->stream;
+    const bool fork = (b->overlap & 1) && b->side, gfork = (b->overlap & 2) && b->side;
+    const size_t npos = b->pos.size();
+    int ne = 0;   // events used
+    int wjoin = -1, gjoin = -1;   // pending joins (event index)
+    for (size_t k = 0; k < npos;) {
+        const BatchPos &P = b->pos[k];
+        const bool w = fork && P.kind == LK_WENO, gx = gfork && P.kind == LK_DERIV_X && P.cls == CLS_GRADX;
+        if (gjoin >= 0 && P.cls != CLS_GRADY && P.cls != CLS_GRADZ) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, b->join_ev[gjoin], 0));
+            gjoin = -1;
+        }
+        if (wjoin >= 0 && P.kind == LK_RK) {
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(st, b->join_ev[wjoin], 0));
+            wjoin = -1;
+        }
+        size_t used = 1;
+        if ((w || gx) && ne < 6) {
+            EMIX_CUDA_TRY(cudaEventRecord(b->fork_ev[ne], st));
+            EMIX_CUDA_TRY(cudaStreamWaitEvent(b->side, b->fork_ev[ne], 0));
+            if (int rc = launch_pos(b, k, b->side, &used)) return rc;
+            EMIX_CUDA_TRY(cudaEventRecord(b->join_ev[ne], b->side));
+            (w ? wjoin : gjoin) = ne++;
+        } else if (int rc = launch_pos(b, k, st, &used)) {
+            return rc;
+        }
+        k += used;
+    }
+    if (wjoin >= 0) EMIX_CUDA_TRY(cudaStreamWaitEvent(st, b->join_ev[wjoin], 0));
+    if (gjoin >= 0) EMIX_CUDA_TRY(cudaStreamWaitEvent(st, b->join_ev[gjoin], 0));
+    return EMIX_OK;
+}
+
 void drop_graph(emix_batch *b) {
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->graph) cudaGraphDestroy(b->graph);
     b->gexec = nullptr;
     b->graph = nullptr;
+}
+
+void destroy_side(emix_batch *b) {
+    for (int e = 0; e < 6; ++e) {
+        if (b->fork_ev[e]) cudaEventDestroy(b->fork_ev[e]);
+        if (b->join_ev[e]) cudaEventDestroy(b->join_ev[e]);
+        b->fork_ev[e] = b->join_ev[e] = nullptr;
+    }
+    if (b->side) cudaStreamDestroy(b->side);
+    b->side = nullptr;
 }
 
 int step_impl(emix_batch *b, int nsteps, int use_graph) {
@@ -589,6 +645,15 @@ int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
     }
     b->stream = b->own;
     for (emix_ctx *c : b->grids) emix_ctx_set_stream(c, b->stream);
+    // the second stream of the step's concurrency (without it, one stream)
+    bool ok = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) == cudaSuccess;
+    for (int e = 0; e < 6 && ok; ++e)
+        ok = cudaEventCreateWithFlags(&b->fork_ev[e], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->join_ev[e], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        destroy_side(b);
+    }
     *out = b;
     return EMIX_OK;
 }
@@ -599,6 +664,7 @@ int emix_batch_destroy(emix_batch *b) {
     drop_graph(b);
     for (emix_ctx *c : b->grids) emix_ctx_destroy(c);
     if (b->dmem) cudaFree(b->dmem);
+    destroy_side(b);
     if (b->own) cudaStreamDestroy(b->own);
     delete b;
     return EMIX_OK;
@@ -648,6 +714,14 @@ int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, i
     if (cells_per_thread) *cells_per_thread = b->tune.cpb;
     if (yz_block) *yz_block = b->tune.yz_bs;
     if (ctas_per_sm) *ctas_per_sm = b->tune.ctas_sm;
+    return EMIX_OK;
+}
+
+int emix_batch_set_overlap(emix_batch *b, int mode) {
+    if (!b || mode < 0 || mode > 3) return EMIX_ERR_ARG;
+    EMIX_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->overlap = mode;
+    drop_graph(b);
     return EMIX_OK;
 }
 

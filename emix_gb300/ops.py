@@ -640,6 +640,11 @@ class Batch:
         self.upload()
         return ms.value
 
+    def set_overlap(self, mode: int):
+        """Concurrency inside a batched step: 0 one stream, bit 0 the level-set
+        positions, bit 1 the x-gradient positions on a second stream (3: both)."""
+        check(self.lib.emix_batch_set_overlap(self._h, int(mode)), "emix_batch_set_overlap")
+
     def set_pcr(self, steps: int):
         """PCR steps (2..5) of the y/z pencil positions, 0 for Thomas sweeps."""
         check(self.lib.emix_batch_set_pcr(self._h, steps), "emix_batch_set_pcr")

@@ -522,6 +522,12 @@ int emix_batch_get_tuning(emix_batch *b, int *cells_per_thread, int *yz_block, i
  * positions that run by PCR.  The gradients' y and z positions then run as
  * two launches. */
 int emix_batch_set_pcr(emix_batch *b, int steps);
+
+/* Concurrency inside a batched step, as emix_ctx_set_overlap: bit 0 the
+ * level-set positions, bit 1 the x-gradient positions on a second stream
+ * (3, the default: both; 0: one stream).  The same values bit for bit in
+ * every mode. */
+int emix_batch_set_overlap(emix_batch *b, int mode);
 int emix_batch_get_pcr(emix_batch *b, int *steps);
 int emix_batch_pcr_positions(emix_batch *b, int *count);
 

@@ -35,6 +35,25 @@ def test_batched_equals_per_grid(emix, sgs):
     b.close()
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batched_overlap_modes_give_the_same_bits(emix, use_graph):
+    """The level-set and x-gradient positions on the second stream (every
+    overlap mode) against one stream: bit for bit the same fields."""
+    ws = _grids(1)
+    b = emix.Batch(ws)
+    out = {}
+    for mode in (0, 1, 2, 3):
+        b.upload()
+        b.set_overlap(mode)
+        b.step(3, use_graph=use_graph)
+        out[mode] = [b.download(g) for g in range(len(ws))]
+    for mode in (1, 2, 3):
+        for g in range(len(ws)):
+            assert np.array_equal(out[mode][g][0], out[0][g][0]), (mode, g, "um")
+            assert np.array_equal(out[mode][g][1], out[0][g][1]), (mode, g, "phi")
+    b.close()
+
+
 def test_batched_grid_matches_oracle(emix, oracle):
     ws = _grids(1)
     b = emix.Batch(ws)
