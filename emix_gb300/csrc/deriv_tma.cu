@@ -418,6 +418,21 @@ bool pencil_tma_maps(PencilMaps *M, const int *axis, int nf, const double *const
         const int wv = ((nx + b - 1) / b) * b - nx;
         if (wv < waste) { width = b; waste = wv; }
     }
+    // a launch of fewer than 8 blocks per SM (small grids) is spread evenly
+    // instead: the width that gives the most loaded SM the fewest pencil
+    // slots (its blocks, ceil(blocks / SMs), times the width), the wider on
+    // a tie
+    int nother = 0;
+    for (int f = 0; f < nf; ++f) nother = max(nother, axis[f] == 1 ? nz : ny);
+    const long sms = device_sms();
+    if ((long)((nx + width - 1) / width) * nother * nf < 8 * sms) {
+        long best = 0;
+        for (int b : {128, 64, 32}) {
+            const long blocks = (long)((nx + b - 1) / b) * nother * nf;
+            const long slots = (blocks + sms - 1) / sms * b;
+            if (b == 128 || slots < best) { width = b; best = slots; }
+        }
+    }
     const cuuint32_t estride[3] = {1, 1, 1};
     std::memset(M, 0, sizeof *M);
     for (int f = 0; f < nf; ++f) {

@@ -25,7 +25,9 @@ def _pair(w, **kw):
     return a, b
 
 
-@pytest.mark.parametrize("shape", [(24, 24), (40, 26), (130, 20), (128, 10)])   # blocks of 32, 64, 32, 128
+# blocks of 32 (small launches spread evenly), 64, 32, 32, and 128 (a launch
+# of more than 8 blocks per SM: the width that idles the fewest lanes)
+@pytest.mark.parametrize("shape", [(24, 24), (40, 26), (130, 20), (128, 10), (256, 24)])
 def test_tma_rows_give_the_same_bits(emix, shape):
     n, nz = shape
     timeouts = emix.pencil_tma_timeouts()
@@ -110,8 +112,10 @@ def test_dropped_row_copies_time_out_and_the_context_recovers(emix):
 
 
 # (nf, nz, ny, nx): pencils of 26 and 9 rows (a partial last chunk, whose
-# accumulation box runs past the end), 130 and 64 rows; blocks of 64, 32, 32, 128
-@pytest.mark.parametrize("shape", [(5, 9, 26, 40), (3, 130, 13, 20), (2, 64, 6, 128), (1, 10, 9, 24)])
+# accumulation box runs past the end), 130 and 64 rows, in blocks of 32; and
+# launches of more than 8 blocks per SM along y, in blocks of 128 and 64
+@pytest.mark.parametrize("shape", [(5, 9, 26, 40), (3, 130, 13, 20), (2, 64, 6, 128), (1, 10, 9, 24),
+                                   (1, 640, 8, 256), (1, 416, 10, 192)])
 @pytest.mark.parametrize("scheme", [F.SCHEME_A, F.SCHEME_B, F.SCHEME_C])
 def test_transposed_passes_with_tma_rows_give_the_same_bits(emix, shape, scheme):
     """D^T along y and z (the adjoint's reverse-sweep passes) with rows staged
