@@ -245,10 +245,13 @@ int launch_deriv_t(const DerivTTable &T, int axis, int acc, int nf, const double
     const long np = axis == 0 ? (long)ny * nz : (axis == 1 ? (long)nx * nz : (long)nx * ny);
     dim3 grid((unsigned)((np + 127) / 128), nf);
     if (axis == 0) {
-        // four warps of 32 pencils per block, one staging tile per warp
-        const size_t shm = 4 * kXTile * sizeof(double);
-        if (acc) k_deriv_t_x<1><<<grid, 128, shm, st>>>(T, F, np);
-        else k_deriv_t_x<0><<<grid, 128, shm, st>>>(T, F, np);
+        // warps of 32 pencils (four per block, fewer for small launches,
+        // x_warps), one staging tile per warp
+        const int warps = x_warps(np, nf);
+        const dim3 gx((unsigned)((np + 32 * warps - 1) / (32 * warps)), nf);
+        const size_t shm = warps * kXTile * sizeof(double);
+        if (acc) k_deriv_t_x<1><<<gx, 32 * warps, shm, st>>>(T, F, np);
+        else k_deriv_t_x<0><<<gx, 32 * warps, shm, st>>>(T, F, np);
     } else if (acc) {
         k_deriv_t<1><<<grid, 128, 0, st>>>(T, F, axis, nx, ny, nz);
     } else {

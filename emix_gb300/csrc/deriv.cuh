@@ -314,6 +314,23 @@ constexpr int kXRows = 34;          // 32 rows + 2 look-ahead
 constexpr int kXLd = kXRows + 1;    // padded leading dimension (odd: no bank conflicts)
 constexpr int kXTile = 32 * kXLd;
 
+// warps per block (4, 2 or 1) of an x-pencil launch over np pencils of nf
+// fields: 4, unless that gives fewer than 8 blocks per SM (small grids); then
+// the count that gives the most loaded SM the fewest warps (its blocks,
+// ceil(blocks / SMs), times the warps), the larger on a tie
+inline int x_warps(long np, int nf) {
+    const long sms = device_sms();
+    auto blocks = [&](int w) { return (np + 32L * w - 1) / (32L * w) * nf; };
+    if (blocks(4) >= 8 * sms) return 4;
+    int best = 4;
+    long load = (blocks(4) + sms - 1) / sms * 4;
+    for (int w : {2, 1}) {
+        const long l = (blocks(w) + sms - 1) / sms * w;
+        if (l < load) { best = w; load = l; }
+    }
+    return best;
+}
+
 // Body for one (virtual) block of `nwarps` warps: bid = (pencil group, -, field).
 template <int EPI>
 EMIX_DEV void deriv_x_body(const DerivTable &T, const PencilFields &F, long npencil, uint3 bid,

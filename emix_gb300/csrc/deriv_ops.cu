@@ -63,7 +63,7 @@ int launch_deriv(const DerivTable &T, int axis, int epi, int nf, const double *c
     }
     if (axis == 0) {
         const long np = (long)ny * nz;
-        const int warps = 4;
+        const int warps = x_warps(np, nf);
         const long blocks = (np + 32 * warps - 1) / (32 * warps);
         const size_t shm = (size_t)warps * kXTile * sizeof(double);
         dim3 grid((unsigned)blocks, 1, nf);
