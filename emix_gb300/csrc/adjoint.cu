@@ -39,11 +39,11 @@ struct emix_adj {
     double *arena = nullptr;
     size_t bytes = 0;
     double *cp = nullptr;            // checkpoints: (nsteps/every + 1) x 6n
-    std::vector<double> cp_clock;    // impeller clock (t0, k) of each checkpoint
+    double *cp_clock = nullptr;      // impeller clock (t0, k) of each checkpoint (device)
     double *seg = nullptr;           // states of one segment: every x 6n
-    std::vector<double> seg_clock;
+    double *seg_clock = nullptr;
     double *final_state = nullptr;   // 6n, restored after the reverse sweep
-    double final_clock[2] = {0, 0};
+    double *final_clock = nullptr;   // 2
     // tape of the step being differentiated (tapes[k] in the keep mode)
     Tape *tape = nullptr;
     std::vector<Tape> tapes;
@@ -74,17 +74,16 @@ int grid_n(long n) { return grid_cap(n, 8); }
 
 bool has_clock(const emix_ctx *c) { return c->clock != nullptr; }
 
-// state of the context <-> a 6n buffer (um0, phi) plus the clock head
+// state of the context <-> a 6n buffer (um0, phi) plus the clock head (2
+// values), all on the device and in stream order
 int save_state(emix_adj *a, double *dst, double *clk) {
     emix_ctx *c = a->c;
     const long n = c->n;
     cudaStream_t st = c->stream;
     EMIX_CUDA_TRY(cudaMemcpyAsync(dst, c->um0, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     EMIX_CUDA_TRY(cudaMemcpyAsync(dst + 5 * n, c->phi, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    if (has_clock(c)) {
-        EMIX_CUDA_TRY(cudaMemcpyAsync(clk, c->clock, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        EMIX_CUDA_TRY(cudaStreamSynchronize(st));
-    }
+    if (has_clock(c))
+        EMIX_CUDA_TRY(cudaMemcpyAsync(clk, c->clock, 2 * sizeof(double), cudaMemcpyDeviceToDevice, st));
     return EMIX_OK;
 }
 
@@ -94,10 +93,8 @@ int load_state(emix_adj *a, const double *src, const double *clk) {
     cudaStream_t st = c->stream;
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->um0, src, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     EMIX_CUDA_TRY(cudaMemcpyAsync(c->phi, src + 5 * n, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    if (has_clock(c)) {
-        EMIX_CUDA_TRY(cudaMemcpyAsync(c->clock, clk, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
-        EMIX_CUDA_TRY(cudaStreamSynchronize(st));
-    }
+    if (has_clock(c))
+        EMIX_CUDA_TRY(cudaMemcpyAsync(c->clock, clk, 2 * sizeof(double), cudaMemcpyDeviceToDevice, st));
     return EMIX_OK;
 }
 
@@ -406,12 +403,12 @@ void destroy_events(emix_adj *a) {
 
 // forward steps of one segment: from state `from` (clock clk), storing the
 // state before each step into `store` (when not null)
-int run_steps(emix_adj *a, int nsteps, double *store, std::vector<double> *store_clk, int first) {
+int run_steps(emix_adj *a, int nsteps, double *store, double *store_clk, int first) {
     emix_ctx *c = a->c;
     const long n = c->n;
     for (int k = 0; k < nsteps; ++k) {
         if (store) {
-            int rc = save_state(a, store + (long)(first + k) * 6 * n, store_clk->data() + 2 * (first + k));
+            int rc = save_state(a, store + (long)(first + k) * 6 * n, store_clk + 2 * (first + k));
             if (rc) return rc;
         }
         int rc = emix_step(c, 1, 1);
@@ -457,7 +454,8 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     const long cnt = (long)ncp * 6 * n + (long)nseg * 6 * n + 6 * n        // checkpoints, segment, final
                      + (long)ntape * tape_cnt + (keep ? kImpClockLen : 0)  // tapes, final clock
                      + 5 * n * 3 + 3 * n * 2 + n * 2 + 5 * n + 15 * n + 9 * n + n + 5 * n + 6 * n
-                     + 2 * n + 3 * ng + 3 * ng + 3 * n + 8 + 2048;
+                     + 2 * n + 3 * ng + 3 * ng + 3 * n + 8 + 2048
+                     + 2 * (long)ncp + 2 * (long)nseg + 2;                 // checkpoint clocks
     a->bytes = (size_t)cnt * sizeof(double);
     if (cudaMalloc(&a->arena, a->bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -497,8 +495,9 @@ int emix_adj_create(emix_ctx *c, int nsteps, int every, const emix_objective *ob
     a->LD = take(q, 3 * ng);
     a->LuW = take(q, 3 * n);
     a->red = take(q, 8 + 2048);   // [0] dJ/domega, [1] dJ/dCs, [2] J, then J's block partials
-    a->cp_clock.assign(2 * (size_t)ncp, 0.0);
-    a->seg_clock.assign(2 * (size_t)nseg, 0.0);
+    a->cp_clock = take(q, 2 * (long)ncp);
+    a->seg_clock = take(q, 2 * (long)nseg);
+    a->final_clock = take(q, 2);
     for (int ax = 1; ax <= 2; ++ax) {
         const int axes[5] = {ax, ax, ax, ax, ax};
         if (a->TT[ax].periodic) continue;
@@ -576,7 +575,7 @@ int emix_adj_forward(emix_adj *a, double *J) {
     // checkpoints every `every` steps from the context's current state
     for (int k = 0; k < a->nsteps; k += a->every) {
         const int cpi = k / a->every;
-        if ((rc = save_state(a, a->cp + (long)cpi * 6 * a->c->n, a->cp_clock.data() + 2 * cpi))) return rc;
+        if ((rc = save_state(a, a->cp + (long)cpi * 6 * a->c->n, a->cp_clock + 2 * cpi))) return rc;
         const int m = k + a->every <= a->nsteps ? a->every : a->nsteps - k;
         if ((rc = run_steps(a, m, nullptr, nullptr, 0))) return rc;
     }
@@ -613,11 +612,11 @@ int emix_adj_backward(emix_adj *a, double *dJ) {
         const int first = cpi * a->every;
         const int m = first + a->every <= a->nsteps ? a->every : a->nsteps - first;
         // states before each step of the segment
-        if ((rc = load_state(a, a->cp + (long)cpi * 6 * n, a->cp_clock.data() + 2 * cpi))) return rc;
-        if ((rc = run_steps(a, m - 1, a->seg, &a->seg_clock, 0))) return rc;
-        if ((rc = save_state(a, a->seg + (long)(m - 1) * 6 * n, a->seg_clock.data() + 2 * (m - 1)))) return rc;
+        if ((rc = load_state(a, a->cp + (long)cpi * 6 * n, a->cp_clock + 2 * cpi))) return rc;
+        if ((rc = run_steps(a, m - 1, a->seg, a->seg_clock, 0))) return rc;
+        if ((rc = save_state(a, a->seg + (long)(m - 1) * 6 * n, a->seg_clock + 2 * (m - 1)))) return rc;
         for (int k = m - 1; k >= 0; --k) {
-            if ((rc = load_state(a, a->seg + (long)k * 6 * n, a->seg_clock.data() + 2 * k))) return rc;
+            if ((rc = load_state(a, a->seg + (long)k * 6 * n, a->seg_clock + 2 * k))) return rc;
             if ((rc = taped_step(a))) return rc;
             if ((rc = step_adjoint(a))) return rc;
             // the step's input adjoint becomes the previous step's output adjoint
