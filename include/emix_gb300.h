@@ -456,14 +456,16 @@ int emix_ctx_set_time(emix_ctx *ctx, double t0);
 int emix_ctx_get_time(emix_ctx *ctx, double *t);
 
 /* End-to-end form: copy um/phi from host, advance nsteps, copy back;
- * synchronous.  The copies back overlap the last step where its results are
- * final early (phi after the last level-set stage, um by z-slabs of the last
- * RK update, on a second stream); page-locked host buffers let them run
- * asynchronously.  The values are those of emix_step, bit for bit.  Returns
- * EMIX_ERR_TIMEOUT when a level-set stage block gave up waiting for its TMA
- * plane copies during the call (its cells of phi are then unwritten).
- * emix_step and the other device-pointer forms return before their kernels
- * finish: their callers poll emix_weno_tma_timeouts instead. */
+ * synchronous.  The uploads (phi and um by z-slabs, on a second stream)
+ * overlap the first step's primitive variables, ghost padding and first
+ * level-set stage; the copies back overlap the last step where its results
+ * are final early (phi after the last level-set stage, um by z-slabs of the
+ * last RK update); page-locked host buffers let them run asynchronously.  The
+ * values are those of emix_step, bit for bit.  Returns EMIX_ERR_TIMEOUT when
+ * a level-set stage block or a y/z pencil block gave up waiting for its TMA
+ * copies during the call (its cells are then unwritten).  emix_step and the
+ * other device-pointer forms return before their kernels finish: their
+ * callers poll emix_weno_tma_timeouts and emix_pencil_tma_timeouts instead. */
 int emix_step_host(emix_ctx *ctx, double *um, double *phi, int nsteps);
 
 /* Number of kernel launches one step issues (for accounting; the records
