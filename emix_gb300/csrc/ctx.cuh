@@ -65,8 +65,11 @@ struct emix_ctx {
     // (issue_step_host, step.cu): the uploads and the copies back on `side`,
     // overlapped with the step by z-slabs; the events it orders them with
     static constexpr int kE2eSlabsIn = 8, kE2eSlabs = 4;
-    static constexpr int kE2eEvents = 2 + kE2eSlabsIn + 2 * kE2eSlabs;
+    static constexpr int kE2eEvents = 2 + kE2eSlabsIn + 2 * kE2eSlabs + kE2eSlabsIn + 2;
     cudaEvent_t e2e_ev[kE2eEvents] = {};
+    // the first level-set stage's slabs alternate between these two streams,
+    // so that one slab's last wave overlaps the next slab's first
+    cudaStream_t slab_st[2] = {};
 };
 
 namespace emix {

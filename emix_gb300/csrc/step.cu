@@ -535,8 +535,10 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
     cudaStream_t st = c->stream, sd = c->side;
     constexpr int SI = emix_ctx::kE2eSlabsIn, S = emix_ctx::kE2eSlabs;
     // events: [0] start, [1] unused, [2, 2+SI) phi and um slabs in, then S
-    // um slabs final, then S phi slabs final
+    // um slabs final, then S phi slabs final, then SI slabs padded, then the
+    // two slab streams done
     cudaEvent_t *ev = c->e2e_ev, *ev_in = ev + 2, *ev_um = ev + 2 + SI, *ev_phi = ev + 2 + SI + S;
+    cudaEvent_t *ev_pad = ev + 2 + SI + 2 * S, *ev_slab = ev_pad + SI;
     auto zcut = [nz](int b, int parts) { return (int)((long)nz * b / parts); };
     const size_t db = sizeof(double);
 
@@ -575,13 +577,19 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
                 za = b == 0 ? 0 : g + zin(b);
                 zb = b == su - 1 ? nz + 2 * g : g + zin(b + 1);
             };
-            auto stage1 = [&](int b) {
+            // the stage's slabs alternate between two streams, each after
+            // the padding of the slab above it (and so after everything the
+            // context stream issued before), and join the context stream
+            // after the last
+            auto stage1 = [&](int b, cudaEvent_t after) -> int {
                 Launch Wl = c->plan[h.weno[1]];
                 int za, zb;
                 padded(b, za, zb);
                 Wl.weno.r0[2] = za;
                 Wl.weno.rn[2] = zb - za;
-                return launch_single(Wl, st);
+                cudaStream_t x = c->slab_st[b & 1];
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(x, after, 0));
+                return launch_single(Wl, x);
             };
             for (int b = 0; b < su; ++b) {
                 EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[b], 0));
@@ -595,12 +603,17 @@ int step_host_one(emix_ctx *c, const double *um_in, const double *phi_in, double
                 Pd.pad.qbeg = pg * za;
                 Pd.pad.qend = pg * zb;
                 if (!rc) rc = launch_single(Pd, st);
-                if (!rc && b >= 1) rc = stage1(b - 1);
                 if (rc) return rc;
+                EMIX_CUDA_TRY(cudaEventRecord(ev_pad[b], st));
+                if (b >= 1 && (rc = stage1(b - 1, ev_pad[b]))) return rc;
                 launches += 2 + (b >= 1);
             }
-            if (int rc = stage1(su - 1)) return rc;
+            if (int rc = stage1(su - 1, ev_pad[su - 1])) return rc;
             ++launches;
+            for (int x = 0; x < 2; ++x) {
+                EMIX_CUDA_TRY(cudaEventRecord(ev_slab[x], c->slab_st[x]));
+                EMIX_CUDA_TRY(cudaStreamWaitEvent(st, ev_slab[x], 0));
+            }
             continue;
         }
         if (down && k == h.weno[3]) continue;   // issued after the last RK update
@@ -837,6 +850,8 @@ int emix_ctx_destroy(emix_ctx *c) {
     for (cudaEvent_t e : c->e2e_ev) {
         if (e) cudaEventDestroy(e);
     }
+    for (cudaStream_t x : c->slab_st)
+        if (x) cudaStreamDestroy(x);
     if (c->side) cudaStreamDestroy(c->side);
     cudaFree(c->arena);
     delete c;
@@ -1047,6 +1062,8 @@ static int step_host_run(emix_ctx *c, double *um, double *phi, int nsteps) {
     }
     for (cudaEvent_t &e : c->e2e_ev)
         if (!e) EMIX_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaStream_t &x : c->slab_st)
+        if (!x) EMIX_CUDA_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
     // the first step takes the uploads, the last the copies back, the steps
     // between (if any) replay the graph
     int rc;
