@@ -222,8 +222,9 @@ struct emix_batch {
     // concurrency inside a step (emix_batch_set_overlap): bit 0 the level-set
     // positions, bit 1 the x-gradient positions on the second stream
     int overlap = 3;
+    static constexpr int kForks = 6;   // per step: 3 level-set + 3 x-gradient positions
     cudaStream_t side = nullptr;
-    cudaEvent_t fork_ev[6] = {}, join_ev[6] = {};
+    cudaEvent_t fork_ev[kForks] = {}, join_ev[kForks] = {};
     // ms per step the last autotune measured: [0] the best Thomas shapes,
     // [k] the same with k PCR steps in the y/z positions (-1: not measured)
     double pcr_ms[kPcrMaxSteps + 1] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
@@ -538,7 +539,7 @@ int issue(emix_batch *b) {
             wjoin = -1;
         }
         size_t used = 1;
-        if ((w || gx) && ne < 6) {
+        if ((w || gx) && ne < emix_batch::kForks) {
             EMIX_CUDA_TRY(cudaEventRecord(b->fork_ev[ne], st));
             EMIX_CUDA_TRY(cudaStreamWaitEvent(b->side, b->fork_ev[ne], 0));
             if (int rc = launch_pos(b, k, b->side, &used)) return rc;
@@ -562,7 +563,7 @@ void drop_graph(emix_batch *b) {
 }
 
 void destroy_side(emix_batch *b) {
-    for (int e = 0; e < 6; ++e) {
+    for (int e = 0; e < emix_batch::kForks; ++e) {
         if (b->fork_ev[e]) cudaEventDestroy(b->fork_ev[e]);
         if (b->join_ev[e]) cudaEventDestroy(b->join_ev[e]);
         b->fork_ev[e] = b->join_ev[e] = nullptr;
@@ -647,7 +648,7 @@ int emix_batch_create(int ngrid, const emix_params *params, emix_batch **out) {
     for (emix_ctx *c : b->grids) emix_ctx_set_stream(c, b->stream);
     // the second stream of the step's concurrency (without it, one stream)
     bool ok = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) == cudaSuccess;
-    for (int e = 0; e < 6 && ok; ++e)
+    for (int e = 0; e < emix_batch::kForks && ok; ++e)
         ok = cudaEventCreateWithFlags(&b->fork_ev[e], cudaEventDisableTiming) == cudaSuccess &&
              cudaEventCreateWithFlags(&b->join_ev[e], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
