@@ -80,3 +80,12 @@ def test_argument_errors_without_gpu(lib):
     prm.ls_ghost = 2       # fewer ghost layers than the WENO5 stencil needs
     assert lib.emix_ctx_create(C.byref(prm), C.byref(h)) == ERR_ARG
     assert lib.emix_step(None, 1, 0) == ERR_ARG
+    # the adjoint's and the batch's stream switches, the TMA form of D^T and
+    # the pencil copies' test hook: argument checks before any CUDA call
+    assert lib.emix_adj_set_overlap(None, 1) == ERR_ARG
+    assert lib.emix_batch_set_overlap(None, 3) == ERR_ARG
+    assert lib.emix_deriv_t_tma_dev(3, 1, 7, p, p, 0.1, 8, 8, 8, 0, None) == ERR_ARG
+    assert lib.emix_deriv_t_tma_dev(3, 1, 1, p, p, 0.1, 8, 8, 8, 2, None) == ERR_ARG
+    assert lib.emix_deriv_t_tma_dev(3, 1, 1, p, p, -0.1, 8, 8, 8, 0, None) == ERR_ARG
+    assert lib.emix_pencil_tma_test_drop(2) == ERR_ARG
+    assert lib.emix_weno_tma_test_drop(2) == ERR_ARG
