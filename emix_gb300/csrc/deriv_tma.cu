@@ -114,14 +114,19 @@ EMIX_DEV void box_origin(int axis, int o, int row, int &c1, int &c2) {
 }
 
 // One block's pencils (B consecutive x, one per thread) of one field along
-// `axis`: table T, forward-sweep buffer w, output out (EPI_STORE: w = out),
-// rows brought through the ring R.  Copy numbers run over both sweeps: the
-// forward sweep's copy of chunk c (rows 4c .. 4c+3) is number c, the
-// backward sweep's copy of chunk C-1-q is number C+q.
-template <int B, int EPI>
+// `axis`: table T, input in (read directly only for the cyclic wrap),
+// forward-sweep buffer w, output out (EPI_STORE: w = out), rows brought
+// through the ring R.  Copy numbers run over both sweeps: the forward sweep's
+// copy of chunk c (rows 4c .. 4c+3) is number c, the backward sweep's copy of
+// chunk C-1-q is number C+q.  CYC: the cyclic operator (the load kernels'
+// deriv_yz_accum / deriv_yz_body periodic path, row for row): every row a
+// stencil row, the window wrapping round the pencil, rows [0, ku) summing
+// the Sherman-Morrison y0, the correction fact zz_i on rows outside
+// [zlo, zhi) of the backward sweep.
+template <int B, int EPI, bool CYC>
 EMIX_DEV void tma_pencils(const CUtensorMap *mi, const CUtensorMap *mw, const CUtensorMap *mo,
-                          const DerivTable &T, double *w, double *out, bool live, int x0, int o, int axis,
-                          long s, PencilRing<B> &R) {
+                          const DerivTable &T, const double *in, double *w, double *out, bool live, int x0,
+                          int o, int axis, long s, PencilRing<B> &R) {
     constexpr int kBuf = PencilRing<B>::kBuf;
     const int tid = threadIdx.x;
     const int n = T.n, C = (n + kPtR - 1) / kPtR;
@@ -144,7 +149,45 @@ EMIX_DEV void tma_pencils(const CUtensorMap *mi, const CUtensorMap *mw, const CU
     // ---- forward sweep ----
     if (!R.wait(0)) { R.give_up(0); return; }
     const double h0 = buf[tid], h1 = buf[B + tid], h2 = buf[2 * B + tid], h3 = buf[3 * B + tid];
-    double up = 0.0;
+    double up = 0.0, fact = 0.0;
+    if constexpr (CYC) {
+        // f_{n-2}, f_{n-1} by plain loads, f_n = f_0 and f_{n+1} = f_1 from
+        // the first chunk
+        double fm2 = in[(n - 2) * s], fm1 = in[(n - 1) * s], f0 = h0, fp1 = h1;
+        const int ku = T.ku < n ? T.ku : n;
+        double y0 = 0.0;
+        int cur = 0;
+        for (int i = 0; i < n; ++i) {
+            const int j = i + 2;
+            double fp2;
+            if (j < n) {
+                const int c = j / kPtR;
+                if (c != cur) {
+                    if (!R.wait(c)) { R.give_up(c); return; }
+                    if (cur + kPtS < C) R.refill(cur + kPtS, issue_in);
+                    cur = c;
+                }
+                fp2 = buf[(c % kPtS) * kBuf + (j - c * kPtR) * B + tid];
+            } else {
+                fp2 = j == n ? h0 : h1;
+            }
+            double v;
+            if (EPI == EPI_ACCUM) {
+                const DerivRowU r = T.urows[i];
+                const double t = fma(r.c, fp2 - fm2, fp1 - fm1);
+                v = t - r.mu * up;
+                if (i < ku) y0 += T.u0s[i] * v;
+            } else {
+                const DerivRow r = T.rows[i];
+                v = r.A * (fp1 - fm1) + r.B * (fp2 - fm2) - r.m * up;
+                if (i < ku) y0 += T.u0[i] * v;
+            }
+            if (live) w[i * s] = v;
+            up = v;
+            fm2 = fm1; fm1 = f0; f0 = fp1; fp1 = fp2;
+        }
+        fact = (y0 + (EPI == EPI_ACCUM ? T.sm1s : T.sm1) * up) * T.sm2;
+    } else {
     // closure rows 0, 1 on f_0..f_3 (the table builder guarantees nlo == 2)
     for (int i = 0; i < T.nlo; ++i) {
         const double *c = T.clo + 4 * i;
@@ -188,6 +231,7 @@ EMIX_DEV void tma_pencils(const CUtensorMap *mi, const CUtensorMap *mw, const CU
         if (live) w[i * s] = v;
         up = v;
     }
+    }
     // the stores of w must be visible to the copy unit's reads below
     asm volatile("fence.proxy.async.global;" ::: "memory");
     __syncthreads();
@@ -209,11 +253,15 @@ EMIX_DEV void tma_pencils(const CUtensorMap *mi, const CUtensorMap *mw, const CU
                 const DerivRowU r = T.urows[i];
                 const double z = wi - r.gu * zn;
                 zn = z;
-                if (live) out[i * s] = fma(r.k, z, oi);
+                double acc = oi;
+                if (CYC && (i >= T.zhi || i < T.zlo)) acc = oi - fact * T.zz[i];
+                if (live) out[i * s] = fma(r.k, z, acc);
             } else {
                 const double y = wi - T.rows[i].g * zn;
                 zn = y;
-                if (live) out[i * s] = y;
+                double xv = y;
+                if (CYC && (i >= T.zhi || i < T.zlo)) xv = y - fact * T.zz[i];
+                if (live) out[i * s] = xv;
             }
         }
     }
@@ -358,7 +406,7 @@ EMIX_DEV void tma_pencils_t(const CUtensorMap *mi, const CUtensorMap *mw, const 
 // grid (ceil(nx / B), max of the fields' other extents, nf), B threads.
 // Fields [0, nfa) run with table Ta, the rest with Tb, each along its map's
 // axis.
-template <int B, int EPI>
+template <int B, int EPI, bool CYC>
 __global__ void __launch_bounds__(B)
 k_deriv_yz_tma(const __grid_constant__ PencilMaps M, const DerivTable Ta, const DerivTable Tb,
                const PencilFields F, int nfa, int nx, int ny, int nz) {
@@ -373,13 +421,14 @@ k_deriv_yz_tma(const __grid_constant__ PencilMaps M, const DerivTable Ta, const 
     const int x0 = blockIdx.x * B, x = x0 + (int)threadIdx.x;
     const bool live = x < nx;
     const long off = (long)(live ? x : 0) + (long)o * os;
+    const double *in = pick(F.in, f) + off;
     double *w = pick(F.w, f) + off;
     double *out = pick(F.out, f) + off;
     PencilRing<B> R{buf, bar, s_ok, g_pencil_tma_drop == 0};
     if (f < nfa)
-        tma_pencils<B, EPI>(&M.in[f], &M.w[f], &M.out[f], Ta, w, out, live, x0, o, axis, s, R);
+        tma_pencils<B, EPI, CYC>(&M.in[f], &M.w[f], &M.out[f], Ta, in, w, out, live, x0, o, axis, s, R);
     else
-        tma_pencils<B, EPI>(&M.in[f], &M.w[f], &M.out[f], Tb, w, out, live, x0, o, axis, s, R);
+        tma_pencils<B, EPI, CYC>(&M.in[f], &M.w[f], &M.out[f], Tb, in, w, out, live, x0, o, axis, s, R);
 }
 
 // D^T of nf fields along their maps' axes (one table), the same grid
@@ -456,11 +505,14 @@ int launch_deriv_yz_tma(const DerivTable &Ta, const DerivTable &Tb, const Pencil
                         const double *const *in, double *const *w, double *const *out, int nx, int ny, int nz,
                         cudaStream_t st) {
     if (nf < 1 || nf > kMaxFields || nfa < 0 || nfa > nf || (epi != EPI_STORE && epi != EPI_ACCUM)) return EMIX_ERR_ARG;
+    // one launch is all closed or all cyclic tables
+    const bool cyc = (nfa > 0 ? Ta : Tb).periodic != 0;
     int nother = 0;
     for (int f = 0; f < nf; ++f) {
         const DerivTable &T = f < nfa ? Ta : Tb;
         const int ax = M.axis[f];
-        if ((ax != 1 && ax != 2) || T.periodic || T.nlo != 2 || T.nhi != 2 || T.n != (ax == 1 ? ny : nz))
+        if ((ax != 1 && ax != 2) || (T.periodic != 0) != cyc || (!cyc && (T.nlo != 2 || T.nhi != 2)) ||
+            T.n != (ax == 1 ? ny : nz))
             return EMIX_ERR_ARG;
         nother = max(nother, ax == 1 ? nz : ny);
     }
@@ -473,18 +525,21 @@ int launch_deriv_yz_tma(const DerivTable &Ta, const DerivTable &Tb, const Pencil
     }
     const int B = M.width;
     const dim3 grid((nx + B - 1) / B, nother, nf);
-#define EMIX_TMA_LAUNCH(BW)                                                                         \
-    if (B == BW) {                                                                                  \
+#define EMIX_TMA_LAUNCH(BW, CY)                                                                     \
+    if (B == BW && cyc == CY) {                                                                     \
         if (epi == EPI_ACCUM)                                                                       \
-            k_deriv_yz_tma<BW, EPI_ACCUM><<<grid, BW, 0, st>>>(M, Ta, Tb, F, nfa, nx, ny, nz);      \
+            k_deriv_yz_tma<BW, EPI_ACCUM, CY><<<grid, BW, 0, st>>>(M, Ta, Tb, F, nfa, nx, ny, nz);  \
         else                                                                                        \
-            k_deriv_yz_tma<BW, EPI_STORE><<<grid, BW, 0, st>>>(M, Ta, Tb, F, nfa, nx, ny, nz);      \
+            k_deriv_yz_tma<BW, EPI_STORE, CY><<<grid, BW, 0, st>>>(M, Ta, Tb, F, nfa, nx, ny, nz);  \
         EMIX_CUDA_TRY(cudaGetLastError());                                                          \
         return EMIX_OK;                                                                             \
     }
-    EMIX_TMA_LAUNCH(128)
-    EMIX_TMA_LAUNCH(64)
-    EMIX_TMA_LAUNCH(32)
+    EMIX_TMA_LAUNCH(128, false)
+    EMIX_TMA_LAUNCH(64, false)
+    EMIX_TMA_LAUNCH(32, false)
+    EMIX_TMA_LAUNCH(128, true)
+    EMIX_TMA_LAUNCH(64, true)
+    EMIX_TMA_LAUNCH(32, true)
 #undef EMIX_TMA_LAUNCH
     return EMIX_ERR_ARG;
 }

@@ -39,10 +39,10 @@ struct PencilMaps {
 bool pencil_tma_maps(PencilMaps *M, const int *axis, int nf, const double *const *in, double *const *w,
                      double *const *out, int nx, int ny, int nz);
 
-// D in along each field's axis for closed (non-cyclic) tables, rows staged
-// by TMA through the maps M: out += D in (EPI_ACCUM) or out = D in
-// (EPI_STORE, w = out); fields [0, nfa) with table Ta, the rest with Tb
-// (fields as in launch_deriv).
+// D in along each field's axis, rows staged by TMA through the maps M:
+// out += D in (EPI_ACCUM) or out = D in (EPI_STORE, w = out); fields [0, nfa)
+// with table Ta, the rest with Tb (fields as in launch_deriv), the tables
+// all closed or all cyclic.
 int launch_deriv_yz_tma(const DerivTable &Ta, const DerivTable &Tb, const PencilMaps &M, int epi, int nfa, int nf,
                         const double *const *in, double *const *w, double *const *out, int nx, int ny, int nz,
                         cudaStream_t st);

@@ -1,5 +1,6 @@
 """The flux divergence's y and z passes and the velocity gradients' fused y
-and z launch with their rows staged by TMA tiled copies
+and z launch (closed and cyclic schemes) with their rows staged by TMA tiled
+copies
 (emix_ctx_set_pencil_tma, on by default) against the same passes with
 loads: the same values bit for bit (the same arithmetic in the same order) in
 the graph-replayed and eager steps, the host-buffer step and the taped
@@ -55,16 +56,47 @@ def test_tma_rows_give_the_same_bits(emix, shape):
     assert emix.pencil_tma_timeouts() == timeouts
 
 
+@pytest.mark.parametrize("case", ["tgv128", "box256x64x64"])
+def test_cyclic_tma_rows_give_the_same_bits(emix, case):
+    """The cyclic scheme (periodic boxes) with rows staged by TMA (launches of
+    at least 2^16 pencils): the wrap rows, the Sherman-Morrison sum and
+    correction as in the load kernels, bit for bit, in graph-replayed and
+    eager steps."""
+    if case == "tgv128":
+        w = F.taylor_green(128)
+    else:
+        w = F.random_box(256, 64, 64, periodic=True)
+    timeouts = emix.pencil_tma_timeouts()
+    a, b = _pair(w, level_set=False)
+    assert a.pencil_tma_launches() == 9 and b.pencil_tma_launches() == 0
+    for use_graph in (True, False):
+        for c in (a, b):
+            c.upload(w.um, w.phi)
+            c.step(3, use_graph=use_graph)
+        assert np.array_equal(a.download()[0], b.download()[0])
+    a.close()
+    b.close()
+    assert emix.pencil_tma_timeouts() == timeouts
+
+
 def test_tma_rows_fall_back_where_the_rules_do_not_hold(emix):
     from emix_gb300 import ops
     odd = ops.Context(F.stirred_tank(n=23, nz=20, impeller=True), bc_walls=1)
     odd.set_pencil_tma(True)
     assert odd.pencil_tma_launches() == 0     # nx odd: rows not 16-byte aligned
     odd.close()
-    per = ops.Context(F.taylor_green(16))
-    per.set_pencil_tma(True)
-    assert per.pencil_tma_launches() == 0     # the cyclic scheme keeps its loads
-    per.close()
+    small = ops.Context(F.taylor_green(24))
+    small.set_pencil_tma(True)
+    assert small.pencil_tma_launches() == 0   # cyclic launches of fewer than 2^16 pencils
+    small.close()
+    wm = F.random_box(256, 64, 64)
+    wm.schemes = (F.SCHEME_C, F.SCHEME_BPER, F.SCHEME_C)
+    mixed = ops.Context(wm)
+    mixed.set_pencil_tma(True)
+    # y cyclic, z closed: the divergence's y and z passes by TMA, the fused
+    # gradient pair (one launch of both tables) keeps its loads
+    assert mixed.pencil_tma_launches() == 6
+    mixed.close()
 
 
 def test_taped_forward_with_tma_rows(emix):
